@@ -1,0 +1,264 @@
+"""Host-side mirror of the reference's per-frequency interface, over the C ABI.
+
+Same names, argument meaning and error behaviour as the reference's surface
+(claytonotey/bem):
+
+  GreensFunction(eps, mu, omega, bExternal)   src/GreensFunction.h:7-28, .cpp:17-30
+  Options()                                   src/Options.h, src/Options.cpp:3-27
+  Zts(t, s, g, options)                       src/Impedance.h:21
+  CalcHeatTransfer(a, eV, T1, T2, top, s, t, options)   src/HeatTransfer.h:33
+  Theta(omega, T)                             src/HeatTransfer.cpp:3-6
+  FrequencySweep(file).f                      src/FrequencySweep.h:8-12
+  parseShapes(...) -> (top, s, t)             src/HeatTransfer.cpp:61-109 (with the
+                                              trees kept alive, which the reference's
+                                              by-value out-parameters do not do)
+
+All compute runs in libbemgpu.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import threading
+
+import numpy as np
+
+from . import _lib
+from .mesh import Body, two_body
+
+HBAR = 1.05457148e-34   # src/util/SI.cpp:3-9
+KB = 1.3806503e-23
+EV = 1.60217646e-19
+C0 = 2.99792458e8
+
+
+def _check(rc: int, ctx=None):
+    if rc != _lib.OK:
+        msg = _lib.load().bemgpu_ctx_last_error(ctx.handle if ctx else None).decode()
+        raise _lib.BemGpuError(rc, msg)
+
+
+class Context:
+    """One CUDA device, its stream and workspace (bemgpu_ctx_t)."""
+
+    def __init__(self, device: int = 0):
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = L.bemgpu_ctx_create(int(device), ctypes.byref(h))
+        if rc != _lib.OK:
+            raise _lib.BemGpuError(rc, f"cannot create a context on CUDA device {device}")
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            _lib.load().bemgpu_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+_ctx_lock = threading.Lock()
+
+
+def default_context() -> Context:
+    global _default_ctx
+    with _ctx_lock:
+        if _default_ctx is None:
+            _default_ctx = Context(0)
+        return _default_ctx
+
+
+class Options:
+    """Options fields on the fill path (src/Options.cpp:23-26 defaults)."""
+
+    def __init__(self):
+        self.farThresh6 = 12.0
+        self.farThresh10 = 8.0
+        self.farThresh15 = 4.0
+        self.farThresh21 = 2.0
+        self.minSegmentSize = 32
+
+    def _c(self) -> _lib.Options:
+        return _lib.Options(self.farThresh6, self.farThresh10, self.farThresh15, self.farThresh21)
+
+
+class GreensFunction:
+    """GreensFunction(eps, mu, omega, bExternal); init() recomputes the constants."""
+
+    def __init__(self, eps=1.0, mu=1.0, omega=0.0, bExternal: bool = False):
+        self.bExternal = bool(bExternal)
+        self.init(eps, mu, omega)
+
+    def init(self, eps, mu, omega):
+        g = _lib.Green()
+        e = (ctypes.c_double * 2)(complex(eps).real, complex(eps).imag)
+        m = (ctypes.c_double * 2)(complex(mu).real, complex(mu).imag)
+        w = (ctypes.c_double * 2)(complex(omega).real, complex(omega).imag)
+        _check(_lib.load().bemgpu_green_init(e, m, w, int(self.bExternal), ctypes.byref(g)))
+        self._g = g
+        c = lambda a: complex(a[0], a[1])
+        self.eps, self.mu, self.omega = c(g.eps), c(g.mu), c(g.omega)
+        self.ksquared, self.k, self.ik, self.k2 = c(g.ksquared), c(g.k), c(g.ik), c(g.k2)
+        self.Zeps, self.Zmu = c(g.Zeps), c(g.Zmu)
+        self.normk = abs(self.k)
+
+    def isExternal(self) -> bool:
+        return self.bExternal
+
+
+class FixedLorentz:
+    """Single Lorentz oscillator with SiC::eps's form (src/util/SiC.cpp:16-19),
+    parameters in eV and independent of temperature."""
+
+    def __init__(self, epsinf: float, wTO_eV: float, wLO_eV: float, gamma_eV: float):
+        self.epsinf = epsinf
+        self.wT = wTO_eV * EV / HBAR
+        self.wL = wLO_eV * EV / HBAR
+        self.gamma = gamma_eV * EV / HBAR
+
+    def setTemperature(self, T: float):
+        pass
+
+    def eps(self, feV: float) -> complex:
+        w = feV * EV / HBAR
+        return self.epsinf * (self.wL * self.wL - w * w - 1j * self.gamma * w) / (
+            self.wT * self.wT - w * w - 1j * self.gamma * w)
+
+    def mu(self, feV: float) -> complex:
+        return 1.0 + 0j
+
+
+class SiC(FixedLorentz):
+    """Temperature-dependent SiC (src/util/SiC.cpp:4-14)."""
+
+    def __init__(self):
+        self.setTemperature(300.0)
+
+    def setTemperature(self, T: float):
+        self.epsinf = 6.7 * math.exp(5e-5 * (T - 300))
+        self.wL = 182.7e12 - 5.463e9 * (T - 300)
+        self.wT = 149.5e12 - 4.106e9 * (T - 300)
+        self.gamma = 6.6e11 * (1 + 2.0 / (math.exp(HBAR * self.wT / (2 * KB * T)) - 1))
+
+
+# Material models of the workloads (single Lorentz oscillators, eV units).
+SIC_CONFIG = (6.7, 0.0983, 0.120, 0.00059)
+ALUMINA_CONFIG = (3.1, 0.0787, 0.111, 0.0020)
+
+
+class Geometry:
+    """Resident vertices + triangles (bemgpu_geom_t)."""
+
+    def __init__(self, xyz, tris, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.tris = np.ascontiguousarray(tris, dtype=np.int32)
+        h = ctypes.c_void_p()
+        _check(_lib.load().bemgpu_geom_create(self.ctx.handle, self.xyz.ctypes.data, self.xyz.shape[0],
+                                              self.tris.ctypes.data, self.tris.shape[0], ctypes.byref(h)), self.ctx)
+        self.handle = h
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().bemgpu_geom_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class RWGTree:
+    """An RWG table over a Geometry (bemgpu_tree_t); ``rwgs`` unknown pairs."""
+
+    def __init__(self, geom: Geometry, rwg, diel=None):
+        self.geom = geom
+        self.rwg = np.ascontiguousarray(rwg, dtype=np.int32)
+        self.rwgs = int(self.rwg.shape[0])
+        self.diel = diel
+        self.g = GreensFunction(1.0, 1.0, 0.0, False)
+        h = ctypes.c_void_p()
+        _check(_lib.load().bemgpu_tree_create(geom.handle, self.rwg.ctypes.data, self.rwgs, ctypes.byref(h)), geom.ctx)
+        self.handle = h
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _lib.load().bemgpu_tree_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def parseShapes(body1: Body, body2: Body, diel1, diel2, ctx: Context | None = None):
+    """Builds the two-body tree and the one-body trees over one geometry.
+    ``body1`` is expected already translated by the gap vector (as
+    parseShapes translates body 1, src/HeatTransfer.cpp:67-69).
+    Returns (top, s, t)."""
+    xyz, tris, rwg, ns = two_body(body1, body2)
+    geom = Geometry(xyz, tris, ctx)
+    top = RWGTree(geom, rwg)
+    s = RWGTree(geom, rwg[:ns], diel1)
+    t = RWGTree(geom, rwg[ns:], diel2)
+    return top, s, t
+
+
+def Zts(t: RWGTree, s: RWGTree, g: GreensFunction, options: Options | None = None, precision: int = _lib.PREC_FP64):
+    """Zts(t, s, g, options): the (2 t.rwgs x 2 s.rwgs) complex128 block,
+    column-major like ComplexDenseMatrix."""
+    options = options or Options()
+    ctx = t.geom.ctx
+    m, n = 2 * t.rwgs, 2 * s.rwgs
+    Z = np.empty((m, n), dtype=np.complex128, order="F")
+    _check(_lib.load().bemgpu_zts_host(ctx.handle, t.handle, s.handle, ctypes.byref(g._g), ctypes.byref(options._c()),
+                                       int(precision), Z.ctypes.data, m), ctx)
+    return Z
+
+
+def Theta(omega: float, T: float) -> float:
+    return _lib.load().bemgpu_theta(float(omega), float(T))
+
+
+def dimensionless_omega(a: float, eV: float) -> float:
+    return _lib.load().bemgpu_dimensionless_omega(float(a), float(eV))
+
+
+def CalcHeatTransfer(a: float, eV: float, T1: float, T2: float, top: RWGTree, s: RWGTree, t: RWGTree,
+                     options: Options | None = None, precision: int = _lib.PREC_FP64, info: dict | None = None) -> float:
+    """Spectral power Re(S) (Theta(omega,T1) - Theta(omega,T2)) at eV."""
+    options = options or Options()
+    s.diel.setTemperature(T1)
+    t.diel.setTemperature(T2)
+    e1, m1, e2, m2 = s.diel.eps(eV), s.diel.mu(eV), t.diel.eps(eV), t.diel.mu(eV)
+    req = _lib.SolveReq(a, eV, T1, T2, (ctypes.c_double * 2)(e1.real, e1.imag), (ctypes.c_double * 2)(m1.real, m1.imag),
+                        (ctypes.c_double * 2)(e2.real, e2.imag), (ctypes.c_double * 2)(m2.real, m2.imag))
+    P = ctypes.c_double()
+    si = _lib.SolveInfo()
+    ctx = top.geom.ctx
+    _check(_lib.load().bemgpu_heat_transfer(ctx.handle, top.handle, s.handle, t.handle, ctypes.byref(req),
+                                            ctypes.byref(options._c()), int(precision), ctypes.byref(P),
+                                            ctypes.byref(si)), ctx)
+    if info is not None:
+        for k, _ in _lib.SolveInfo._fields_:
+            info[k] = getattr(si, k)
+    return P.value
+
+
+class FrequencySweep:
+    """FrequencySweep(file): one frequency (eV) per line (src/FrequencySweep.cpp:4-16)."""
+
+    def __init__(self, filename: str):
+        self.f = []
+        try:
+            with open(filename) as fh:
+                for line in fh:
+                    try:
+                        self.f.append(float(line.split()[0]) if line.split() else 0.0)
+                    except ValueError:
+                        self.f.append(0.0)
+        except OSError as e:
+            import sys
+            sys.stderr.write(f"{filename}: {e.strerror}\n")

@@ -1,0 +1,167 @@
+// Internal declarations shared by the bemgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <map>
+#include <mutex>
+
+#include "../../include/bemgpu.h"
+
+// src/util/MathUtils.h:16,33 (values as the reference defines them)
+#define BEM_ONETHIRD 0.33333333333333333333333333333333
+#define BEM_ONEOVER4PI 0.079577471545947667884441881686257
+
+// Device-resident per-triangle record of one RWG tree (FP64).  The frame
+// (p0, p1, p2 and derived vectors) is that of the triangle's first half-RWG in
+// the tree's RWG order: Zts integrates the outer rule over t[0] and the inner
+// rule over s[0] (src/Impedance.cpp:283, 156, 196), and the analytic terms use
+// s[0] / t[0] (src/Impedance.cpp:196-204, 264-265, 308).
+struct TriRec {
+  double p0[3], p1[3], p2[3];
+  double v01[3], v12[3], v20[3], v02[3];
+  double n[3], m01[3], m12[3], m20[3];
+  double nv01i, nv12i, nv20i, Ai, elen0;
+  double c[3];        // centroid, ((p1+p2)+p3)*ONETHIRD in the triangle's own vertex order
+  double emax;        // longest of the triangle's three edges
+  double hp0[3][3];   // free vertex p0 of each half-RWG
+  double helen[3];    // RWG edge length of each half
+  int vid[3];         // vertex ids (vertex-sharing test)
+  int gid;            // triangle id in the geometry
+  int nh;             // number of half-RWGs on this triangle in this tree (1..3)
+  int hrwg[3];        // RWG index (row/column pair of the matrix)
+  int hneg[3];        // 0 for the positive half, 1 for the negative half
+  int pad;
+};
+
+// A (test, source) near pair: shares at least one vertex, or is the same triangle.
+struct NearPair {
+  int t, s;      // local triangle indices in the two trees
+  int same;      // 1 if the same triangle
+  int pad;
+};
+
+struct bemgpu_geom_s;
+
+struct bemgpu_tree_s {
+  bemgpu_geom_s *geom = nullptr;
+  int nrwg = 0;
+  int ntri = 0;                 // triangles touched by the tree
+  std::vector<int> rwg;         // host copy of the table (4*nrwg)
+  std::vector<int> tri_gid;     // local triangle -> geometry triangle id
+  std::vector<TriRec> host_rec;
+  TriRec *d_rec = nullptr;
+};
+
+struct bemgpu_geom_s {
+  bemgpu_ctx_s *ctx = nullptr;
+  int nv = 0, nt = 0;
+  std::vector<double> xyz;
+  std::vector<int> tri;
+  std::vector<std::vector<int>> tris_at_vertex;
+};
+
+struct NearList {
+  NearPair *d = nullptr;
+  int64_t n = 0;
+};
+
+struct bemgpu_ctx_s {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  std::mutex mu;
+  // workspace: one growable device buffer per purpose
+  std::map<std::string, std::pair<void *, size_t>> ws;
+  // near-pair lists cached per (t, s) tree pair
+  std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, NearList> near_cache;
+  std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, std::vector<int64_t>> far_rule_cache;
+  cudaEvent_t ev[8];
+  int64_t launches = 0;  // kernels launched by this context
+  // live kernel statistics
+  bool prof = false;
+  struct ProfRec {
+    int kind;
+    cudaEvent_t a, b;
+    double flops, bytes;
+  };
+  std::vector<ProfRec> prof_recs;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+};
+
+// Records CUDA events around the launches in its scope when profiling is on.
+struct ProfScope {
+  bemgpu_ctx_s *ctx;
+  int kind;
+  cudaStream_t st;
+  double flops, bytes;
+  cudaEvent_t a = nullptr;
+  ProfScope(bemgpu_ctx_s *c, int k, cudaStream_t s, double f, double b);
+  ~ProfScope();
+};
+
+// Sets ctx->last_error and returns code.
+int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...);
+// Returns a device buffer of at least `bytes` for `name` (grown on demand).
+void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes);
+// Near-pair list of (t, s), built on the host once and cached on the device.
+const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s);
+// Far-pair counts per rule (6, 10, 15, 21, 36 points) of (t, s), classified on
+// the host with the kernel's test; cached.  Used for algorithmic flop counts.
+const int64_t *bem_far_rule_counts(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s,
+                                   const bemgpu_options_t *opt);
+
+// Algorithmic work per unit (frozen counting convention: real +,-,*,/ = 1 flop,
+// complex*complex = 6, complex+complex = 2, real*complex = 2; sqrt/exp/sincos/
+// log/atan2 counted apart and not included).
+inline double bem_far_pair_flops(int P) { return P * (148.0 * P + 324.0) + 9.0 * 26.0; }
+inline double bem_near_pair_flops(bool neighbour) { return 105.0 * (91.0 * 158.0 + 200.0 + 324.0) + (neighbour ? 45.0 * 80.0 : 0.0); }
+constexpr double BEM_HALFPAIR_BYTES_FP64 = 32.0;   // (cL, cK) complex128 per half-RWG pair
+
+#define BEM_CUDA_TRY(ctx, call)                                                               \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return bem_fail((ctx), BEMGPU_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,       \
+                      cudaGetErrorString(e_));                                                \
+  } while (0)
+
+// ---- fill (fill.cu) ----
+// Half-pair accumulator block for one RWG pair (i, j): four (cL, cK) complex
+// values, one per (test half a, source half b), a,b in {pos, neg}.
+struct HalfPairBlock {
+  double v[16];  // [a*2+b] -> {cL.re, cL.im, cK.re, cK.im}
+};
+
+// Computes every triangle pair of (t, s) with one Green's function and writes
+// the per-half-pair products into H (ntr x nsr blocks, index j*ntr+i).
+int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s,
+                   const bemgpu_green_t *g, const bemgpu_options_t *opt, HalfPairBlock *H,
+                   cudaStream_t stream, int64_t *n_near, int64_t *n_far);
+// Z (complex128, column-major, ld) = gather of one H with g's Zeps/Zmu.
+int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, const bemgpu_green_t *g,
+                 double *Z, int64_t ld, cudaStream_t stream);
+// W = gather(Hext, gext) (+ gather(Hint1, g1) on the s block, + gather(Hint2, g2) on the t block),
+// G1 = gather(Hint1, g1), G2 = gather(Hint2, g2).
+int bem_gather_w(bemgpu_ctx_s *ctx, const HalfPairBlock *Hext, const HalfPairBlock *H1,
+                 const HalfPairBlock *H2, int ns, int nt, const bemgpu_green_t *gext,
+                 const bemgpu_green_t *g1, const bemgpu_green_t *g2, double *W, int64_t ldw, double *G1,
+                 int64_t ld1, double *G2, int64_t ld2, cudaStream_t stream);
+
+// ---- dense complex linear algebra (dense.cu) ----
+// In-place LU with partial pivoting of the n x n complex128 column-major A.
+int bem_zgetrf(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, int *d_info,
+               cudaStream_t stream);
+// B (n x nrhs) <- A^{-1} B using the LU factors and pivots of bem_zgetrf.
+int bem_zgetrs(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int *d_ipiv, double *B,
+               int64_t ldb, int nrhs, cudaStream_t stream);
+// C = alpha * op(A) * op(B) + beta * C for complex128 column-major matrices.
+// op: 'N' or 'C' (conjugate transpose) for A; 'N' for B.
+int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const double alpha[2], const double *A,
+              int64_t lda, const double *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
+              cudaStream_t stream);

@@ -1,0 +1,419 @@
+// Context, resident geometry and RWG trees, Green's function constants.
+//
+// Host-side set-up runs once per geometry: the half-RWG frames of every
+// triangle are computed here in FP64 with the reference's arithmetic
+// (HalfRWG::HalfRWG, src/RWG.cpp:7-39) and kept on the device.
+#include "bemgpu_internal.h"
+
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstring>
+#include <algorithm>
+#include <unordered_map>
+
+namespace {
+
+// src/util/SI.cpp:3-9
+const double SI_HBAR = 1.05457148e-34;
+const double SI_KB = 1.3806503e-23;
+const double SI_EV = 1.60217646e-19;
+const double SI_C = 2.99792458e8;
+
+struct V3 {
+  double x, y, z;
+};
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 scale(double c, V3 a) { return {c * a.x, c * a.y, c * a.z}; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double norm2(V3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+inline V3 normalized(V3 a) {
+  double ni = 1. / std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  return {a.x * ni, a.y * ni, a.z * ni};
+}
+inline void put(double *d, V3 a) { d[0] = a.x; d[1] = a.y; d[2] = a.z; }
+
+V3 vtx(const bemgpu_geom_s *g, int i) { return {g->xyz[3 * i], g->xyz[3 * i + 1], g->xyz[3 * i + 2]}; }
+
+const char *kVersion = "bemgpu 0.1 (sm_103a)";
+
+}  // namespace
+
+int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->last_error = buf;
+  return code;
+}
+
+void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes) {
+  auto it = ctx->ws.find(name);
+  if (it != ctx->ws.end() && it->second.second >= bytes) return it->second.first;
+  if (it != ctx->ws.end()) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(it->second.first);
+    ctx->ws.erase(it);
+  }
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  ctx->ws[name] = {p, bytes};
+  return p;
+}
+
+const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
+  auto key = std::make_pair(t, s);
+  auto it = ctx->near_cache.find(key);
+  if (it != ctx->near_cache.end()) return &it->second;
+  const bemgpu_geom_s *g = t->geom;
+  std::unordered_map<int, int> s_local;
+  for (int i = 0; i < s->ntri; i++) s_local[s->tri_gid[i]] = i;
+  std::vector<NearPair> pairs;
+  std::vector<int> seen;
+  for (int a = 0; a < t->ntri; a++) {
+    int gt = t->tri_gid[a];
+    seen.clear();
+    for (int k = 0; k < 3; k++) {
+      int v = g->tri[3 * gt + k];
+      for (int gs : g->tris_at_vertex[v]) {
+        auto f = s_local.find(gs);
+        if (f == s_local.end()) continue;
+        if (std::find(seen.begin(), seen.end(), f->second) != seen.end()) continue;
+        seen.push_back(f->second);
+      }
+    }
+    std::sort(seen.begin(), seen.end());
+    for (int b : seen) pairs.push_back({a, b, s->tri_gid[b] == gt ? 1 : 0, 0});
+  }
+  NearList nl;
+  nl.n = (int64_t)pairs.size();
+  if (nl.n) {
+    if (cudaMalloc(&nl.d, sizeof(NearPair) * pairs.size()) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    cudaMemcpy(nl.d, pairs.data(), sizeof(NearPair) * pairs.size(), cudaMemcpyHostToDevice);
+  }
+  auto res = ctx->near_cache.emplace(key, nl);
+  return &res.first->second;
+}
+
+static cudaEvent_t prof_event(bemgpu_ctx_s *c) {
+  if (c->ev_used == c->ev_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    c->ev_pool.push_back(e);
+  }
+  return c->ev_pool[c->ev_used++];
+}
+
+ProfScope::ProfScope(bemgpu_ctx_s *c, int k, cudaStream_t s, double f, double b)
+    : ctx(c), kind(k), st(s), flops(f), bytes(b) {
+  if (ctx && ctx->prof) {
+    a = prof_event(ctx);
+    cudaEventRecord(a, st);
+  }
+}
+
+ProfScope::~ProfScope() {
+  if (a) {
+    cudaEvent_t b = prof_event(ctx);
+    cudaEventRecord(b, st);
+    ctx->prof_recs.push_back({kind, a, b, flops, bytes});
+  }
+}
+
+const int64_t *bem_far_rule_counts(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s,
+                                   const bemgpu_options_t *opt) {
+  auto key = std::make_pair(t, s);
+  auto it = ctx->far_rule_cache.find(key);
+  if (it != ctx->far_rule_cache.end()) return it->second.data();
+  std::vector<int64_t> c(5, 0);
+  for (const TriRec &T : t->host_rec)
+    for (const TriRec &S : s->host_rec) {
+      if (T.gid == S.gid) continue;
+      int sh = 0;
+      for (int i = 0; i < 3; i++) sh += (T.vid[i] == S.vid[0]) | (T.vid[i] == S.vid[1]) | (T.vid[i] == S.vid[2]);
+      if (sh) continue;
+      double x = T.c[0] - S.c[0], y = T.c[1] - S.c[1], z = T.c[2] - S.c[2];
+      double d = x * x + y * y + z * z;
+      double e = std::max(T.emax, S.emax);
+      double e2 = e * e;
+      int k = d * opt->farThresh6 > e2 ? 0 : d * opt->farThresh10 > e2 ? 1 : d * opt->farThresh15 > e2 ? 2
+            : d * opt->farThresh21 > e2 ? 3 : 4;
+      c[k]++;
+    }
+  auto res = ctx->far_rule_cache.emplace(key, c);
+  return res.first->second.data();
+}
+
+extern "C" {
+
+const char *bemgpu_version(void) { return kVersion; }
+
+int bemgpu_prof_enable(bemgpu_ctx_t ctx, int enable) {
+  if (!ctx) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->prof = enable != 0;
+  ctx->prof_recs.clear();
+  ctx->ev_used = 0;
+  return BEMGPU_OK;
+}
+
+int bemgpu_prof_query(bemgpu_ctx_t ctx, int kind, int64_t *launches, double *ms, double *flops, double *bytes) {
+  if (!ctx || kind < 0 || kind >= BEMGPU_K_COUNT) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return bem_fail(ctx, BEMGPU_ERR_CUDA, "prof_query: sync");
+  int64_t n = 0;
+  double t = 0, f = 0, b = 0;
+  for (auto &r : ctx->prof_recs) {
+    if (r.kind != kind) continue;
+    float e = 0;
+    cudaEventElapsedTime(&e, r.a, r.b);
+    n++;
+    t += e;
+    f += r.flops;
+    b += r.bytes;
+  }
+  if (launches) *launches = n;
+  if (ms) *ms = t;
+  if (flops) *flops = f;
+  if (bytes) *bytes = b;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_create(int device, bemgpu_ctx_t *out) {
+  if (!out) return BEMGPU_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return BEMGPU_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return BEMGPU_ERR_CUDA;
+  bemgpu_ctx_s *c = new bemgpu_ctx_s();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return BEMGPU_ERR_CUDA;
+  }
+  for (auto &e : c->ev) cudaEventCreate(&e);
+  *out = c;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_destroy(bemgpu_ctx_t ctx) {
+  if (!ctx) return BEMGPU_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->ws) cudaFree(kv.second.first);
+  for (auto &kv : ctx->near_cache) cudaFree(kv.second.d);
+  for (auto &e : ctx->ev) cudaEventDestroy(e);
+  for (auto &e : ctx->ev_pool) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BEMGPU_OK;
+}
+
+int bemgpu_ctx_stream(bemgpu_ctx_t ctx, void **stream) {
+  if (!ctx || !stream) return BEMGPU_ERR_ARG;
+  *stream = (void *)ctx->stream;
+  return BEMGPU_OK;
+}
+
+int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx) { return ctx ? ctx->launches : BEMGPU_ERR_ARG; }
+
+const char *bemgpu_ctx_last_error(bemgpu_ctx_t ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int bemgpu_geom_create(bemgpu_ctx_t ctx, const double *xyz, int nv, const int *tri, int nt,
+                       bemgpu_geom_t *out) {
+  if (!ctx || !xyz || !tri || !out || nv < 3 || nt < 1)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "geom_create: bad arguments");
+  for (int i = 0; i < 3 * nt; i++)
+    if (tri[i] < 0 || tri[i] >= nv) return bem_fail(ctx, BEMGPU_ERR_MESH, "geom_create: vertex id out of range");
+  for (int i = 0; i < 3 * nv; i++)
+    if (!std::isfinite(xyz[i])) return bem_fail(ctx, BEMGPU_ERR_MESH, "geom_create: non-finite coordinate");
+  bemgpu_geom_s *g = new bemgpu_geom_s();
+  g->ctx = ctx;
+  g->nv = nv;
+  g->nt = nt;
+  g->xyz.assign(xyz, xyz + 3 * (size_t)nv);
+  g->tri.assign(tri, tri + 3 * (size_t)nt);
+  g->tris_at_vertex.resize(nv);
+  for (int t = 0; t < nt; t++)
+    for (int k = 0; k < 3; k++) g->tris_at_vertex[tri[3 * t + k]].push_back(t);
+  *out = g;
+  return BEMGPU_OK;
+}
+
+int bemgpu_geom_destroy(bemgpu_geom_t g) {
+  if (!g) return BEMGPU_ERR_ARG;
+  delete g;
+  return BEMGPU_OK;
+}
+
+int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t *out) {
+  if (!g || !rwg || !out || nrwg < 1) return bem_fail(g ? g->ctx : nullptr, BEMGPU_ERR_ARG, "tree_create: bad arguments");
+  bemgpu_ctx_s *ctx = g->ctx;
+  *out = nullptr;
+  bemgpu_tree_s *t = new bemgpu_tree_s();
+  t->geom = g;
+  t->nrwg = nrwg;
+  t->rwg.assign(rwg, rwg + 4 * (size_t)nrwg);
+  std::vector<int> local(g->nt, -1);
+  // TriangleRWGMap construction order (src/Impedance.cpp:397-406)
+  for (int i = 0; i < nrwg; i++) {
+    int tp = rwg[4 * i], tn = rwg[4 * i + 1], e1 = rwg[4 * i + 2], e2 = rwg[4 * i + 3];
+    if (tp < 0 || tp >= g->nt || tn < 0 || tn >= g->nt || tp == tn || e1 == e2 || e1 < 0 || e2 < 0 ||
+        e1 >= g->nv || e2 >= g->nv) {
+      delete t;
+      return bem_fail(ctx, BEMGPU_ERR_MESH, "tree_create: RWG %d has invalid ids", i);
+    }
+    for (int side = 0; side < 2; side++) {
+      int tr = side == 0 ? tp : tn;
+      const int *tv = &g->tri[3 * tr];
+      int has1 = (tv[0] == e1) + (tv[1] == e1) + (tv[2] == e1);
+      int has2 = (tv[0] == e2) + (tv[1] == e2) + (tv[2] == e2);
+      if (has1 != 1 || has2 != 1) {
+        delete t;
+        return bem_fail(ctx, BEMGPU_ERR_MESH, "tree_create: RWG %d edge is not on triangle %d", i, tr);
+      }
+      if (local[tr] < 0) {
+        local[tr] = t->ntri++;
+        t->tri_gid.push_back(tr);
+        TriRec r;
+        memset(&r, 0, sizeof r);
+        r.gid = tr;
+        t->host_rec.push_back(r);
+      }
+      TriRec &r = t->host_rec[local[tr]];
+      if (r.nh >= 3) {
+        delete t;
+        return bem_fail(ctx, BEMGPU_ERR_MESH, "tree_create: triangle %d carries more than 3 RWGs", tr);
+      }
+      // HalfRWG::HalfRWG (src/RWG.cpp:9-21): p0 off the edge, p1/p2 follow the
+      // triangle's vertex cycle.
+      int rot = (tv[0] != e1 && tv[0] != e2) ? 0 : ((tv[1] != e1 && tv[1] != e2) ? 1 : 2);
+      V3 p0 = vtx(g, tv[rot]), p1 = vtx(g, tv[(rot + 1) % 3]), p2 = vtx(g, tv[(rot + 2) % 3]);
+      int h = r.nh++;
+      put(r.hp0[h], p0);
+      r.helen[h] = std::sqrt(norm2(sub(vtx(g, e2), vtx(g, e1))));  // Edge::length
+      r.hrwg[h] = i;
+      r.hneg[h] = side;
+      if (h == 0) {
+        V3 v01 = sub(p1, p0), v12 = sub(p2, p1), v20 = sub(p0, p2), v02 = sub(p2, p0);
+        r.nv01i = 1. / std::sqrt(norm2(v01));
+        r.nv12i = 1. / std::sqrt(norm2(v12));
+        r.nv20i = 1. / std::sqrt(norm2(v20));
+        V3 n = cross(v01, v02);
+        double A2 = std::sqrt(norm2(n));
+        n = scale(1. / A2, n);
+        r.Ai = 2.0 / A2;
+        put(r.p0, p0); put(r.p1, p1); put(r.p2, p2);
+        put(r.v01, v01); put(r.v12, v12); put(r.v20, v20); put(r.v02, v02);
+        put(r.n, n);
+        put(r.m01, normalized(cross(v01, n)));
+        put(r.m12, normalized(cross(v12, n)));
+        put(r.m20, normalized(cross(v20, n)));
+        r.elen0 = r.helen[0];
+        // center, src/Triangle.cpp:30-34; edge lengths, src/ShapeMesh.cpp:938-943
+        V3 a = vtx(g, tv[0]), b = vtx(g, tv[1]), c = vtx(g, tv[2]);
+        put(r.c, scale(BEM_ONETHIRD, add(add(a, b), c)));
+        r.emax = std::max(std::max(std::sqrt(norm2(sub(b, a))), std::sqrt(norm2(sub(c, b)))),
+                          std::sqrt(norm2(sub(a, c))));
+        r.vid[0] = tv[0]; r.vid[1] = tv[1]; r.vid[2] = tv[2];
+      }
+    }
+  }
+  for (const TriRec &r : t->host_rec)
+    if (!(std::isfinite(r.Ai) && r.Ai > 0)) {
+      delete t;
+      return bem_fail(ctx, BEMGPU_ERR_MESH, "tree_create: degenerate triangle %d", r.gid);
+    }
+  cudaSetDevice(ctx->device);
+  if (cudaMalloc(&t->d_rec, sizeof(TriRec) * t->ntri) != cudaSuccess) {
+    cudaGetLastError();
+    delete t;
+    return bem_fail(ctx, BEMGPU_ERR_OOM, "tree_create: device allocation failed");
+  }
+  if (cudaMemcpy(t->d_rec, t->host_rec.data(), sizeof(TriRec) * t->ntri, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(t->d_rec);
+    delete t;
+    return bem_fail(ctx, BEMGPU_ERR_CUDA, "tree_create: upload failed");
+  }
+  *out = t;
+  return BEMGPU_OK;
+}
+
+int bemgpu_tree_destroy(bemgpu_tree_t t) {
+  if (!t) return BEMGPU_ERR_ARG;
+  bemgpu_ctx_s *ctx = t->geom->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto it = ctx->far_rule_cache.begin(); it != ctx->far_rule_cache.end();) {
+    if (it->first.first == t || it->first.second == t) it = ctx->far_rule_cache.erase(it);
+    else ++it;
+  }
+  for (auto it = ctx->near_cache.begin(); it != ctx->near_cache.end();) {
+    if (it->first.first == t || it->first.second == t) {
+      cudaFree(it->second.d);
+      it = ctx->near_cache.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  cudaFree(t->d_rec);
+  delete t;
+  return BEMGPU_OK;
+}
+
+int bemgpu_tree_size(bemgpu_tree_t t) { return t ? t->nrwg : BEMGPU_ERR_ARG; }
+
+int bemgpu_green_init(const double eps[2], const double mu[2], const double omega[2], int external,
+                      bemgpu_green_t *out) {
+  if (!eps || !mu || !omega || !out) return BEMGPU_ERR_ARG;
+  typedef std::complex<double> C;
+  C e(eps[0], eps[1]), m(mu[0], mu[1]), w(omega[0], omega[1]), I(0., 1.);
+  // GreensFunction::init, src/GreensFunction.cpp:17-30
+  C ksq = e * m * w * w;
+  C k = std::sqrt(ksq);
+  C ik = I * k;
+  C k2 = -0.5 * ksq;
+  C Zeps = 1. / (I * w * e);
+  C Zmu = 1. / (I * w * m);
+  auto st = [](double *d, C v) { d[0] = v.real(); d[1] = v.imag(); };
+  st(out->eps, e); st(out->mu, m); st(out->omega, w);
+  st(out->ksquared, ksq); st(out->k, k); st(out->ik, ik); st(out->k2, k2);
+  st(out->Zeps, Zeps); st(out->Zmu, Zmu);
+  out->external = external;
+  return BEMGPU_OK;
+}
+
+void bemgpu_options_default(bemgpu_options_t *opt) {
+  if (!opt) return;
+  opt->farThresh6 = 12.0;
+  opt->farThresh10 = 8.0;
+  opt->farThresh15 = 4.0;
+  opt->farThresh21 = 2.0;
+}
+
+double bemgpu_theta(double omega, double T) {
+  return SI_HBAR * omega / (std::exp(SI_HBAR * omega / (SI_KB * T)) - 1);
+}
+
+double bemgpu_dimensionless_omega(double a, double eV) {
+  double omegaSI = eV * SI_EV / SI_HBAR;
+  return omegaSI * a / SI_C;
+}
+
+}  // extern "C"

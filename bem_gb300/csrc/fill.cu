@@ -1,0 +1,689 @@
+// PMCHWT RWG impedance fill on the GPU: Zts (src/Impedance.cpp:276-413).
+//
+// Work decomposition
+//   * far pairs (no shared vertex): one thread per (test, source) triangle
+//     pair over a 2-D grid, FP64 (plain path).  The reference contracts the
+//     inner integrals per half-RWG (Gphi[j], DGxphi[j], src/Impedance.cpp:126-167);
+//     here the inner loop accumulates four j-independent moments
+//        I0 = sum w g,  A = sum w g (r_s - P_s),  Q0 = sum w q,  Q1 = sum w q (r_s - P_s)
+//     (g, q of GreensFunction::scalar_gradient, gradient = q (r_t - r_s)), and the
+//     outer loop eight moments U0..U3, V0..V3, from which all nine (i, j)
+//     products L_ij, K_ij follow in closed form (derivation beside far_pair()).
+//   * near pairs (same triangle or a shared vertex): one warp per pair, lanes over
+//     the 105 outer nodes, each lane runs the 91-node smooth inner rule, the
+//     analytic singular terms (EHNonSmoothIntegral, src/Source.cpp:16-86) and the
+//     close-pair contraction of src/Impedance.cpp:194-250 in FP64; the
+//     neighbour-edge K correction (src/Impedance.cpp:301-324) runs on the same warp.
+//   * every pair writes its nine (c L_ij, c K_ij) half-pair products into a
+//     half-pair block array H (one 128-byte block per RWG pair (i, j), four
+//     slots for (pos/neg test half) x (pos/neg source half)); each slot has
+//     exactly one writer, so no atomics are needed.  A gather kernel then
+//     reduces each block into the 2x2 (J, M) entries of Z in RWG-pair order with
+//     coalesced stores (src/Impedance.cpp:365-384).
+#include "bemgpu_internal.h"
+#include "quadrature_tables.h"
+
+#include <cmath>
+
+namespace {
+
+struct GreenDev {
+  double ikr, iki;      // ik
+  double k2r, k2i;      // k2 = -ksquared/2
+  double ksqr, ksqi;    // ksquared
+};
+
+struct FarOpts {
+  double th6, th10, th15, th21;
+};
+
+__constant__ double c_rule6[6][3];
+__constant__ double c_rule10[10][3];
+__constant__ double c_rule15[15][3];
+__constant__ double c_rule21[21][3];
+__constant__ double c_rule36[36][3];
+__constant__ double c_rule91[91][3];
+__constant__ double c_rule105[105][3];
+__constant__ double c_line15[15][2];
+
+// ---------------- small FP64 vector / complex helpers ----------------
+struct d3 {
+  double x, y, z;
+};
+struct z1 {
+  double r, i;
+};
+struct z3 {
+  z1 x, y, z;
+};
+
+__device__ __forceinline__ d3 ld3(const double *p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ d3 operator*(double c, d3 a) { return {c * a.x, c * a.y, c * a.z}; }
+__device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ d3 cross(d3 a, d3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ z1 zmul(z1 a, z1 b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+__device__ __forceinline__ z1 zadd(z1 a, z1 b) { return {a.r + b.r, a.i + b.i}; }
+__device__ __forceinline__ z1 zsub(z1 a, z1 b) { return {a.r - b.r, a.i - b.i}; }
+__device__ __forceinline__ z1 zscale(double c, z1 a) { return {c * a.r, c * a.i}; }
+__device__ __forceinline__ z3 z3zero() { return {{0, 0}, {0, 0}, {0, 0}}; }
+// complex scalar times real vector
+__device__ __forceinline__ z3 zs_v(z1 c, d3 v) { return {{c.r * v.x, c.i * v.x}, {c.r * v.y, c.i * v.y}, {c.r * v.z, c.i * v.z}}; }
+__device__ __forceinline__ z3 z3add(z3 a, z3 b) { return {zadd(a.x, b.x), zadd(a.y, b.y), zadd(a.z, b.z)}; }
+__device__ __forceinline__ z3 z3sub(z3 a, z3 b) { return {zsub(a.x, b.x), zsub(a.y, b.y), zsub(a.z, b.z)}; }
+__device__ __forceinline__ z3 z3add_r(z3 a, d3 b) { return {{a.x.r + b.x, a.x.i}, {a.y.r + b.y, a.y.i}, {a.z.r + b.z, a.z.i}}; }
+__device__ __forceinline__ z3 z3scale(double c, z3 a) { return {zscale(c, a.x), zscale(c, a.y), zscale(c, a.z)}; }
+// dot(real, complex) — no conjugation (ComplexVector3.h:124-126)
+__device__ __forceinline__ z1 rdot(d3 a, z3 b) {
+  return {a.x * b.x.r + a.y * b.y.r + a.z * b.z.r, a.x * b.x.i + a.y * b.y.i + a.z * b.z.i};
+}
+// complex x real cross product
+__device__ __forceinline__ z3 zcross(z3 a, d3 b) {
+  return {{a.y.r * b.z - a.z.r * b.y, a.y.i * b.z - a.z.i * b.y},
+          {a.z.r * b.x - a.x.r * b.z, a.z.i * b.x - a.x.i * b.z},
+          {a.x.r * b.y - a.y.r * b.x, a.x.i * b.y - a.y.i * b.x}};
+}
+// real x complex cross product
+__device__ __forceinline__ z3 rcross(d3 a, z3 b) {
+  return {{a.y * b.z.r - a.z * b.y.r, a.y * b.z.i - a.z * b.y.i},
+          {a.z * b.x.r - a.x * b.z.r, a.z * b.x.i - a.x * b.z.i},
+          {a.x * b.y.r - a.y * b.x.r, a.x * b.y.i - a.y * b.x.i}};
+}
+__device__ __forceinline__ void zacc(z1 &a, z1 b) { a.r += b.r; a.i += b.i; }
+
+// exp(ikR) for real R: exp(Re(ik) R) * (cos(Im(ik) R), sin(Im(ik) R))
+__device__ __forceinline__ z1 zexp_ikR(const GreenDev &g, double R) {
+  double m = exp(g.ikr * R);
+  double s, c;
+  sincos(g.iki * R, &s, &c);
+  return {m * c, m * s};
+}
+
+__device__ __forceinline__ int shares_vertex(const int *a, const int *b) {
+  int c = 0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) c += (a[i] == b[0]) | (a[i] == b[1]) | (a[i] == b[2]);
+  return c;
+}
+
+// IEEE-exact squared distance without contraction (the far-rule test compares
+// it with emax^2, src/Impedance.cpp:329-336).
+__device__ __forceinline__ double dist2_rn(const double *a, const double *b) {
+  double x = __dsub_rn(a[0], b[0]), y = __dsub_rn(a[1], b[1]), z = __dsub_rn(a[2], b[2]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+__device__ __forceinline__ void store_block(HalfPairBlock *H, int ntr, int i, int a, int j, int b, z1 cL, z1 cK) {
+  double2 *p = reinterpret_cast<double2 *>(&H[(size_t)j * ntr + i].v[(a * 2 + b) * 4]);
+  p[0] = make_double2(cL.r, cL.i);
+  p[1] = make_double2(cK.r, cK.i);
+}
+
+// Scatter coefficient of src/Impedance.cpp:372-375.
+__device__ __forceinline__ double scatter_coef(const TriRec &T, int i, const TriRec &S, int j) {
+  double c = BEM_ONEOVER4PI * T.helen[i] * S.helen[j];
+  return (T.hneg[i] != S.hneg[j]) ? -c : c;
+}
+
+// ---------------- far pairs ----------------
+//
+// Closed form of the nine products.  With P_t, P_s the frame origins (p0 of
+// t[0], s[0]), rho = r_t - P_t, l = r_s - P_s, e_i = p0_i - P_t, d_j = p0_j - P_s,
+// D_ij = p0_i - p0_j (test half i, source half j):
+//   Gphi_j(r_t)   = 1/2 (A - d_j I0)
+//   DGxphi_j(r_t) = 1/2 (r_t - p0_j) x (Q1 - d_j Q0)     [(r_t-r_s)x(r_s-p0_j) = (r_t-p0_j)x(r_s-p0_j)]
+//   phi_i . DGxphi_j = 1/4 D_ij . ((Q1 - d_j Q0) x (rho - e_i))   [a.(a x X) = 0]
+// and, with the outer moments U0 = sum w I0, U1 = sum w rho.A, U2 = sum w I0 rho,
+// U3 = sum w A, V0 = sum w Q0, V1 = sum w Q1 x rho, V2 = sum w Q1, V3 = sum w Q0 rho:
+//   L_ij = k^2/4 [U1 - d_j.U2 - e_i.U3 + (e_i.d_j) U0] - U0
+//   K_ij = -1/4 D_ij . [V1 - V2 x e_i - d_j x V3 + V0 (d_j x e_i)]
+// which is LKFarOuterIntegrand (src/Impedance.cpp:154-168) summed over the outer rule.
+__device__ __noinline__ void far_pair(const TriRec &T, const TriRec &S, const GreenDev &g,
+                                      const double (*rule)[3], int nr, HalfPairBlock *H, int ntr) {
+  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+  const d3 v01t = ld3(T.v01), v02t = ld3(T.v02), v01s = ld3(S.v01), v02s = ld3(S.v02);
+  z1 U0 = {0, 0}, U1 = {0, 0}, V0 = {0, 0};
+  z3 U2 = z3zero(), U3 = z3zero(), V1 = z3zero(), V2 = z3zero(), V3 = z3zero();
+  for (int q = 0; q < nr; q++) {
+    const double a = rule[q][0], b = rule[q][1], w = rule[q][2];
+    const d3 rho = a * v01t + b * v02t;
+    const d3 rt = Pt + rho;
+    z1 I0 = {0, 0}, Q0 = {0, 0};
+    z3 A = z3zero(), Q1 = z3zero();
+    for (int u = 0; u < nr; u++) {
+      const double as = rule[u][0], bs = rule[u][1], ws = rule[u][2];
+      const d3 l = as * v01s + bs * v02s;
+      const d3 x = rt - (Ps + l);
+      const double R2 = dot(x, x);
+      const double Ri = rsqrt(R2);
+      const double R = R2 * Ri;
+      const z1 e = zexp_ikR(g, R);
+      // scalar_gradient, src/GreensFunction.cpp:41-52
+      const z1 gs = zscale(Ri, e);
+      const z1 one_m_ikR = {1.0 - g.ikr * R, -g.iki * R};
+      const z1 qq = zscale(Ri * Ri, zmul(gs, one_m_ikR));
+      const z1 gw = zscale(ws, gs), qw = zscale(ws, qq);
+      zacc(I0, gw);
+      A = z3add(A, zs_v(gw, l));
+      zacc(Q0, qw);
+      Q1 = z3add(Q1, zs_v(qw, l));
+    }
+    zacc(U0, zscale(w, I0));
+    zacc(U1, zscale(w, rdot(rho, A)));
+    U2 = z3add(U2, zs_v(zscale(w, I0), rho));
+    U3 = z3add(U3, z3scale(w, A));
+    zacc(V0, zscale(w, Q0));
+    V1 = z3add(V1, z3scale(w, zcross(Q1, rho)));
+    V2 = z3add(V2, z3scale(w, Q1));
+    V3 = z3add(V3, zs_v(zscale(w, Q0), rho));
+  }
+  const z1 ksq = {g.ksqr, g.ksqi};
+  for (int i = 0; i < T.nh; i++) {
+    const d3 p0i = ld3(T.hp0[i]);
+    const d3 ei = p0i - Pt;
+    for (int j = 0; j < S.nh; j++) {
+      const d3 p0j = ld3(S.hp0[j]);
+      const d3 dj = p0j - Ps;
+      const d3 D = p0i - p0j;
+      // L_ij
+      z1 bracket = zsub(zsub(U1, rdot(dj, U2)), rdot(ei, U3));
+      zacc(bracket, zscale(dot(ei, dj), U0));
+      const z1 L = zsub(zscale(0.25, zmul(ksq, bracket)), U0);
+      // K_ij
+      z3 X = z3sub(z3sub(V1, zcross(V2, ei)), rcross(dj, V3));
+      X = z3add(X, zs_v(V0, cross(dj, ei)));
+      const z1 K = zscale(-0.25, rdot(D, X));
+      const double c = scatter_coef(T, i, S, j);
+      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, L), zscale(c, K));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) far_pairs_fp64_kernel(const TriRec *__restrict__ Tr, int ntT,
+                                                             const TriRec *__restrict__ Sr, int ntS, GreenDev g,
+                                                             FarOpts o, HalfPairBlock *__restrict__ H, int ntr) {
+  const int sb = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ta = blockIdx.y * blockDim.y + threadIdx.y;
+  if (sb >= ntS || ta >= ntT) return;
+  const TriRec &T = Tr[ta];
+  const TriRec &S = Sr[sb];
+  if (T.gid == S.gid || shares_vertex(T.vid, S.vid)) return;  // near kernel
+  // far-rule choice, src/Impedance.cpp:329-360
+  const double d = dist2_rn(T.c, S.c);
+  const double e = fmax(T.emax, S.emax);
+  const double emax2 = __dmul_rn(e, e);
+  if (__dmul_rn(d, o.th6) > emax2) far_pair(T, S, g, c_rule6, 6, H, ntr);
+  else if (__dmul_rn(d, o.th10) > emax2) far_pair(T, S, g, c_rule10, 10, H, ntr);
+  else if (__dmul_rn(d, o.th15) > emax2) far_pair(T, S, g, c_rule15, 15, H, ntr);
+  else if (__dmul_rn(d, o.th21) > emax2) far_pair(T, S, g, c_rule21, 21, H, ntr);
+  else far_pair(T, S, g, c_rule36, 36, H, ntr);
+}
+
+// ---------------- near pairs ----------------
+
+// EHNonSmoothIntegral, src/Source.cpp:16-86 (frame of the source triangle's s[0]).
+__device__ void eh_nonsmooth(const TriRec &S, d3 rt, double &ISn3h, double &ISn1, double &IS1, d3 &IL1,
+                             d3 &IL3) {
+  const double tol = 1e-6 * S.elen0;
+  const d3 p0 = rt - ld3(S.p0), p1 = rt - ld3(S.p1), p2 = rt - ld3(S.p2);
+  const double R02 = dot(p0, p0), R0 = sqrt(R02);
+  const double R12 = dot(p1, p1), R1 = sqrt(R12);
+  const double R22 = dot(p2, p2), R2 = sqrt(R22);
+  const d3 a0 = (1. / R0) * p0, a1 = (1. / R1) * p1, a2 = (1. / R2) * p2;
+  const d3 n = ld3(S.n);
+  const double x = 1.0 + dot(a0, a1 + a2) + dot(a1, a2);
+  const double y = fabs(dot(a0, cross(a1, a2)));
+  const double h = dot(p0, n);
+  ISn3h = (h < 0. ? -2. : 2.) * atan2(y, x);
+  const d3 v01 = ld3(S.v01), v12 = ld3(S.v12), v20 = ld3(S.v20);
+  double num, den;
+  const double s010 = S.nv01i * dot(v01, p0), s011 = S.nv01i * dot(v01, p1);
+  num = R1 - s011; den = R0 - s010;
+  const double ILn1_01 = (fabs(num) < tol || fabs(den) < tol) ? 0. : log(num / den);
+  const double s121 = S.nv12i * dot(v12, p1), s122 = S.nv12i * dot(v12, p2);
+  num = R2 - s122; den = R1 - s121;
+  const double ILn1_12 = (fabs(num) < tol || fabs(den) < tol) ? 0. : log(num / den);
+  const double s202 = S.nv20i * dot(v20, p2), s200 = S.nv20i * dot(v20, p0);
+  num = R0 - s200; den = R2 - s202;
+  const double ILn1_20 = (fabs(num) < tol || fabs(den) < tol) ? 0. : log(num / den);
+  const d3 m01 = ld3(S.m01), m12 = ld3(S.m12), m20 = ld3(S.m20);
+  const double t01 = dot(m01, p0), t12 = dot(m12, p1), t20 = dot(m20, p2);
+  ISn1 = -h * ISn3h - (t01 * ILn1_01 + t12 * ILn1_12 + t20 * ILn1_20);
+  const double R02_01 = R02 - s010 * s010;
+  const double IL1_01 = 0.5 * (R02_01 * ILn1_01 - (R1 * s011 - R0 * s010));
+  const double R02_12 = R12 - s121 * s121;
+  const double IL1_12 = 0.5 * (R02_12 * ILn1_12 - (R2 * s122 - R1 * s121));
+  const double R02_20 = R22 - s202 * s202;
+  const double IL1_20 = 0.5 * (R02_20 * ILn1_20 - (R0 * s200 - R2 * s202));
+  const double IL3_01 = 0.75 * R02_01 * IL1_01 - 0.25 * (R12 * R1 * s011 - R02 * R0 * s010);
+  const double IL3_12 = 0.75 * R02_12 * IL1_12 - 0.25 * (R22 * R2 * s122 - R12 * R1 * s121);
+  const double IL3_20 = 0.75 * R02_20 * IL1_20 - 0.25 * (R02 * R0 * s200 - R22 * R2 * s202);
+  IS1 = BEM_ONETHIRD * (h * h * ISn1 - (t01 * IL1_01 + t12 * IL1_12 + t20 * IL1_20));
+  IL1 = IL1_01 * m01 + IL1_12 * m12 + IL1_20 * m20;
+  IL3 = IL3_01 * m01 + IL3_12 * m12 + IL3_20 * m20;
+}
+
+// LKEdgeIntegral, src/Impedance.cpp:13-73 (frame of the test triangle's t[0]).
+__device__ void lk_edge_integral(const TriRec &T, d3 rs, double &ISn1, d3 &IL1) {
+  const d3 p0 = rs - ld3(T.p0), p1 = rs - ld3(T.p1), p2 = rs - ld3(T.p2);
+  const double R02 = dot(p0, p0), R0 = sqrt(R02);
+  const double R12 = dot(p1, p1), R1 = sqrt(R12);
+  const double R22 = dot(p2, p2), R2 = sqrt(R22);
+  const double tol = 1e-8 * T.elen0;
+  const d3 a0 = (1. / R0) * p0, a1 = (1. / R1) * p1, a2 = (1. / R2) * p2;
+  const double h = dot(p0, ld3(T.n));
+  const double x = 1.0 + dot(a0, a1 + a2) + dot(a1, a2);
+  const double y = fabs(dot(a0, cross(a1, a2)));
+  const double ISn3h = (h < 0 ? -2. : 2.) * atan2(y, x);
+  const d3 m01 = ld3(T.m01), m12 = ld3(T.m12), m20 = ld3(T.m20);
+  const double t01 = dot(m01, p0), t12 = dot(m12, p1), t20 = dot(m20, p2);
+  const d3 v01 = ld3(T.v01), v12 = ld3(T.v12), v20 = ld3(T.v20);
+  double num, den;
+  const double s010 = T.nv01i * dot(v01, p0), s011 = T.nv01i * dot(v01, p1);
+  num = R1 - s011; den = R0 - s010;
+  const double ILn1_01 = (fabs(num) < tol || fabs(den) < tol) ? 0. : log(num / den);
+  const double s121 = T.nv12i * dot(v12, p1), s122 = T.nv12i * dot(v12, p2);
+  num = R2 - s122; den = R1 - s121;
+  const double ILn1_12 = (fabs(num) < tol || fabs(den) < tol) ? 0. : log(num / den);
+  const double s202 = T.nv20i * dot(v20, p2), s200 = T.nv20i * dot(v20, p0);
+  num = R0 - s200; den = R2 - s202;
+  const double ILn1_20 = (fabs(num) < tol || fabs(den) < tol) ? 0. : log(num / den);
+  ISn1 = -h * ISn3h - (t01 * ILn1_01 + t12 * ILn1_12 + t20 * ILn1_20);
+  const double IL1_01 = 0.5 * ((R02 - s010 * s010) * ILn1_01 - (R1 * s011 - R0 * s010));
+  const double IL1_12 = 0.5 * ((R12 - s121 * s121) * ILn1_12 - (R2 * s122 - R1 * s121));
+  const double IL1_20 = 0.5 * ((R22 - s202 * s202) * ILn1_20 - (R0 * s200 - R2 * s202));
+  IL1 = IL1_01 * m01 + IL1_12 * m12 + IL1_20 * m20;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+constexpr int NEAR_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_fp64_kernel(
+    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
+    GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
+  __shared__ double s_nodes[NEAR_WARPS][BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  double(*nodes)[4] = s_nodes[wid];
+  const z1 ksq = {g.ksqr, g.ksqi};
+  const z1 k2 = {g.k2r, g.k2i};
+  for (int64_t p = (int64_t)blockIdx.x * NEAR_WARPS + wid; p < npairs; p += (int64_t)gridDim.x * NEAR_WARPS) {
+    const NearPair np = list[p];
+    const TriRec &T = Tr[np.t];
+    const TriRec &S = Sr[np.s];
+    const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+    const d3 v01t = ld3(T.v01), v02t = ld3(T.v02);
+    {
+      const d3 v01s = ld3(S.v01), v02s = ld3(S.v02);
+      for (int u = lane; u < BEMGPU_TRI_RULE91_N; u += 32) {
+        const d3 l = c_rule91[u][0] * v01s + c_rule91[u][1] * v02s;
+        nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
+        nodes[u][3] = c_rule91[u][2];
+      }
+    }
+    __syncwarp();
+    const int nht = T.nh, nhs = S.nh;
+    d3 dj[3];
+    for (int j = 0; j < 3; j++) dj[j] = (j < nhs) ? ld3(S.hp0[j]) - Ps : d3{0, 0, 0};
+    z1 L[9], K[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) { L[k] = {0, 0}; K[k] = {0, 0}; }
+    const d3 nS = ld3(S.n);
+    const double Ai2 = 0.5 * S.Ai;
+    for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
+      const double w = c_rule105[q][2];
+      const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
+      const d3 rts = rt - Ps;
+      // LKSmoothInnerIntegrand over s[0] (src/Impedance.cpp:93-105) as moments
+      z1 I0 = {0, 0}, Q0 = {0, 0};
+      z3 A = z3zero(), Q1 = z3zero();
+      for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
+        const d3 l = {nodes[u][0], nodes[u][1], nodes[u][2]};
+        const double ws = nodes[u][3];
+        const d3 x = rts - l;
+        const double R2 = dot(x, x);
+        const double R = sqrt(R2);
+        const z1 e = zexp_ikR(g, R);
+        // scalar_gradient_smooth, src/GreensFunction.cpp:54-69
+        const double Ri = 1.0 / R;
+        const z1 gs = zsub(zscale(Ri, z1{e.r - 1.0, e.i}), zscale(R, k2));
+        const z1 ikR = {g.ikr * R, g.iki * R};
+        z1 num = zmul(e, z1{1.0 - ikR.r, -ikR.i});
+        num = zadd(num, zscale(R2, k2));
+        num.r -= 1.0;
+        const z1 qq = zscale(Ri / R2, num);
+        const z1 gw = zscale(ws, gs), qw = zscale(ws, qq);
+        zacc(I0, gw);
+        A = z3add(A, zs_v(gw, l));
+        zacc(Q0, qw);
+        Q1 = z3add(Q1, zs_v(qw, l));
+      }
+      // LKCloseOuterIntegrand::weighPoint, src/Impedance.cpp:194-250
+      double ISn3h, ISn1, IS1;
+      d3 IL1, IL3;
+      eh_nonsmooth(S, rt, ISn3h, ISn1, IS1, IL1, IL3);
+      const z3 IL13 = z3scale(Ai2, z3add_r(zs_v(zscale(BEM_ONETHIRD, k2), IL3), IL1));
+      z1 ISn11 = zscale(Ai2, z1{ISn1 + k2.r * IS1, k2.i * IS1});
+      const double h = dot(rt - Ps, nS);
+      const z1 L2 = zadd(zscale(2.0, ISn11), I0);
+      if (fabs(h) < 1e-8 * S.elen0) {
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          if (j >= nhs) break;
+          const z3 Gphij = z3scale(0.5, z3sub(A, zs_v(I0, dj[j])));
+          const z3 K21 = z3add(IL13, zs_v(ISn11, rt - ld3(S.hp0[j])));
+          const z3 GK = z3add(Gphij, K21);
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            if (i >= nht) break;
+            const d3 phi = 0.5 * (rt - ld3(T.hp0[i]));
+            const z1 t = zsub(zmul(ksq, rdot(phi, GK)), L2);
+            zacc(L[i * 3 + j], zscale(w, t));
+          }
+        }
+      } else {
+        const d3 ISn3hn = (Ai2 * ISn3h) * nS;
+        const d3 rho = rt - h * nS;
+        const z1 Ai2k2 = zscale(Ai2, k2);
+        const z3 K31 = zs_v(Ai2k2, IL1 - (h * ISn1) * nS);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          if (j >= nhs) break;
+          const d3 p0j = ld3(S.hp0[j]);
+          const z3 Gphij = z3scale(0.5, z3sub(A, zs_v(I0, dj[j])));
+          const z3 DGxphij = z3scale(0.5, rcross(rt - p0j, z3sub(Q1, zs_v(Q0, dj[j]))));
+          const z3 K21 = z3add(IL13, zs_v(ISn11, rho - p0j));
+          const z3 K41 = zcross(K31, rt - p0j);
+          const z3 GK = z3add(Gphij, K21);
+#pragma unroll
+          for (int i = 0; i < 3; i++) {
+            if (i >= nht) break;
+            const d3 p0i = ld3(T.hp0[i]);
+            const d3 phi = 0.5 * (rt - p0i);
+            const z1 t = zsub(zmul(ksq, rdot(phi, GK)), L2);
+            zacc(L[i * 3 + j], zscale(w, t));
+            const d3 vts = p0j - p0i;
+            const z3 KK = z3add(z3add_r(DGxphij, cross(vts, ISn3hn)), K41);
+            const z1 kk = rdot(phi, KK);
+            K[i * 3 + j].r -= w * kk.r;
+            K[i * 3 + j].i -= w * kk.i;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      L[k].r = warp_sum(L[k].r); L[k].i = warp_sum(L[k].i);
+      K[k].r = warp_sum(K[k].r); K[k].i = warp_sum(K[k].i);
+    }
+    if (!np.same) {
+      // neighbour-edge K correction, src/Impedance.cpp:301-324: three source
+      // edges x QuadratureGauss15, LKNeighborEdgeIntegrand over t[0].
+      d3 Ke[3][3];
+#pragma unroll
+      for (int e = 0; e < 3; e++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) Ke[e][i] = {0, 0, 0};
+      const d3 nT = ld3(T.n);
+      for (int idx = lane; idx < 45; idx += 32) {
+        const int e = idx / 15, q = idx - e * 15;
+        const d3 v0 = e == 0 ? ld3(S.p0) : (e == 1 ? ld3(S.p1) : ld3(S.p2));
+        const d3 v1 = e == 0 ? ld3(S.v01) : (e == 1 ? ld3(S.v12) : ld3(S.v20));
+        const d3 v = v0 + c_line15[q][0] * v1;
+        const double w = c_line15[q][1];
+        double ISn1;
+        d3 IL1;
+        lk_edge_integral(T, v, ISn1, IL1);
+        const double h = dot(v - Pt, nT);
+        const d3 rho = v - h * nT;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          if (i >= nht) break;
+          const d3 c = IL1 + ISn1 * (rho - ld3(T.hp0[i]));
+          if (e == 0) Ke[0][i] = Ke[0][i] + w * c;
+          else if (e == 1) Ke[1][i] = Ke[1][i] + w * c;
+          else Ke[2][i] = Ke[2][i] + w * c;
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 3; e++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          Ke[e][i].x = warp_sum(Ke[e][i].x);
+          Ke[e][i].y = warp_sum(Ke[e][i].y);
+          Ke[e][i].z = warp_sum(Ke[e][i].z);
+        }
+      const double c = 0.125 * T.Ai * S.Ai;
+      const d3 m01 = ld3(S.m01), m12 = ld3(S.m12), m20 = ld3(S.m20);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          if (i >= nht || j >= nhs) continue;
+          const d3 v = ld3(T.hp0[i]) - ld3(S.hp0[j]);
+          K[i * 3 + j].r += c * (dot(cross(v, m01), Ke[0][i]) / S.nv01i + dot(cross(v, m12), Ke[1][i]) / S.nv12i +
+                                 dot(cross(v, m20), Ke[2][i]) / S.nv20i);
+        }
+    }
+    if (lane < nht * nhs) {
+      const int i = lane / nhs, j = lane - (lane / nhs) * nhs;
+      z1 Lv = {0, 0}, Kv = {0, 0};
+#pragma unroll
+      for (int k = 0; k < 9; k++)
+        if (k == i * 3 + j) { Lv = L[k]; Kv = K[k]; }
+      const double c = scatter_coef(T, i, S, j);
+      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, Lv), zscale(c, Kv));
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------- gather: half-pair blocks -> Z ----------------
+struct ZDev {
+  double zer, zei, zmr, zmi;  // Zeps, Zmu
+};
+
+__device__ __forceinline__ void block_sum(const HalfPairBlock &b, z1 &sL, z1 &sK) {
+  const double2 *p = reinterpret_cast<const double2 *>(b.v);
+  sL = {0, 0};
+  sK = {0, 0};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const double2 l = p[2 * k], kk = p[2 * k + 1];
+    sL.r += l.x; sL.i += l.y;
+    sK.r += kk.x; sK.i += kk.y;
+  }
+}
+
+__device__ __forceinline__ void write_2x2(double *Z, int64_t ld, int i, int j, z1 Ze, z1 Zm, z1 sL, z1 sK) {
+  // src/Impedance.cpp:378-381
+  const z1 a = zmul(Ze, sL), d = zmul(Zm, sL);
+  double2 *c0 = reinterpret_cast<double2 *>(Z + 2 * ((int64_t)2 * i + ld * (2 * (int64_t)j)));
+  double2 *c1 = reinterpret_cast<double2 *>(Z + 2 * ((int64_t)2 * i + ld * (2 * (int64_t)j + 1)));
+  c0[0] = make_double2(a.r, a.i);
+  c0[1] = make_double2(-sK.r, -sK.i);
+  c1[0] = make_double2(sK.r, sK.i);
+  c1[1] = make_double2(d.r, d.i);
+}
+
+__global__ void gather_z_kernel(const HalfPairBlock *__restrict__ H, int ntr, int nsr, ZDev z, double *Z, int64_t ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= ntr) return;
+  z1 sL, sK;
+  block_sum(H[(size_t)j * ntr + i], sL, sK);
+  write_2x2(Z, ld, i, j, {z.zer, z.zei}, {z.zmr, z.zmi}, sL, sK);
+}
+
+// W = Z_ext + blockdiag(G1, G2) and the G blocks themselves (src/HeatTransfer.cpp:26-35).
+__global__ void gather_w_kernel(const HalfPairBlock *__restrict__ He, const HalfPairBlock *__restrict__ H1,
+                                const HalfPairBlock *__restrict__ H2, int ns, int nt, ZDev ze, ZDev z1d, ZDev z2d,
+                                double *W, int64_t ldw, double *G1, int64_t ld1, double *G2, int64_t ld2) {
+  const int n = ns + nt;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= n) return;
+  z1 sL, sK;
+  block_sum(He[(size_t)j * n + i], sL, sK);
+  z1 a = zmul({ze.zer, ze.zei}, sL), d = zmul({ze.zmr, ze.zmi}, sL), k = sK;
+  const bool in1 = i < ns && j < ns, in2 = i >= ns && j >= ns;
+  if (in1 || in2) {
+    z1 gL, gK;
+    const ZDev &zz = in1 ? z1d : z2d;
+    const int li = in1 ? i : i - ns, lj = in1 ? j : j - ns, nn = in1 ? ns : nt;
+    block_sum((in1 ? H1 : H2)[(size_t)lj * nn + li], gL, gK);
+    write_2x2(in1 ? G1 : G2, in1 ? ld1 : ld2, li, lj, {zz.zer, zz.zei}, {zz.zmr, zz.zmi}, gL, gK);
+    const z1 ga = zmul({zz.zer, zz.zei}, gL), gd = zmul({zz.zmr, zz.zmi}, gL);
+    a = zadd(a, ga);
+    d = zadd(d, gd);
+    k = zadd(k, gK);
+  }
+  double2 *c0 = reinterpret_cast<double2 *>(W + 2 * ((int64_t)2 * i + ldw * (2 * (int64_t)j)));
+  double2 *c1 = reinterpret_cast<double2 *>(W + 2 * ((int64_t)2 * i + ldw * (2 * (int64_t)j + 1)));
+  c0[0] = make_double2(a.r, a.i);
+  c0[1] = make_double2(-k.r, -k.i);
+  c1[0] = make_double2(k.r, k.i);
+  c1[1] = make_double2(d.r, d.i);
+}
+
+GreenDev to_dev(const bemgpu_green_t *g) {
+  GreenDev d;
+  d.ikr = g->ik[0]; d.iki = g->ik[1];
+  d.k2r = g->k2[0]; d.k2i = g->k2[1];
+  d.ksqr = g->ksquared[0]; d.ksqi = g->ksquared[1];
+  return d;
+}
+
+ZDev to_zdev(const bemgpu_green_t *g) { return {g->Zeps[0], g->Zeps[1], g->Zmu[0], g->Zmu[1]}; }
+
+bool g_tables_loaded[64] = {false};
+
+int load_tables(bemgpu_ctx_s *ctx) {
+  if (g_tables_loaded[ctx->device]) return BEMGPU_OK;
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule6, bemgpu_tri_rule6, sizeof(bemgpu_tri_rule6)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule10, bemgpu_tri_rule10, sizeof(bemgpu_tri_rule10)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule15, bemgpu_tri_rule15, sizeof(bemgpu_tri_rule15)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule21, bemgpu_tri_rule21, sizeof(bemgpu_tri_rule21)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule36, bemgpu_tri_rule36, sizeof(bemgpu_tri_rule36)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule91, bemgpu_tri_rule91, sizeof(bemgpu_tri_rule91)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule105, bemgpu_tri_rule105, sizeof(bemgpu_tri_rule105)));
+  BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_line15, bemgpu_line_rule15, sizeof(bemgpu_line_rule15)));
+  g_tables_loaded[ctx->device] = true;
+  return BEMGPU_OK;
+}
+
+}  // namespace
+
+int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s, const bemgpu_green_t *g,
+                   const bemgpu_options_t *opt, HalfPairBlock *H, cudaStream_t stream, int64_t *n_near,
+                   int64_t *n_far) {
+  int rc = load_tables(ctx);
+  if (rc) return rc;
+  const NearList *nl = bem_near_list(ctx, t, s);
+  if (!nl) return bem_fail(ctx, BEMGPU_ERR_OOM, "near list allocation failed");
+  GreenDev gd = to_dev(g);
+  FarOpts fo = {opt->farThresh6, opt->farThresh10, opt->farThresh15, opt->farThresh21};
+  dim3 blk(32, 4);
+  dim3 grd((s->ntri + 31) / 32, (t->ntri + 3) / 4);
+  double far_flops = 0, far_bytes = 0, near_flops = 0, near_bytes = 0;
+  if (ctx->prof) {
+    const int64_t *fc = bem_far_rule_counts(ctx, t, s, opt);
+    const int P[5] = {6, 10, 15, 21, 36};
+    int64_t nfar = 0;
+    for (int k = 0; k < 5; k++) { far_flops += fc[k] * bem_far_pair_flops(P[k]); nfar += fc[k]; }
+    // half-pair products written: 9 per pair on average (nh_t * nh_s)
+    far_bytes = (double)nfar * 9.0 * BEM_HALFPAIR_BYTES_FP64;
+    near_flops = (double)nl->n * bem_near_pair_flops(true);
+    near_bytes = (double)nl->n * 9.0 * BEM_HALFPAIR_BYTES_FP64;
+  }
+  {
+    ProfScope ps(ctx, BEMGPU_K_FILL_FAR, stream, far_flops, far_bytes);
+    far_pairs_fp64_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg);
+    ctx->launches++;
+  }
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  if (nl->n > 0) {
+    int64_t blocks = (nl->n + NEAR_WARPS - 1) / NEAR_WARPS;
+    int nb = (int)std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 16);
+    ProfScope ps(ctx, BEMGPU_K_FILL_NEAR, stream, near_flops, near_bytes);
+    near_pairs_fp64_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
+    ctx->launches++;
+  }
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  if (n_near) *n_near = nl->n;
+  if (n_far) *n_far = (int64_t)t->ntri * s->ntri - nl->n;
+  return BEMGPU_OK;
+}
+
+int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, const bemgpu_green_t *g, double *Z,
+                 int64_t ld, cudaStream_t stream) {
+  dim3 blk(128);
+  dim3 grd((ntr + 127) / 128, nsr);
+  ProfScope ps(ctx, BEMGPU_K_GATHER, stream, (double)ntr * nsr * (6 * 8 + 2 * 6), (double)ntr * nsr * (128 + 64));
+  gather_z_kernel<<<grd, blk, 0, stream>>>(H, ntr, nsr, to_zdev(g), Z, ld);
+  ctx->launches++;
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+int bem_gather_w(bemgpu_ctx_s *ctx, const HalfPairBlock *Hext, const HalfPairBlock *H1, const HalfPairBlock *H2,
+                 int ns, int nt, const bemgpu_green_t *gext, const bemgpu_green_t *g1, const bemgpu_green_t *g2,
+                 double *W, int64_t ldw, double *G1, int64_t ld1, double *G2, int64_t ld2, cudaStream_t stream) {
+  dim3 blk(128);
+  dim3 grd((ns + nt + 127) / 128, ns + nt);
+  const double nn = (double)(ns + nt) * (ns + nt), nd = (double)ns * ns + (double)nt * nt;
+  ProfScope ps(ctx, BEMGPU_K_GATHER, stream, nn * 60 + nd * 80, nn * 192 + nd * 192);
+  gather_w_kernel<<<grd, blk, 0, stream>>>(Hext, H1, H2, ns, nt, to_zdev(gext), to_zdev(g1), to_zdev(g2), W, ldw, G1,
+                                           ld1, G2, ld2);
+  ctx->launches++;
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+// ---------------- public Zts ----------------
+extern "C" int bemgpu_zts(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
+                          const bemgpu_options_t *opt, int precision, void *dZ, int64_t ldz, void *stream) {
+  if (!ctx || !t || !s || !g || !dZ) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: null argument");
+  if (t->geom != s->geom) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: t and s must share one geometry");
+  if (ldz < 2 * (int64_t)t->nrwg) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: ldz < 2*size(t)");
+  if (precision != BEMGPU_PREC_FP64) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: precision %d not available", precision);
+  bemgpu_options_t o;
+  if (opt) o = *opt; else bemgpu_options_default(&o);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  HalfPairBlock *H = (HalfPairBlock *)bem_workspace(ctx, "H0", sizeof(HalfPairBlock) * (size_t)t->nrwg * s->nrwg);
+  if (!H) return bem_fail(ctx, BEMGPU_ERR_OOM, "zts: workspace allocation failed");
+  int rc = bem_fill_pairs(ctx, t, s, g, &o, H, st, nullptr, nullptr);
+  if (rc) return rc;
+  return bem_gather_z(ctx, H, t->nrwg, s->nrwg, g, (double *)dZ, ldz, st);
+}
+
+extern "C" int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
+                               const bemgpu_options_t *opt, int precision, double *Z, int64_t ldz) {
+  if (!ctx || !t || !s || !Z) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_host: null argument");
+  const int64_t m = 2 * (int64_t)t->nrwg, n = 2 * (int64_t)s->nrwg;
+  if (ldz < m) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_host: ldz < 2*size(t)");
+  double *dZ = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    dZ = (double *)bem_workspace(ctx, "Zhost", sizeof(double) * 2 * m * n);
+    if (!dZ) return bem_fail(ctx, BEMGPU_ERR_OOM, "zts_host: workspace allocation failed");
+  }
+  int rc = bemgpu_zts(ctx, t, s, g, opt, precision, dZ, m, nullptr);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  BEM_CUDA_TRY(ctx, cudaMemcpy2DAsync(Z, sizeof(double) * 2 * ldz, dZ, sizeof(double) * 2 * m, sizeof(double) * 2 * m,
+                                      n, cudaMemcpyDeviceToHost, ctx->stream));
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BEMGPU_OK;
+}

@@ -1,0 +1,195 @@
+// Per-frequency driver: CalcHeatTransfer (src/HeatTransfer.cpp:8-59) on the GPU.
+//
+//   W = Zext(top,top) + blockdiag(G1, G2)          (fill + gather, one pass)
+//   X = W^{-1}[s rows, t cols]                      (LU, then solve with the t
+//                                                   columns of the identity; the
+//                                                   reference forms the whole inverse)
+//   B1 = sym(G1) X,  B2 = X sym(G2)                 (the [s,t] blocks the reference
+//                                                   keeps after its two full products)
+//   S  = 1/4 sum conj(B2) o B1  = 1/4 Tr(B2^H B1)   (multiply_Adagger_B + trace)
+//   P  = Re(S) (Theta(omega,T1) - Theta(omega,T2))
+#include "bemgpu_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+namespace {
+
+__global__ void sym_kernel(double *G, int64_t ld, int m) {
+  // symm, src/util/DenseMatrix.cpp:477-486: G <- G + G^H
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= m || i < j) return;
+  double2 *g = reinterpret_cast<double2 *>(G);
+  if (i == j) {
+    double2 d = g[i + ld * (int64_t)i];
+    g[i + ld * (int64_t)i] = make_double2(d.x + d.x, 0.0);
+    return;
+  }
+  const double2 a = g[i + ld * (int64_t)j], b = g[j + ld * (int64_t)i];
+  const double2 nij = make_double2(a.x + b.x, a.y - b.y);
+  g[i + ld * (int64_t)j] = nij;
+  g[j + ld * (int64_t)i] = make_double2(nij.x, -nij.y);
+}
+
+__global__ void identity_cols_kernel(double *Y, int64_t ld, int n, int row0, int ncols) {
+  // Y (n x ncols) = columns row0..row0+ncols of the n x n identity
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (r >= n) return;
+  reinterpret_cast<double2 *>(Y)[r + ld * (int64_t)c] = make_double2(r == row0 + c ? 1.0 : 0.0, 0.0);
+}
+
+constexpr int TR_THREADS = 256;
+
+// Partial sums of conj(B2) o B1 over a column-major (m x n) pair, fixed order.
+__global__ void trace_partial_kernel(const double *B1, const double *B2, int64_t ld, int m, int n, double *partial) {
+  __shared__ double sr[TR_THREADS], si[TR_THREADS];
+  const int64_t total = (int64_t)m * n;
+  double ar = 0, ai = 0;
+  for (int64_t idx = (int64_t)blockIdx.x * TR_THREADS + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * TR_THREADS) {
+    const int64_t r = idx % m, c = idx / m;
+    const double2 b1 = reinterpret_cast<const double2 *>(B1)[r + ld * c];
+    const double2 b2 = reinterpret_cast<const double2 *>(B2)[r + ld * c];
+    ar += b2.x * b1.x + b2.y * b1.y;
+    ai += b2.x * b1.y - b2.y * b1.x;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int s = TR_THREADS / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = sr[0];
+    partial[2 * blockIdx.x + 1] = si[0];
+  }
+}
+
+__global__ void trace_final_kernel(const double *partial, int np, double *out) {
+  if (threadIdx.x != 0) return;
+  double r = 0, i = 0;
+  for (int k = 0; k < np; k++) {
+    r += partial[2 * k];
+    i += partial[2 * k + 1];
+  }
+  out[0] = 0.25 * r;
+  out[1] = 0.25 * i;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+}  // namespace
+
+extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
+                                    const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
+                                    double *P_out, bemgpu_solve_info_t *info) {
+  if (!ctx || !top || !s || !t || !req || !P_out) return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: null argument");
+  if (top->geom != s->geom || top->geom != t->geom)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: trees must share one geometry");
+  if (top->nrwg != s->nrwg + t->nrwg)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: size(top) != size(s) + size(t)");
+  if (precision != BEMGPU_PREC_FP64)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: precision %d not available", precision);
+  bemgpu_options_t o;
+  if (opt) o = *opt; else bemgpu_options_default(&o);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+
+  const int Ns = s->nrwg, Nt = t->nrwg, N = Ns + Nt;
+  const int n = 2 * N, ns2 = 2 * Ns, nt2 = 2 * Nt;
+  const double omega = bemgpu_dimensionless_omega(req->a, req->eV);
+  const double om[2] = {omega, 0.0}, one_c[2] = {1.0, 0.0};
+  bemgpu_green_t gext, g1, g2;
+  bemgpu_green_init(one_c, one_c, om, 1, &gext);
+  bemgpu_green_init(req->eps1, req->mu1, om, 0, &g1);
+  bemgpu_green_init(req->eps2, req->mu2, om, 0, &g2);
+
+  HalfPairBlock *He = (HalfPairBlock *)bem_workspace(ctx, "Hext", sizeof(HalfPairBlock) * (size_t)N * N);
+  HalfPairBlock *H1 = (HalfPairBlock *)bem_workspace(ctx, "Hint1", sizeof(HalfPairBlock) * (size_t)Ns * Ns);
+  HalfPairBlock *H2 = (HalfPairBlock *)bem_workspace(ctx, "Hint2", sizeof(HalfPairBlock) * (size_t)Nt * Nt);
+  double *W = (double *)bem_workspace(ctx, "W", sizeof(double) * 2 * (size_t)n * n);
+  double *G1 = (double *)bem_workspace(ctx, "G1", sizeof(double) * 2 * (size_t)ns2 * ns2);
+  double *G2 = (double *)bem_workspace(ctx, "G2", sizeof(double) * 2 * (size_t)nt2 * nt2);
+  double *Y = (double *)bem_workspace(ctx, "Y", sizeof(double) * 2 * (size_t)n * nt2);
+  double *B1 = (double *)bem_workspace(ctx, "B1", sizeof(double) * 2 * (size_t)ns2 * nt2);
+  double *B2 = (double *)bem_workspace(ctx, "B2", sizeof(double) * 2 * (size_t)ns2 * nt2);
+  int *ipiv = (int *)bem_workspace(ctx, "ipiv", sizeof(int) * (size_t)n);
+  int *dinfo = (int *)bem_workspace(ctx, "info", sizeof(int));
+  const int TRB = 1024;
+  double *partial = (double *)bem_workspace(ctx, "trace_partial", sizeof(double) * 2 * TRB + 16);
+  if (!He || !H1 || !H2 || !W || !G1 || !G2 || !Y || !B1 || !B2 || !ipiv || !dinfo || !partial)
+    return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
+  double *dS = partial + 2 * TRB;
+
+  cudaEvent_t *ev = ctx->ev;
+  cudaEventRecord(ev[0], st);
+  int64_t near1 = 0, far1 = 0, near2 = 0, far2 = 0, near3 = 0, far3 = 0;
+  int rc = bem_fill_pairs(ctx, top, top, &gext, &o, He, st, &near1, &far1);
+  if (!rc) rc = bem_fill_pairs(ctx, s, s, &g1, &o, H1, st, &near2, &far2);
+  if (!rc) rc = bem_fill_pairs(ctx, t, t, &g2, &o, H2, st, &near3, &far3);
+  if (!rc) rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st);
+  if (rc) return rc;
+  cudaEventRecord(ev[1], st);
+  rc = bem_zgetrf(ctx, W, n, n, ipiv, dinfo, st);
+  if (rc) return rc;
+  cudaEventRecord(ev[2], st);
+  {
+    ProfScope ps(ctx, BEMGPU_K_SOLVE_GEMM, st, 0.0, 16.0 * n * nt2);
+    identity_cols_kernel<<<dim3((n + 255) / 256, nt2), 256, 0, st>>>(Y, n, n, ns2, nt2);
+    ctx->launches++;
+  }
+  rc = bem_zgetrs(ctx, W, n, n, ipiv, Y, n, nt2, st);
+  if (rc) return rc;
+  cudaEventRecord(ev[3], st);
+  {
+    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 2.0 * ((double)ns2 * ns2 + (double)nt2 * nt2),
+                 32.0 * ((double)ns2 * ns2 + (double)nt2 * nt2));
+    sym_kernel<<<dim3((ns2 + 255) / 256, ns2), 256, 0, st>>>(G1, ns2, ns2);
+    ctx->launches++;
+    sym_kernel<<<dim3((nt2 + 255) / 256, nt2), 256, 0, st>>>(G2, nt2, nt2);
+    ctx->launches++;
+  }
+  const double zero_c[2] = {0.0, 0.0};
+  rc = bem_zgemm(ctx, BEMGPU_K_TRACE, 'N', ns2, nt2, ns2, one_c, G1, ns2, Y, n, zero_c, B1, ns2, st);
+  if (!rc) rc = bem_zgemm(ctx, BEMGPU_K_TRACE, 'N', ns2, nt2, nt2, one_c, Y, n, G2, nt2, zero_c, B2, ns2, st);
+  if (rc) return rc;
+  {
+    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 8.0 * ns2 * nt2, 32.0 * ns2 * nt2);
+    trace_partial_kernel<<<TRB, TR_THREADS, 0, st>>>(B1, B2, ns2, ns2, nt2, partial);
+    ctx->launches++;
+    trace_final_kernel<<<1, 32, 0, st>>>(partial, TRB, dS);
+    ctx->launches++;
+  }
+  cudaEventRecord(ev[4], st);
+  double S[2];
+  int hinfo = 0;
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(S, dS, sizeof S, cudaMemcpyDeviceToHost, st));
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if (hinfo != 0) return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "heat_transfer: zero pivot at column %d", hinfo);
+  *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
+  if (info) {
+    memset(info, 0, sizeof *info);
+    info->ms_fill = elapsed(ev[0], ev[1]);
+    info->ms_lu = elapsed(ev[1], ev[2]);
+    info->ms_solve = elapsed(ev[2], ev[3]);
+    info->ms_trace = elapsed(ev[3], ev[4]);
+    info->S_re = S[0];
+    info->S_im = S[1];
+    info->pairs_near = near1 + near2 + near3;
+    info->pairs_far_fp64 = far1 + far2 + far3;
+  }
+  return BEMGPU_OK;
+}

@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Benchmark: spectral-power solves/s of the per-frequency hot path
+(fill -> LU -> trace, CalcHeatTransfer) on one GB300, plus Z-fill entries/s.
+
+Workload (default): two jittered icospheres, radius 1 um, subdivision level 3
+(1280 triangles, 1920 RWG edges per body, N = 7680 complex unknowns), SiC
+Lorentz model, gaps {20, 50, 100, 200, 500, 1000} nm x 64 frequencies in
+0.08-0.13 eV; a step is one (gap, frequency) solve, steps walk that grid.
+Synthetic meshes from bem_gb300.mesh (seeded), no dataset.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp64|mixed] [--workload ico3|cube4|ico2]
+
+--impl reference times the reference path's CPU implementation on the host
+cores (the oracle port: oracle/bem_oracle.c fill + numpy LAPACK algebra), on a
+bounded sample of each step's work.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "spectral-power solves/s"
+SIC = (6.7, 0.0983, 0.120, 0.00059)
+
+WORKLOADS = {
+    # name: (generator kwargs, gaps um, freqs)
+    "ico3": dict(kind="ico", level=3, gaps=[0.02, 0.05, 0.1, 0.2, 0.5, 1.0], freqs=np.linspace(0.08, 0.13, 64)),
+    "ico2": dict(kind="ico", level=2, gaps=[0.02, 0.05, 0.1, 0.2, 0.5, 1.0], freqs=np.linspace(0.08, 0.13, 64)),
+    "cube4": dict(kind="cube", nsub=4, gaps=[0.1], freqs=np.linspace(0.08, 0.13, 20)),
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_bodies(wl):
+    from bem_gb300 import mesh
+    if wl["kind"] == "ico":
+        v, t = mesh.icosphere(1.0, wl["level"], jitter=0.02, seed=12345)
+    else:
+        v, t = mesh.cube(1.0, wl["nsub"])
+    b2 = mesh.Body.from_mesh(v, t)
+    bodies = []
+    for gap in wl["gaps"]:
+        b1 = b2.translated(mesh.gap_translation(v, v, gap))
+        bodies.append((b1, b2))
+    return bodies
+
+
+def step_grid(wl):
+    return [(gi, float(f)) for gi in range(len(wl["gaps"])) for f in wl["freqs"]]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# Nominal GB300 FP64 rate (vector and tensor): MEASURED_PEAKS.json carries HBM and
+# bf16 only, so FP64-bound kernels are compared with this nominal figure.
+FP64_NOMINAL_TFLOPS = 1.25
+
+
+def run_ours(args, rank, world):
+    import ctypes
+    import torch
+    from bem_gb300 import api, _lib
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    wl = WORKLOADS[args.workload]
+    prec = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[args.precision]
+    ctx = api.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    L = _lib.load()
+    diel = api.FixedLorentz(*SIC)
+    bodies = make_bodies(wl)
+    systems = [api.parseShapes(b1, b2, diel, diel, ctx) for (b1, b2) in bodies]
+    grid = step_grid(wl)
+    # each rank walks its own slice of the (gap, f) grid: independent solves, no collective
+    order = grid[rank::world] if world > 1 else grid
+    a = 1e-6
+
+    def solve(k, info=None, sysset=None):
+        gi, f = order[k % len(order)]
+        top, s, t = (sysset or systems)[gi]
+        return api.CalcHeatTransfer(a, f, 300.0, 0.0, top, s, t, precision=prec, info=info)
+
+    sp = ctypes.c_void_p()
+    L.bemgpu_ctx_stream(ctx.handle, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    for k in range(args.warmup):
+        solve(k)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    L.bemgpu_prof_enable(ctx.handle, 1)
+    launches0 = L.bemgpu_ctx_launches(ctx.handle)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    infos = []
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ev0.record(stream)
+        Ps = []
+        for k in range(args.steps):
+            info = {}
+            Ps.append(solve(args.warmup + k, info))
+            infos.append(info)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = L.bemgpu_ctx_launches(ctx.handle) - launches0
+    ms = ev0.elapsed_time(ev1)
+    stats = {}
+    for kk, name in enumerate(_lib.K_NAMES):
+        n = ctypes.c_int64()
+        t_ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        L.bemgpu_prof_query(ctx.handle, kk, ctypes.byref(n), ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by))
+        stats[name] = dict(launches=n.value, ms=t_ms.value, flops=fl.value, bytes=by.value)
+    L.bemgpu_prof_enable(ctx.handle, 0)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # e2e through the public API from host buffers: geometry + trees uploaded
+    # from host arrays inside the timed region every step, result read back.
+    from bem_gb300 import mesh as _mesh
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_ev0 = torch.cuda.Event(enable_timing=True)
+    e2e_ev1 = torch.cuda.Event(enable_timing=True)
+    e2e_ev0.record(stream)
+    h2d = 0
+    for k in range(args.steps):
+        gi, f = order[(args.warmup + k) % len(order)]
+        b1, b2 = bodies[gi]
+        xyz, tris, rwg, ns = _mesh.two_body(b1, b2)
+        sysk = api.parseShapes(b1, b2, diel, diel, ctx)
+        h2d += xyz.nbytes + tris.nbytes + rwg.nbytes * 2
+        api.CalcHeatTransfer(a, f, 300.0, 0.0, *sysk, precision=prec)
+        del sysk
+    e2e_ev1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e2e_ev0.elapsed_time(e2e_ev1)
+    e2e_wall = (time.perf_counter() - t0) * 1e3
+    e2e_ms = max(e2e_ms, e2e_wall)
+
+    n_unknowns = 2 * systems[0][0].rwgs
+    ns2 = 2 * systems[0][1].rwgs
+    nt2 = 2 * systems[0][2].rwgs
+    entries = n_unknowns ** 2 + ns2 ** 2 + nt2 ** 2
+    value = args.steps * world / (ms / 1e3)
+    fill_ms = sum(i["ms_fill"] for i in infos) / len(infos)
+    pk, pk_kind = peaks()
+    # dominant kernel class by device time
+    dom = max(stats, key=lambda k: stats[k]["ms"])
+    d = stats[dom]
+    fp64_bound = args.precision == "fp64" or dom in ("fill_near",)
+    if d["flops"] > 0:
+        achieved = d["flops"] / (d["ms"] / 1e3) / 1e12
+        peak = FP64_NOMINAL_TFLOPS if fp64_bound else pk.get("bf16_tflops_sustained", 1700.0)
+        roof = {"kernel": dom, "bound": "fp64" if fp64_bound else "tensor", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak,
+                "peak_source": "nominal GB300 FP64 (not in MEASURED_PEAKS.json)" if fp64_bound
+                else f"{pk_kind} bf16 sustained",
+                "launches": d["launches"], "avg_launch_ms": d["ms"] / max(1, d["launches"]),
+                "traffic": None}
+    else:
+        achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "peak_source": pk_kind, "traffic": None}
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
+        "data": "synthetic (seeded jittered icospheres; no dataset)",
+        "config": {"workload": f"{args.workload}: two r=1um icospheres L3 (1280 tris, 1920 RWGs each), N={n_unknowns}, SiC, "
+                               f"gaps {wl['gaps']} um x {len(wl['freqs'])} f in 0.08-0.13 eV" if args.workload == "ico3"
+                   else args.workload,
+                   "precision": args.precision, "N": n_unknowns, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_unknowns ** 2 * 16 / 1e6)},
+        "fill_gentries_per_s": entries / (fill_ms / 1e3) / 1e9,
+        "stage_ms": {k: sum(i[k] for i in infos) / len(infos) for k in ("ms_fill", "ms_lu", "ms_solve", "ms_trace")},
+        "kernel_ms_per_step": {k: v["ms"] / args.steps for k, v in stats.items()},
+        "roofline": roof,
+        "gpu_launches": int(launches),
+        "e2e": {"value": args.steps / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": 8 + 16 + 4},
+        "clocks": clk.summary(),
+        "P_sample": Ps[:2],
+    }
+    return out
+
+
+def run_reference_sample(wl_name, threads=None, frac=None):
+    """Times the oracle port (the reference path restated on the CPU) on a
+    bounded sample of one solve: the three fills over a fraction of the test
+    triangles (scaled up), and the dense algebra at full size."""
+    from bem_gb300 import mesh
+    from oracle import oracle
+    wl = WORKLOADS[wl_name]
+    (b1, b2) = make_bodies(wl)[0]
+    xyz, tris, rwg, ns = mesh.two_body(b1, b2)
+    ntri = b1.nt + b2.nt
+    frac = frac or (1.0 if ntri <= 500 else 64.0 / ntri)
+    threads = threads or os.cpu_count() or 1
+    f = float(wl["freqs"][0])
+    om = oracle.dimensionless_omega(1e-6, f)
+    eps = oracle.lorentz_eps(f, *SIC)
+    t0 = time.perf_counter()
+    k = max(1, int(round(frac * ntri)))
+    oracle.zts(xyz, tris, rwg, rwg, 1 + 0j, 1 + 0j, om, tri_range=(0, k), nthreads=threads)
+    k1 = max(1, int(round(frac * b1.nt)))
+    oracle.zts(xyz, tris, rwg[:ns], rwg[:ns], eps, 1 + 0j, om, tri_range=(0, k1), nthreads=threads)
+    oracle.zts(xyz, tris, rwg[ns:], rwg[ns:], eps, 1 + 0j, om, tri_range=(0, k1), nthreads=threads)
+    t_fill = (time.perf_counter() - t0) * (ntri / k)
+    n = 2 * rwg.shape[0]
+    rng = np.random.default_rng(0)
+    W = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + n * np.eye(n)
+    t0 = time.perf_counter()
+    Wi = np.linalg.inv(W)
+    ns2 = 2 * ns
+    G = W[:ns2, :ns2]
+    B1 = (G @ Wi[:ns2, :])[:, ns2:]
+    B2 = (Wi[:, ns2:] @ W[ns2:, ns2:])[:ns2, :]
+    _ = np.trace(B2.conj().T @ B1)
+    t_la = time.perf_counter() - t0
+    return {"solve_s": t_fill + t_la, "fill_s": t_fill, "la_s": t_la, "threads": threads,
+            "sample": f"fills over {k}/{ntri} test triangles (x{ntri / k:.1f}) + full-size inverse/products, "
+                      f"n={n}, one frequency"}
+
+
+def run_reference(args, rank, world):
+    wl = WORKLOADS[args.workload]
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    samples = []
+    for k in range(max(1, args.steps)):
+        samples.append(run_reference_sample(args.workload))
+    s = statistics.median(x["solve_s"] for x in samples)
+    v = 1.0 / s
+    return {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded meshes; no dataset)",
+            "config": {"workload": args.workload, "N": None}, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": samples[0]["threads"], "kind": "port",
+                             "sample": samples[0]["sample"]},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="ico3", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args, rank, world)))
+        return
+    out = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline and world == 1:
+            r = run_reference_sample(args.workload)
+            out["cpu_baseline"] = {"value": 1.0 / r["solve_s"], "unit": "solves/s", "cores": r["threads"],
+                                   "kind": "port", "sample": r["sample"]}
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/*
+ * bemgpu — C ABI of the GB300 (sm_103a) implementation of bem's per-frequency
+ * hot path: PMCHWT RWG impedance fill, dense complex LU, heat-transfer trace.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (BEMGPU_OK or a negative BEMGPU_ERR_*).  Device buffers are owned by the
+ * handles; a host-side caller never needs a CUDA type.  Streams are passed as
+ * opaque void* (cudaStream_t), NULL meaning the context's own stream.
+ *
+ * Reference interfaces replaced (claytonotey/bem):
+ *   bemgpu_green_init   -> GreensFunction::init            src/GreensFunction.cpp:17-30
+ *   bemgpu_zts[_host]   -> Zts(RWGTree*,RWGTree*,GreensFunction*,Options&)
+ *                                                          src/Impedance.h:21, src/Impedance.cpp:388-413
+ *   bemgpu_heat_transfer-> CalcHeatTransfer(a,eV,T1,T2,top,s,t,Options&)
+ *                                                          src/HeatTransfer.h:33, src/HeatTransfer.cpp:8-59
+ *   bemgpu_theta        -> Theta(omega,T)                  src/HeatTransfer.cpp:3-6
+ *   bemgpu_geom_create / bemgpu_tree_create
+ *                       -> the RWGTree a caller builds (src/RWGTree.cpp:602-722),
+ *                          flattened: the RWG order of the table is the matrix order.
+ */
+#ifndef BEMGPU_H
+#define BEMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define BEMGPU_OK 0
+#define BEMGPU_ERR_ARG (-1)          /* invalid argument (sizes, indices, null pointers) */
+#define BEMGPU_ERR_OOM (-2)          /* device allocation failed / over the admission budget */
+#define BEMGPU_ERR_CUDA (-3)         /* a CUDA runtime call failed */
+#define BEMGPU_ERR_SINGULAR (-4)     /* zero pivot in the LU */
+#define BEMGPU_ERR_NO_CONVERGE (-5)  /* iterative refinement did not reach its tolerance */
+#define BEMGPU_ERR_TIMEOUT (-6)      /* a bounded device wait ran out */
+#define BEMGPU_ERR_MESH (-7)         /* mesh/RWG table is not a valid closed RWG table */
+
+/* ---- precision modes ---- */
+#define BEMGPU_PREC_FP64 0    /* plain path: every stage in FP64 / complex128 */
+#define BEMGPU_PREC_MIXED 1   /* FP32 far pairs (centroid distance > 3 edge lengths), FP64
+                                 near/singular; complex64 tensor-core LU + FP64 refinement */
+
+typedef struct bemgpu_ctx_s *bemgpu_ctx_t;
+typedef struct bemgpu_geom_s *bemgpu_geom_t;
+typedef struct bemgpu_tree_s *bemgpu_tree_t;
+
+/* GreensFunction fields (src/GreensFunction.h:7-28), complex values as {re, im}. */
+typedef struct {
+  double eps[2], mu[2], omega[2];
+  double ksquared[2], k[2], ik[2], k2[2], Zeps[2], Zmu[2];
+  int external;
+} bemgpu_green_t;
+
+/* The Options fields on the fill path (src/Options.h; defaults src/Options.cpp:23-26). */
+typedef struct {
+  double farThresh6, farThresh10, farThresh15, farThresh21;
+} bemgpu_options_t;
+
+/* One frequency point of CalcHeatTransfer. */
+typedef struct {
+  double a;          /* length scale of the mesh coordinates, metres */
+  double eV;         /* photon energy */
+  double T1, T2;     /* body temperatures, K */
+  double eps1[2], mu1[2], eps2[2], mu2[2]; /* body material constants at eV */
+} bemgpu_solve_req_t;
+
+/* Per-solve diagnostics (any pointer argument may be NULL). */
+typedef struct {
+  double ms_fill, ms_lu, ms_solve, ms_trace, ms_refine; /* stage times, device clock */
+  double S_re, S_im;        /* 0.25 * Tr(B2^H B1) before the Theta factor */
+  double err_est;           /* estimated relative error of Re S (0 on the FP64 path) */
+  int refine_iters;
+  int64_t pairs_near, pairs_far_fp64, pairs_far_fp32;
+} bemgpu_solve_info_t;
+
+/* ---- context ---- */
+/* Creates a context on a CUDA device (its own stream and workspace). */
+int bemgpu_ctx_create(int device, bemgpu_ctx_t *out);
+int bemgpu_ctx_destroy(bemgpu_ctx_t ctx);
+/* Last error message of this context (static storage, never NULL). */
+const char *bemgpu_ctx_last_error(bemgpu_ctx_t ctx);
+/* Library version string. */
+const char *bemgpu_version(void);
+/* The context's CUDA stream (cudaStream_t) on which all its work is launched. */
+int bemgpu_ctx_stream(bemgpu_ctx_t ctx, void **stream);
+/* Number of kernels the context launched since it was created. */
+int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx);
+
+/* ---- live kernel statistics (measurement hooks; no counterpart in the reference) ---- */
+/* Kernel classes timed with CUDA events on the context stream while enabled. */
+#define BEMGPU_K_FILL_FAR 0     /* far triangle pairs */
+#define BEMGPU_K_FILL_NEAR 1    /* same / vertex-sharing triangle pairs */
+#define BEMGPU_K_GATHER 2       /* half-pair blocks -> matrix entries */
+#define BEMGPU_K_LU_PANEL 3     /* LU panel columns, row interchanges */
+#define BEMGPU_K_LU_GEMM 4      /* LU trailing-matrix update */
+#define BEMGPU_K_TRSM 5         /* triangular blocks (LU and solve) */
+#define BEMGPU_K_SOLVE_GEMM 6   /* off-diagonal updates of the triangular solves */
+#define BEMGPU_K_TRACE 7        /* sym, the two trace products, the trace reduction */
+#define BEMGPU_K_COUNT 8
+/* Enables (1) or disables (0) event timing of every launch; resets the totals. */
+int bemgpu_prof_enable(bemgpu_ctx_t ctx, int enable);
+/* Totals of one kernel class since the last enable: launches, device ms,
+ * algorithmic flops and algorithmic DRAM bytes (synchronizes the context stream). */
+int bemgpu_prof_query(bemgpu_ctx_t ctx, int kind, int64_t *launches, double *ms, double *flops, double *bytes);
+
+/* ---- resident geometry and RWG trees ---- */
+/* Uploads vertices (xyz[3*nv]) and triangles (tri[3*nt], vertex ids, each
+ * triangle's own vertex order kept).  Vertex identity is the id: two bodies
+ * never share vertex ids (sharedpoints, src/Triangle.h:23-30). */
+int bemgpu_geom_create(bemgpu_ctx_t ctx, const double *xyz, int nv, const int *tri, int nt,
+                       bemgpu_geom_t *out);
+int bemgpu_geom_destroy(bemgpu_geom_t g);
+/* An RWG table over a geometry: rwg[4*i] = {pos triangle, neg triangle, edge
+ * vertex 1, edge vertex 2}; row i is matrix unknown pair (2i: J, 2i+1: M).
+ * Precomputes the half-RWG frames (HalfRWG::HalfRWG, src/RWG.cpp:7-39). */
+int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t *out);
+int bemgpu_tree_destroy(bemgpu_tree_t t);
+int bemgpu_tree_size(bemgpu_tree_t t);
+
+/* ---- Green's function / constants ---- */
+/* GreensFunction::init(eps, mu, omega) (src/GreensFunction.cpp:17-30). */
+int bemgpu_green_init(const double eps[2], const double mu[2], const double omega[2], int external,
+                      bemgpu_green_t *out);
+/* Default Options far-rule thresholds (src/Options.cpp:23-26). */
+void bemgpu_options_default(bemgpu_options_t *opt);
+/* Theta(omega, T) = hbar*omega/(exp(hbar*omega/(kb*T))-1) (src/HeatTransfer.cpp:3-6). */
+double bemgpu_theta(double omega, double T);
+/* Dimensionless frequency omega_SI*a/c used by CalcHeatTransfer (src/HeatTransfer.cpp:10-11). */
+double bemgpu_dimensionless_omega(double a, double eV);
+
+/* ---- impedance fill ---- */
+/* Zts(t, s, g): fills dZ (device, column-major complex128 or complex64 per
+ * precision, leading dimension ldz >= 2*size(t)) with the (2Nt x 2Ns) PMCHWT
+ * block.  t and s must share one geometry.  Asynchronous on `stream`. */
+int bemgpu_zts(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
+               const bemgpu_options_t *opt, int precision, void *dZ, int64_t ldz, void *stream);
+/* Same, writing a host column-major complex128 matrix (synchronous). */
+int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
+                    const bemgpu_options_t *opt, int precision, double *Z, int64_t ldz);
+
+/* ---- per-frequency solve ---- */
+/* CalcHeatTransfer: top is the two-body tree (s's RWGs first, then t's),
+ * s and t the one-body trees, all over one geometry.  Writes the spectral
+ * power Re(S)*(Theta(omega,T1)-Theta(omega,T2)) to *P_out (synchronous). */
+int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
+                         const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
+                         double *P_out, bemgpu_solve_info_t *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEMGPU_H */
