@@ -47,7 +47,8 @@ struct NearPair {
 struct bemgpu_geom_s;
 
 struct bemgpu_tree_s {
-  bemgpu_geom_s *geom = nullptr;
+  bemgpu_ctx_s *ctx = nullptr;
+  bemgpu_geom_s *geom = nullptr;   // kept alive by the tree (reference count)
   int nrwg = 0;
   int ntri = 0;                 // triangles touched by the tree
   std::vector<int> rwg;         // host copy of the table (4*nrwg)
@@ -58,6 +59,7 @@ struct bemgpu_tree_s {
 
 struct bemgpu_geom_s {
   bemgpu_ctx_s *ctx = nullptr;
+  int refs = 1;  // the caller's handle + one per tree; freed at zero
   int nv = 0, nt = 0;
   std::vector<double> xyz;
   std::vector<int> tri;
@@ -70,6 +72,7 @@ struct NearList {
 };
 
 struct bemgpu_ctx_s {
+  int refs = 1;  // the caller's handle + one per geometry; torn down at zero
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;

@@ -210,8 +210,7 @@ int bemgpu_ctx_create(int device, bemgpu_ctx_t *out) {
   return BEMGPU_OK;
 }
 
-int bemgpu_ctx_destroy(bemgpu_ctx_t ctx) {
-  if (!ctx) return BEMGPU_ERR_ARG;
+static void ctx_teardown(bemgpu_ctx_s *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto &kv : ctx->ws) cudaFree(kv.second.first);
@@ -220,6 +219,22 @@ int bemgpu_ctx_destroy(bemgpu_ctx_t ctx) {
   for (auto &e : ctx->ev_pool) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
+}
+
+// The context is torn down when its handle and every geometry created on it
+// are destroyed, in whatever order a caller finalizes them.
+static void ctx_release(bemgpu_ctx_s *ctx) {
+  bool last;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    last = (--ctx->refs == 0);
+  }
+  if (last) ctx_teardown(ctx);
+}
+
+int bemgpu_ctx_destroy(bemgpu_ctx_t ctx) {
+  if (!ctx) return BEMGPU_ERR_ARG;
+  ctx_release(ctx);
   return BEMGPU_OK;
 }
 
@@ -252,13 +267,35 @@ int bemgpu_geom_create(bemgpu_ctx_t ctx, const double *xyz, int nv, const int *t
   g->tris_at_vertex.resize(nv);
   for (int t = 0; t < nt; t++)
     for (int k = 0; k < 3; k++) g->tris_at_vertex[tri[3 * t + k]].push_back(t);
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->refs++;
+  }
   *out = g;
   return BEMGPU_OK;
 }
 
+// The geometry is freed when its handle and every tree over it are destroyed,
+// in whatever order a caller's garbage collector finalizes them.
+// Called with ctx->mu held; returns true when the geometry was freed (the
+// caller then drops the geometry's reference on the context, unlocked).
+static bool geom_release(bemgpu_geom_s *g) {
+  if (--g->refs == 0) {
+    delete g;
+    return true;
+  }
+  return false;
+}
+
 int bemgpu_geom_destroy(bemgpu_geom_t g) {
   if (!g) return BEMGPU_ERR_ARG;
-  delete g;
+  bemgpu_ctx_s *ctx = g->ctx;
+  bool freed;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    freed = geom_release(g);
+  }
+  if (freed) ctx_release(ctx);
   return BEMGPU_OK;
 }
 
@@ -267,6 +304,7 @@ int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t 
   bemgpu_ctx_s *ctx = g->ctx;
   *out = nullptr;
   bemgpu_tree_s *t = new bemgpu_tree_s();
+  t->ctx = ctx;
   t->geom = g;
   t->nrwg = nrwg;
   t->rwg.assign(rwg, rwg + 4 * (size_t)nrwg);
@@ -351,13 +389,19 @@ int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t 
     delete t;
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "tree_create: upload failed");
   }
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    g->refs++;
+  }
   *out = t;
   return BEMGPU_OK;
 }
 
 int bemgpu_tree_destroy(bemgpu_tree_t t) {
   if (!t) return BEMGPU_ERR_ARG;
-  bemgpu_ctx_s *ctx = t->geom->ctx;
+  bemgpu_ctx_s *ctx = t->ctx;
+  bool geom_freed;
+  {
   std::lock_guard<std::mutex> lk(ctx->mu);
   cudaStreamSynchronize(ctx->stream);
   for (auto it = ctx->far_rule_cache.begin(); it != ctx->far_rule_cache.end();) {
@@ -373,7 +417,10 @@ int bemgpu_tree_destroy(bemgpu_tree_t t) {
     }
   }
   cudaFree(t->d_rec);
+  geom_freed = geom_release(t->geom);
   delete t;
+  }
+  if (geom_freed) ctx_release(ctx);
   return BEMGPU_OK;
 }
 

@@ -100,3 +100,25 @@ def test_invalid_mesh_is_rejected():
     with pytest.raises(Exception) as e:
         api.RWGTree(geom, bad)
     assert "MESH" in str(e.value)
+
+
+def test_handles_can_be_released_in_any_order():
+    """A caller's garbage collector may finalize the context, the geometry and
+    the trees in any order (e.g. objects in a reference cycle)."""
+    import ctypes
+    from bem_gb300 import _lib
+    L = _lib.load()
+    v, t = mesh.cube(1.0, 1)
+    b = mesh.Body.from_mesh(v, t)
+    for order in ("ctx-geom-tree", "geom-tree-ctx", "tree-ctx-geom"):
+        ctx, geom, tree = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        assert L.bemgpu_ctx_create(0, ctypes.byref(ctx)) == 0
+        xyz = np.ascontiguousarray(b.verts)
+        tri = np.ascontiguousarray(b.tris, dtype=np.int32)
+        rwg = np.ascontiguousarray(b.rwg, dtype=np.int32)
+        assert L.bemgpu_geom_create(ctx, xyz.ctypes.data, b.nv, tri.ctypes.data, b.nt, ctypes.byref(geom)) == 0
+        assert L.bemgpu_tree_create(geom, rwg.ctypes.data, b.nrwg, ctypes.byref(tree)) == 0
+        rel = {"ctx": lambda: L.bemgpu_ctx_destroy(ctx), "geom": lambda: L.bemgpu_geom_destroy(geom),
+               "tree": lambda: L.bemgpu_tree_destroy(tree)}
+        for name in order.split("-"):
+            assert rel[name]() == 0

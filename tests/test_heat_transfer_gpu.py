@@ -44,8 +44,11 @@ def test_spectral_power_matches_oracle_icosphere2():
         assert info["pairs_near"] > 0 and info["ms_fill"] > 0
 
 
-def test_solve_is_order_independent():
-    """Spectral power is invariant under a permutation of the RWG order."""
+def test_permuted_rwg_order_matches_oracle():
+    """The RWG order fixes each triangle's quadrature frame (the first half-RWG's
+    free vertex, src/Impedance.cpp:283,156) and the 91/105-point rules are not
+    rotation-symmetric, so a permuted order changes P at the quadrature-error
+    level (~1e-4) in the reference as well; parity holds order by order."""
     v, t = mesh.cube(1.0, 2)
     b2 = mesh.Body.from_mesh(v, t)
     b1 = b2.translated(mesh.gap_translation(v, v, 0.1))
@@ -55,7 +58,11 @@ def test_solve_is_order_independent():
     b1p = mesh.Body(b1.verts, b1.tris, b1.rwg[rng.permutation(b1.nrwg)])
     b2p = mesh.Body(b2.verts, b2.tris, b2.rwg[rng.permutation(b2.nrwg)])
     P1 = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, *api.parseShapes(b1p, b2p, d, d))
-    assert abs(P1 / P0 - 1) < 1e-9
+    xyz, tris, rwg, ns = mesh.two_body(b1p, b2p)
+    e = d.eps(0.1)
+    Po = oracle.calc_heat_transfer(1e-6, 0.1, 300.0, 0.0, xyz, tris, rwg, ns, e, e)
+    assert abs(P1 / Po - 1) < TOL
+    assert abs(P1 / P0 - 1) < 1e-2
 
 
 def test_size_mismatch_is_rejected():
