@@ -17,6 +17,7 @@ ERR_ARG, ERR_OOM, ERR_CUDA, ERR_SINGULAR, ERR_NO_CONVERGE, ERR_TIMEOUT, ERR_MESH
 K_NAMES = ["fill_far", "fill_near", "gather", "lu_panel", "lu_gemm", "trsm", "solve_gemm", "trace"]
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_MIXED_LA = 2
 
 ERR_NAMES = {ERR_ARG: "BEMGPU_ERR_ARG", ERR_OOM: "BEMGPU_ERR_OOM", ERR_CUDA: "BEMGPU_ERR_CUDA",
              ERR_SINGULAR: "BEMGPU_ERR_SINGULAR", ERR_NO_CONVERGE: "BEMGPU_ERR_NO_CONVERGE",

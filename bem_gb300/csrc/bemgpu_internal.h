@@ -143,8 +143,9 @@ struct HalfPairBlock {
 
 // Computes every triangle pair of (t, s) with one Green's function and writes
 // the per-half-pair products into H (ntr x nsr blocks, index j*ntr+i).
+// precision BEMGPU_PREC_MIXED integrates pairs farther apart than 3 edge lengths in FP32.
 int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s,
-                   const bemgpu_green_t *g, const bemgpu_options_t *opt, HalfPairBlock *H,
+                   const bemgpu_green_t *g, const bemgpu_options_t *opt, int precision, HalfPairBlock *H,
                    cudaStream_t stream, int64_t *n_near, int64_t *n_far);
 // Z (complex128, column-major, ld) = gather of one H with g's Zeps/Zmu.
 int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, const bemgpu_green_t *g,
@@ -163,8 +164,27 @@ int bem_zgetrf(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, in
 // B (n x nrhs) <- A^{-1} B using the LU factors and pivots of bem_zgetrf.
 int bem_zgetrs(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int *d_ipiv, double *B,
                int64_t ldb, int nrhs, cudaStream_t stream);
+// complex64 versions (mixed path).
+int bem_cgetrf(bemgpu_ctx_s *ctx, float *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream);
+int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int *d_ipiv, float *B, int64_t ldb,
+               int nrhs, cudaStream_t stream);
+// complex64 GEMM: tensor cores where the shape allows (gemm_tc.cu), else FMA pipes.
+int bem_cgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const float alpha[2], const float *A,
+              int64_t lda, const float *B, int64_t ldb, const float beta[2], float *C, int64_t ldc,
+              cudaStream_t stream);
+int bem_cgemm_comp64(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
+                     int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
+                     cudaStream_t stream);
+int bem_cgemm_fma(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const float alpha[2], const float *A,
+                  int64_t lda, const float *B, int64_t ldb, const float beta[2], float *C, int64_t ldc,
+                  cudaStream_t stream);
 // C = alpha * op(A) * op(B) + beta * C for complex128 column-major matrices.
 // op: 'N' or 'C' (conjugate transpose) for A; 'N' for B.
 int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const double alpha[2], const double *A,
               int64_t lda, const double *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
               cudaStream_t stream);
+
+// ---- mixed-precision solve (mixed.cu) ----
+// W (FP64, n x n, ld n), G1 (ns2 x ns2), G2 ((n-ns2) x (n-ns2)) as filled; writes S = 1/4 Tr(B2^H B1).
+int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const double *G1, const double *G2,
+                    cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info);

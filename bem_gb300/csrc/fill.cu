@@ -202,9 +202,130 @@ __device__ __noinline__ void far_pair(const TriRec &T, const TriRec &S, const Gr
   }
 }
 
-__global__ void __launch_bounds__(128) far_pairs_fp64_kernel(const TriRec *__restrict__ Tr, int ntT,
-                                                             const TriRec *__restrict__ Sr, int ntS, GreenDev g,
-                                                             FarOpts o, HalfPairBlock *__restrict__ H, int ntr) {
+// ---------------- far pairs in FP32 (mixed precision) ----------------
+//
+// Same closed form as far_pair(), evaluated in FP32 with a pair-centred
+// distance: r_t - r_s = D0 + u, D0 = P_t - P_s (FP64 once per pair), u = rho - l
+// (small, FP32).  R = R0 + dR with R0 = |D0| in FP64 and
+// dR = (2 D0.u + u.u) / (R0 + R) in FP32, so the phase k R is k R0 reduced
+// modulo 2 pi in FP64 once per pair plus k dR in FP32; the relative error of
+// every node's e^{ikR}/R stays near FP32 rounding at any distance.
+struct f3 {
+  float x, y, z;
+};
+struct c1 {
+  float r, i;
+};
+struct c3 {
+  c1 x, y, z;
+};
+__device__ __forceinline__ f3 f3of(d3 a) { return {(float)a.x, (float)a.y, (float)a.z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(float c, f3 a) { return {c * a.x, c * a.y, c * a.z}; }
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 fcross(f3 a, f3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ c1 cmulf(c1 a, c1 b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+__device__ __forceinline__ c1 csubf(c1 a, c1 b) { return {a.r - b.r, a.i - b.i}; }
+__device__ __forceinline__ c1 cscalef(float c, c1 a) { return {c * a.r, c * a.i}; }
+__device__ __forceinline__ void caccf(c1 &a, c1 b) { a.r += b.r; a.i += b.i; }
+__device__ __forceinline__ c3 c3zerof() { return {{0, 0}, {0, 0}, {0, 0}}; }
+__device__ __forceinline__ c3 cs_vf(c1 c, f3 v) { return {{c.r * v.x, c.i * v.x}, {c.r * v.y, c.i * v.y}, {c.r * v.z, c.i * v.z}}; }
+__device__ __forceinline__ void c3accf(c3 &a, c3 b) {
+  caccf(a.x, b.x); caccf(a.y, b.y); caccf(a.z, b.z);
+}
+__device__ __forceinline__ c3 c3scalef(float c, c3 a) { return {cscalef(c, a.x), cscalef(c, a.y), cscalef(c, a.z)}; }
+__device__ __forceinline__ c3 c3subf(c3 a, c3 b) { return {csubf(a.x, b.x), csubf(a.y, b.y), csubf(a.z, b.z)}; }
+__device__ __forceinline__ c1 rdotf(f3 a, c3 b) {
+  return {a.x * b.x.r + a.y * b.y.r + a.z * b.z.r, a.x * b.x.i + a.y * b.y.i + a.z * b.z.i};
+}
+__device__ __forceinline__ c3 zcrossf(c3 a, f3 b) {
+  return {{a.y.r * b.z - a.z.r * b.y, a.y.i * b.z - a.z.i * b.y},
+          {a.z.r * b.x - a.x.r * b.z, a.z.i * b.x - a.x.i * b.z},
+          {a.x.r * b.y - a.y.r * b.x, a.x.i * b.y - a.y.i * b.x}};
+}
+__device__ __forceinline__ c3 rcrossf(f3 a, c3 b) {
+  return {{a.y * b.z.r - a.z * b.y.r, a.y * b.z.i - a.z * b.y.i},
+          {a.z * b.x.r - a.x * b.z.r, a.z * b.x.i - a.x * b.z.i},
+          {a.x * b.y.r - a.y * b.x.r, a.x * b.y.i - a.y * b.x.i}};
+}
+
+__device__ __noinline__ void far_pair_fp32(const TriRec &T, const TriRec &S, const GreenDev &g,
+                                           const double (*rule)[3], int nr, HalfPairBlock *H, int ntr) {
+  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+  const d3 D0d = Pt - Ps;
+  const double R0d = sqrt(dot(D0d, D0d));
+  // per-pair FP64: magnitude and phase of e^{ik R0}
+  const double ph0d = g.iki * R0d;
+  const double ph0r = ph0d - 6.283185307179586476925286766559 * rint(ph0d * 0.15915494309189533576888376337251);
+  const float ph0 = (float)ph0r;
+  const float m0 = (float)exp(g.ikr * R0d);
+  const float R0 = (float)R0d, R0sq = (float)(R0d * R0d);
+  const f3 D0 = f3of(D0d);
+  const float ikr = (float)g.ikr, iki = (float)g.iki;
+  const f3 v01t = f3of(ld3(T.v01)), v02t = f3of(ld3(T.v02)), v01s = f3of(ld3(S.v01)), v02s = f3of(ld3(S.v02));
+  c1 U0 = {0, 0}, U1 = {0, 0}, V0 = {0, 0};
+  c3 U2 = c3zerof(), U3 = c3zerof(), V1 = c3zerof(), V2 = c3zerof(), V3 = c3zerof();
+  for (int q = 0; q < nr; q++) {
+    const float a = (float)rule[q][0], b = (float)rule[q][1], w = (float)rule[q][2];
+    const f3 rho = a * v01t + b * v02t;
+    c1 I0 = {0, 0}, Q0 = {0, 0};
+    c3 A = c3zerof(), Q1 = c3zerof();
+    for (int uix = 0; uix < nr; uix++) {
+      const float as = (float)rule[uix][0], bs = (float)rule[uix][1], ws = (float)rule[uix][2];
+      const f3 l = as * v01s + bs * v02s;
+      const f3 u = rho - l;
+      const float sdel = 2.0f * fdot(D0, u) + fdot(u, u);
+      const float Rf = sqrtf(R0sq + sdel);
+      const float dR = sdel / (R0 + Rf);
+      const float R = R0 + dR;
+      float sn, cs;
+      sincosf(ph0 + iki * dR, &sn, &cs);
+      const float mag = m0 * expf(ikr * dR);
+      const float Ri = 1.0f / R;
+      const c1 gs = {mag * cs * Ri, mag * sn * Ri};
+      const c1 one_m_ikR = {1.0f - ikr * R, -iki * R};
+      const c1 qq = cscalef(Ri * Ri, cmulf(gs, one_m_ikR));
+      const c1 gw = cscalef(ws, gs), qw = cscalef(ws, qq);
+      caccf(I0, gw);
+      c3accf(A, cs_vf(gw, l));
+      caccf(Q0, qw);
+      c3accf(Q1, cs_vf(qw, l));
+    }
+    caccf(U0, cscalef(w, I0));
+    caccf(U1, cscalef(w, rdotf(rho, A)));
+    c3accf(U2, cs_vf(cscalef(w, I0), rho));
+    c3accf(U3, c3scalef(w, A));
+    caccf(V0, cscalef(w, Q0));
+    c3accf(V1, c3scalef(w, zcrossf(Q1, rho)));
+    c3accf(V2, c3scalef(w, Q1));
+    c3accf(V3, cs_vf(cscalef(w, Q0), rho));
+  }
+  const c1 ksq = {(float)g.ksqr, (float)g.ksqi};
+  for (int i = 0; i < T.nh; i++) {
+    const f3 ei = f3of(ld3(T.hp0[i]) - Pt);
+    for (int j = 0; j < S.nh; j++) {
+      const f3 dj = f3of(ld3(S.hp0[j]) - Ps);
+      const f3 D = (D0 + ei) - dj;
+      c1 bracket = csubf(csubf(U1, rdotf(dj, U2)), rdotf(ei, U3));
+      caccf(bracket, cscalef(fdot(ei, dj), U0));
+      const c1 L = csubf(cscalef(0.25f, cmulf(ksq, bracket)), U0);
+      c3 X = c3subf(c3subf(V1, zcrossf(V2, ei)), rcrossf(dj, V3));
+      c3accf(X, cs_vf(V0, fcross(dj, ei)));
+      const c1 K = cscalef(-0.25f, rdotf(D, X));
+      const double c = scatter_coef(T, i, S, j);
+      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], z1{c * L.r, c * L.i}, z1{c * K.r, c * K.i});
+    }
+  }
+}
+
+// mixed != 0: pairs whose centroid distance exceeds 3 edge lengths (the longer
+// of the two triangles' longest edges) are integrated in FP32.
+__global__ void __launch_bounds__(128) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
+                                                        const TriRec *__restrict__ Sr, int ntS, GreenDev g,
+                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mixed) {
   const int sb = blockIdx.x * blockDim.x + threadIdx.x;
   const int ta = blockIdx.y * blockDim.y + threadIdx.y;
   if (sb >= ntS || ta >= ntT) return;
@@ -215,6 +336,16 @@ __global__ void __launch_bounds__(128) far_pairs_fp64_kernel(const TriRec *__res
   const double d = dist2_rn(T.c, S.c);
   const double e = fmax(T.emax, S.emax);
   const double emax2 = __dmul_rn(e, e);
+  if (mixed && d > 9.0 * emax2) {
+    // beyond 3 edge lengths every default threshold selects the 6-point rule;
+    // the cascade is kept for non-default Options
+    if (__dmul_rn(d, o.th6) > emax2) far_pair_fp32(T, S, g, c_rule6, 6, H, ntr);
+    else if (__dmul_rn(d, o.th10) > emax2) far_pair_fp32(T, S, g, c_rule10, 10, H, ntr);
+    else if (__dmul_rn(d, o.th15) > emax2) far_pair_fp32(T, S, g, c_rule15, 15, H, ntr);
+    else if (__dmul_rn(d, o.th21) > emax2) far_pair_fp32(T, S, g, c_rule21, 21, H, ntr);
+    else far_pair_fp32(T, S, g, c_rule36, 36, H, ntr);
+    return;
+  }
   if (__dmul_rn(d, o.th6) > emax2) far_pair(T, S, g, c_rule6, 6, H, ntr);
   else if (__dmul_rn(d, o.th10) > emax2) far_pair(T, S, g, c_rule10, 10, H, ntr);
   else if (__dmul_rn(d, o.th15) > emax2) far_pair(T, S, g, c_rule15, 15, H, ntr);
@@ -583,8 +714,8 @@ int load_tables(bemgpu_ctx_s *ctx) {
 }  // namespace
 
 int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s, const bemgpu_green_t *g,
-                   const bemgpu_options_t *opt, HalfPairBlock *H, cudaStream_t stream, int64_t *n_near,
-                   int64_t *n_far) {
+                   const bemgpu_options_t *opt, int precision, HalfPairBlock *H, cudaStream_t stream,
+                   int64_t *n_near, int64_t *n_far) {
   int rc = load_tables(ctx);
   if (rc) return rc;
   const NearList *nl = bem_near_list(ctx, t, s);
@@ -606,7 +737,8 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
   }
   {
     ProfScope ps(ctx, BEMGPU_K_FILL_FAR, stream, far_flops, far_bytes);
-    far_pairs_fp64_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg);
+    far_pairs_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg,
+                                              precision == BEMGPU_PREC_MIXED ? 1 : 0);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -654,7 +786,8 @@ extern "C" int bemgpu_zts(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, co
   if (!ctx || !t || !s || !g || !dZ) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: null argument");
   if (t->geom != s->geom) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: t and s must share one geometry");
   if (ldz < 2 * (int64_t)t->nrwg) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: ldz < 2*size(t)");
-  if (precision != BEMGPU_PREC_FP64) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: precision %d not available", precision);
+  if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: unknown precision %d", precision);
   bemgpu_options_t o;
   if (opt) o = *opt; else bemgpu_options_default(&o);
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -662,7 +795,7 @@ extern "C" int bemgpu_zts(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, co
   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
   HalfPairBlock *H = (HalfPairBlock *)bem_workspace(ctx, "H0", sizeof(HalfPairBlock) * (size_t)t->nrwg * s->nrwg);
   if (!H) return bem_fail(ctx, BEMGPU_ERR_OOM, "zts: workspace allocation failed");
-  int rc = bem_fill_pairs(ctx, t, s, g, &o, H, st, nullptr, nullptr);
+  int rc = bem_fill_pairs(ctx, t, s, g, &o, precision, H, st, nullptr, nullptr);
   if (rc) return rc;
   return bem_gather_z(ctx, H, t->nrwg, s->nrwg, g, (double *)dZ, ldz, st);
 }

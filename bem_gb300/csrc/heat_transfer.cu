@@ -99,8 +99,9 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: trees must share one geometry");
   if (top->nrwg != s->nrwg + t->nrwg)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: size(top) != size(s) + size(t)");
-  if (precision != BEMGPU_PREC_FP64)
-    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: precision %d not available", precision);
+  if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED && precision != BEMGPU_PREC_MIXED_LA)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: unknown precision %d", precision);
+  const int fill_prec = precision == BEMGPU_PREC_MIXED ? BEMGPU_PREC_MIXED : BEMGPU_PREC_FP64;
   bemgpu_options_t o;
   if (opt) o = *opt; else bemgpu_options_default(&o);
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -122,6 +123,35 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   double *W = (double *)bem_workspace(ctx, "W", sizeof(double) * 2 * (size_t)n * n);
   double *G1 = (double *)bem_workspace(ctx, "G1", sizeof(double) * 2 * (size_t)ns2 * ns2);
   double *G2 = (double *)bem_workspace(ctx, "G2", sizeof(double) * 2 * (size_t)nt2 * nt2);
+  if (!He || !H1 || !H2 || !W || !G1 || !G2)
+    return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
+
+  cudaEvent_t *ev = ctx->ev;
+  cudaEventRecord(ev[0], st);
+  int64_t near1 = 0, far1 = 0, near2 = 0, far2 = 0, near3 = 0, far3 = 0;
+  int rc = bem_fill_pairs(ctx, top, top, &gext, &o, fill_prec, He, st, &near1, &far1);
+  if (!rc) rc = bem_fill_pairs(ctx, s, s, &g1, &o, fill_prec, H1, st, &near2, &far2);
+  if (!rc) rc = bem_fill_pairs(ctx, t, t, &g2, &o, fill_prec, H2, st, &near3, &far3);
+  if (!rc) rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st);
+  if (rc) return rc;
+  cudaEventRecord(ev[7], st);
+  if (precision != BEMGPU_PREC_FP64) {
+    bemgpu_solve_info_t mi;
+    memset(&mi, 0, sizeof mi);
+    double S[2] = {0, 0};
+    rc = bem_mixed_solve(ctx, W, n, ns2, G1, G2, st, S, &mi);
+    if (rc && rc != BEMGPU_ERR_NO_CONVERGE) return rc;
+    *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
+    if (info) {
+      *info = mi;
+      info->ms_fill = elapsed(ev[0], ev[7]);
+      info->S_re = S[0];
+      info->S_im = S[1];
+      info->pairs_near = near1 + near2 + near3;
+      info->pairs_far_fp64 = far1 + far2 + far3;
+    }
+    return rc;
+  }
   double *Y = (double *)bem_workspace(ctx, "Y", sizeof(double) * 2 * (size_t)n * nt2);
   double *B1 = (double *)bem_workspace(ctx, "B1", sizeof(double) * 2 * (size_t)ns2 * nt2);
   double *B2 = (double *)bem_workspace(ctx, "B2", sizeof(double) * 2 * (size_t)ns2 * nt2);
@@ -129,18 +159,9 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   int *dinfo = (int *)bem_workspace(ctx, "info", sizeof(int));
   const int TRB = 1024;
   double *partial = (double *)bem_workspace(ctx, "trace_partial", sizeof(double) * 2 * TRB + 16);
-  if (!He || !H1 || !H2 || !W || !G1 || !G2 || !Y || !B1 || !B2 || !ipiv || !dinfo || !partial)
+  if (!Y || !B1 || !B2 || !ipiv || !dinfo || !partial)
     return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
   double *dS = partial + 2 * TRB;
-
-  cudaEvent_t *ev = ctx->ev;
-  cudaEventRecord(ev[0], st);
-  int64_t near1 = 0, far1 = 0, near2 = 0, far2 = 0, near3 = 0, far3 = 0;
-  int rc = bem_fill_pairs(ctx, top, top, &gext, &o, He, st, &near1, &far1);
-  if (!rc) rc = bem_fill_pairs(ctx, s, s, &g1, &o, H1, st, &near2, &far2);
-  if (!rc) rc = bem_fill_pairs(ctx, t, t, &g2, &o, H2, st, &near3, &far3);
-  if (!rc) rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st);
-  if (rc) return rc;
   cudaEventRecord(ev[1], st);
   rc = bem_zgetrf(ctx, W, n, n, ipiv, dinfo, st);
   if (rc) return rc;
@@ -182,7 +203,7 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
   if (info) {
     memset(info, 0, sizeof *info);
-    info->ms_fill = elapsed(ev[0], ev[1]);
+    info->ms_fill = elapsed(ev[0], ev[7]);
     info->ms_lu = elapsed(ev[1], ev[2]);
     info->ms_solve = elapsed(ev[2], ev[3]);
     info->ms_trace = elapsed(ev[3], ev[4]);
