@@ -112,6 +112,8 @@ struct ProfScope {
 int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...);
 // Returns a device buffer of at least `bytes` for `name` (grown on demand).
 void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes);
+// Near pairs of (t, s) built on the host (no device memory touched).
+void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::vector<NearPair> &pairs);
 // Near-pair list of (t, s), built on the host once and cached on the device.
 const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s);
 // Far-pair counts per rule (6, 10, 15, 21, 36 points) of (t, s), classified on

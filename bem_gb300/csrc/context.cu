@@ -67,14 +67,11 @@ void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes) {
   return p;
 }
 
-const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
-  auto key = std::make_pair(t, s);
-  auto it = ctx->near_cache.find(key);
-  if (it != ctx->near_cache.end()) return &it->second;
+void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::vector<NearPair> &pairs) {
+  pairs.clear();
   const bemgpu_geom_s *g = t->geom;
   std::unordered_map<int, int> s_local;
   for (int i = 0; i < s->ntri; i++) s_local[s->tri_gid[i]] = i;
-  std::vector<NearPair> pairs;
   std::vector<int> seen;
   for (int a = 0; a < t->ntri; a++) {
     int gt = t->tri_gid[a];
@@ -91,6 +88,14 @@ const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const b
     std::sort(seen.begin(), seen.end());
     for (int b : seen) pairs.push_back({a, b, s->tri_gid[b] == gt ? 1 : 0, 0});
   }
+}
+
+const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
+  auto key = std::make_pair(t, s);
+  auto it = ctx->near_cache.find(key);
+  if (it != ctx->near_cache.end()) return &it->second;
+  std::vector<NearPair> pairs;
+  bem_build_near_pairs(t, s, pairs);
   NearList nl;
   nl.n = (int64_t)pairs.size();
   if (nl.n) {

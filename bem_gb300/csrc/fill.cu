@@ -820,3 +820,4 @@ extern "C" int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t 
   BEM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return BEMGPU_OK;
 }
+
