@@ -30,6 +30,7 @@ EXPORTED = [
     "bemgpu_geom_create", "bemgpu_geom_destroy", "bemgpu_tree_create", "bemgpu_tree_destroy",
     "bemgpu_tree_size", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
+    "bemgpu_zts_noalloc",
 ]
 
 
@@ -90,6 +91,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_dimensionless_omega": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
         "bemgpu_zts": (i32, [vp, vp, vp, P(Green), P(Options), i32, vp, i64, vp]),
         "bemgpu_zts_host": (i32, [vp, vp, vp, P(Green), P(Options), i32, dp, i64]),
+        "bemgpu_zts_noalloc": (i32, [vp, vp, vp, P(Green), P(Options), vp, i64, vp]),
         "bemgpu_heat_transfer": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(ctypes.c_double), P(SolveInfo)]),
     }
     for name, (res, args) in sig.items():

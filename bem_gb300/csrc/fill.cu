@@ -821,3 +821,88 @@ extern "C" int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t 
   return BEMGPU_OK;
 }
 
+// ---------------- Zts without device allocation ----------------
+//
+// For callers that cannot allocate device memory while they run: code inside
+// a CUDA graph capture or a callback, a real-time loop that must not block on
+// the allocator, or an embedding host whose memory pool owns the device.
+// bemgpu_zts_noalloc does the same fill as bemgpu_zts into the caller's
+// buffer, but keeps its scratch (the half-pair blocks and the near-pair list)
+// in one file-scope device array of fixed size, allocated when the library
+// is loaded on a GPU and held until the process exits.
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 32u << 20;   // 32 MiB
+constexpr size_t NOALLOC_NEAR_BYTES = 2u << 20;       // first 2 MiB: the near-pair list
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[64] = {nullptr};
+
+}  // namespace
+
+extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
+                                  const bemgpu_options_t *opt, void *dZ, int64_t ldz, void *stream) {
+  if (!ctx || !t || !s || !g || !dZ) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: null argument");
+  if (t->geom != s->geom) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: t and s must share one geometry");
+  if (ldz < 2 * (int64_t)t->nrwg) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: ldz < 2*size(t)");
+  const size_t hbytes = sizeof(HalfPairBlock) * (size_t)t->nrwg * (size_t)s->nrwg;
+  if (hbytes > NOALLOC_SCRATCH_BYTES - NOALLOC_NEAR_BYTES)
+    return bem_fail(ctx, BEMGPU_ERR_ARG,
+                    "zts_noalloc: %d x %d RWGs need %zu bytes of scratch, the fixed scratch holds %zu "
+                    "(at most size(t) * size(s) = %zu)",
+                    t->nrwg, s->nrwg, hbytes, NOALLOC_SCRATCH_BYTES - NOALLOC_NEAR_BYTES,
+                    (NOALLOC_SCRATCH_BYTES - NOALLOC_NEAR_BYTES) / sizeof(HalfPairBlock));
+  std::vector<NearPair> pairs;
+  bem_build_near_pairs(t, s, pairs);
+  if (pairs.size() * sizeof(NearPair) > NOALLOC_NEAR_BYTES)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: %zu near pairs exceed the fixed scratch (%zu)", pairs.size(),
+                    NOALLOC_NEAR_BYTES / sizeof(NearPair));
+  bemgpu_options_t o;
+  if (opt) o = *opt; else bemgpu_options_default(&o);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  // Set-up, once per device with that device current: the host-side name of
+  // the array is not a device address; ask the runtime for the address.
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk2(g_noalloc_mu);
+    if (!g_noalloc_addr[ctx->device]) {
+      void *p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p)
+        return bem_fail(ctx, BEMGPU_ERR_CUDA, "zts_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      g_noalloc_addr[ctx->device] = p;
+    }
+    base = (unsigned char *)g_noalloc_addr[ctx->device];
+  }
+  int rc = load_tables(ctx);
+  if (rc) return rc;
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+  NearPair *dnear = reinterpret_cast<NearPair *>(base);
+  HalfPairBlock *H = reinterpret_cast<HalfPairBlock *>(base + NOALLOC_NEAR_BYTES);
+  if (!pairs.empty())
+    BEM_CUDA_TRY(ctx, cudaMemcpyAsync(dnear, pairs.data(), pairs.size() * sizeof(NearPair), cudaMemcpyHostToDevice, st));
+  // Every half-pair slot of H has exactly one writer (the pair kernels below),
+  // so nothing left by an earlier call needs clearing.
+  const GreenDev gd = to_dev(g);
+  const FarOpts fo = {o.farThresh6, o.farThresh10, o.farThresh15, o.farThresh21};
+  dim3 blk(32, 4);
+  dim3 grd((s->ntri + 31) / 32, (t->ntri + 3) / 4);
+  far_pairs_kernel<<<grd, blk, 0, st>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, 0);
+  ctx->launches++;
+  if (!pairs.empty()) {
+    const int64_t np = (int64_t)pairs.size();
+    const int nb = (int)std::min<int64_t>((np + NEAR_WARPS - 1) / NEAR_WARPS, (int64_t)ctx->num_sms * 16);
+    near_pairs_fp64_kernel<<<nb, 32 * NEAR_WARPS, 0, st>>>(t->d_rec, s->d_rec, dnear, np, gd, H, t->nrwg);
+    ctx->launches++;
+  }
+  dim3 gblk(128);
+  dim3 ggrd((t->nrwg + 127) / 128, s->nrwg);
+  gather_z_kernel<<<ggrd, gblk, 0, st>>>(H, t->nrwg, s->nrwg, to_zdev(g), (double *)dZ, ldz);
+  ctx->launches++;
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  // The near-pair list was copied from host memory owned by this call.
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  return BEMGPU_OK;
+}
