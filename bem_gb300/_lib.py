@@ -14,7 +14,8 @@ LIB_PATH = os.path.join(HERE, "libbemgpu.so")
 
 OK = 0
 ERR_ARG, ERR_OOM, ERR_CUDA, ERR_SINGULAR, ERR_NO_CONVERGE, ERR_TIMEOUT, ERR_MESH = -1, -2, -3, -4, -5, -6, -7
-K_NAMES = ["fill_far", "fill_near", "gather", "lu_panel", "lu_gemm", "trsm", "solve_gemm", "trace"]
+K_NAMES = ["fill_far", "fill_near", "gather", "lu_panel", "lu_gemm", "trsm", "solve_gemm", "trace", "refine_gemm",
+           "near_spmm", "slice"]
 PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_LA = 2
@@ -26,11 +27,11 @@ ERR_NAMES = {ERR_ARG: "BEMGPU_ERR_ARG", ERR_OOM: "BEMGPU_ERR_OOM", ERR_CUDA: "BE
 # Every symbol include/bemgpu.h declares.
 EXPORTED = [
     "bemgpu_ctx_create", "bemgpu_ctx_destroy", "bemgpu_ctx_last_error", "bemgpu_version",
-    "bemgpu_ctx_stream", "bemgpu_ctx_launches", "bemgpu_prof_enable", "bemgpu_prof_query",
+    "bemgpu_ctx_stream", "bemgpu_ctx_launches", "bemgpu_ctx_set_engines", "bemgpu_prof_enable", "bemgpu_prof_query",
     "bemgpu_geom_create", "bemgpu_geom_destroy", "bemgpu_tree_create", "bemgpu_tree_destroy",
     "bemgpu_tree_size", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
-    "bemgpu_zts_noalloc",
+    "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64",
 ]
 
 
@@ -78,6 +79,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_version": (ctypes.c_char_p, []),
         "bemgpu_ctx_stream": (i32, [vp, P(vp)]),
         "bemgpu_ctx_launches": (i64, [vp]),
+        "bemgpu_ctx_set_engines": (i32, [vp, i32, i32]),
         "bemgpu_prof_enable": (i32, [vp, i32]),
         "bemgpu_prof_query": (i32, [vp, i32, P(i64), P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
         "bemgpu_geom_create": (i32, [vp, dp, i32, dp, i32, P(vp)]),
@@ -92,6 +94,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_zts": (i32, [vp, vp, vp, P(Green), P(Options), i32, vp, i64, vp]),
         "bemgpu_zts_host": (i32, [vp, vp, vp, P(Green), P(Options), i32, dp, i64]),
         "bemgpu_zts_noalloc": (i32, [vp, vp, vp, P(Green), P(Options), vp, i64, vp]),
+        "bemgpu_cgemm": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
+        "bemgpu_cgemm_acc64": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_heat_transfer": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(ctypes.c_double), P(SolveInfo)]),
     }
     for name, (res, args) in sig.items():

@@ -85,6 +85,9 @@ struct bemgpu_ctx_s {
   std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, std::vector<int64_t>> far_rule_cache;
   cudaEvent_t ev[8];
   int64_t launches = 0;  // kernels launched by this context
+  bool tc_ready = false;  // tensor-core GEMM: smem attribute set, error flag zeroed
+  int gemm_engine = 0;   // complex64 LU/solve GEMMs: 0 tensor cores where possible, 2 FMA pipes only
+  int acc_engine = 0;    // residual/trace GEMMs with FP64 output: same choices
   // live kernel statistics
   bool prof = false;
   struct ProfRec {
@@ -174,6 +177,19 @@ int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int 
 int bem_cgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const float alpha[2], const float *A,
               int64_t lda, const float *B, int64_t ldb, const float beta[2], float *C, int64_t ldc,
               cudaStream_t stream);
+// Tensor-core complex64 GEMM: C (+)= sign * A B (A m x k, B k x n, column-major).
+enum { TC_OUT_F32 = 0, TC_OUT_F64 = 1, TC_OUT_F64_COMP = 2 };
+int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, const float *A, int64_t lda,
+                 const float *B, int64_t ldb, void *C, int64_t ldc, int out, int accumulate, cudaStream_t st);
+// The same product on the FP32 FMA pipes (any alpha, beta).
+int bem_cgemm_comp64_fma(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
+                         int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
+                         cudaStream_t stream);
+// Non-zero when a tensor-core pipeline wait ran out since the last reset (synchronizes).
+int bem_tc_error(bemgpu_ctx_s *ctx, bool reset);
+// C (complex128) = alpha A B + beta C, complex64 A and B, products summed
+// in short FP32 runs and across runs as two-float sums (tensor cores where
+// alpha = +-1 and beta = 0 or 1, else FMA pipes).
 int bem_cgemm_comp64(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
                      int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
                      cudaStream_t stream);

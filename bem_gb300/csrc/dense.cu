@@ -433,9 +433,9 @@ int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const 
 // C (complex128) = alpha A B + beta C with complex64 A, B: FP32 products,
 // compensated accumulation (per 8-deep K tile in FP32, across tiles as a
 // two-float sum), FP64 output.
-int bem_cgemm_comp64(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
-                     int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
-                     cudaStream_t stream) {
+int bem_cgemm_comp64_fma(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
+                         int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
+                         cudaStream_t stream) {
   if (m <= 0 || n <= 0) return BEMGPU_OK;
   dim3 grd((m + 63) / 64, (n + 63) / 64);
   cx<float> al = {alpha[0], alpha[1]};

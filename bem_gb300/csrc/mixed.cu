@@ -295,7 +295,7 @@ int spectral_trace(bemgpu_ctx_s *ctx, const MixedBufs &b, int n, int ns2, int nt
   const double one64[2] = {1.0, 0.0};
   const double *X = b.Y;  // rows [0, ns2) of Y, leading dimension n
   {
-    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 8.0 * ns2 * (double)nt2 * NEAR_CAP, 48.0 * ns2 * (double)nt2);
+    ProfScope ps(ctx, BEMGPU_K_NEAR_SPMM, st, 8.0 * ns2 * (double)nt2 * NEAR_CAP, 48.0 * ns2 * (double)nt2);
     zero64_kernel<<<1024, 256, 0, st>>>(b.B1, 2 * (int64_t)ns2 * nt2);
     ctx->launches++;
     ell_left_kernel<<<dim3((ns2 + 255) / 256, nt2), 256, 0, st>>>(b.eH1.col, b.eH1.val, b.eH1.cnt, ns2, X, n, b.B1,
@@ -305,7 +305,7 @@ int spectral_trace(bemgpu_ctx_s *ctx, const MixedBufs &b, int n, int ns2, int nt
   int rc = bem_cgemm_comp64(ctx, BEMGPU_K_TRACE, ns2, nt2, ns2, one, b.H1f, ns2, b.Y32, n, one64, b.B1, ns2, st);
   if (rc) return rc;
   {
-    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 8.0 * ns2 * (double)nt2 * NEAR_CAP, 64.0 * ns2 * (double)nt2);
+    ProfScope ps(ctx, BEMGPU_K_NEAR_SPMM, st, 8.0 * ns2 * (double)nt2 * NEAR_CAP, 64.0 * ns2 * (double)nt2);
     conj_transpose_kernel<<<dim3((ns2 + 31) / 32, (nt2 + 31) / 32), dim3(32, 8), 0, st>>>(X, n, ns2, nt2, b.XH,
                                                                                            b.XH32);
     ctx->launches++;
@@ -399,10 +399,10 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   const int max_iters = 4;
   while (iters < max_iters) {
     // R = E_t - W_far Y - W_near Y
-    rc = bem_cgemm_comp64(ctx, BEMGPU_K_SOLVE_GEMM, n, nt2, n, mone, b.Wf, n, b.Y32, n, zero64, b.R64, n, st);
+    rc = bem_cgemm_comp64(ctx, BEMGPU_K_REFINE_GEMM, n, nt2, n, mone, b.Wf, n, b.Y32, n, zero64, b.R64, n, st);
     if (rc) return rc;
     {
-      ProfScope ps(ctx, BEMGPU_K_SOLVE_GEMM, st, 8.0 * n * (double)nt2 * 300, 40.0 * n * (double)nt2);
+      ProfScope ps(ctx, BEMGPU_K_NEAR_SPMM, st, 8.0 * n * (double)nt2 * 300, 40.0 * n * (double)nt2);
       ell_left_kernel<<<gm, 256, 0, st>>>(b.eW.col, b.eW.val, b.eW.cnt, n, b.Y, n, b.R64, n, -1.0, ns2, b.R32, n);
       ctx->launches++;
     }

@@ -88,6 +88,11 @@ const char *bemgpu_version(void);
 int bemgpu_ctx_stream(bemgpu_ctx_t ctx, void **stream);
 /* Number of kernels the context launched since it was created. */
 int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx);
+/* Engines of the complex64 products: gemm = LU and correction solves,
+ * acc64 = refinement residual and trace (FP64 output); 0 = the library's
+ * choice (tensor cores where the shape allows), 1 = tensor cores where the
+ * shape allows, 2 = FMA pipes only.  No reference counterpart (tuning). */
+int bemgpu_ctx_set_engines(bemgpu_ctx_t ctx, int gemm, int acc64);
 
 /* ---- live kernel statistics (measurement hooks; no counterpart in the reference) ---- */
 /* Kernel classes timed with CUDA events on the context stream while enabled. */
@@ -99,7 +104,10 @@ int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx);
 #define BEMGPU_K_TRSM 5         /* triangular blocks (LU and solve) */
 #define BEMGPU_K_SOLVE_GEMM 6   /* off-diagonal updates of the triangular solves */
 #define BEMGPU_K_TRACE 7        /* sym, the two trace products, the trace reduction */
-#define BEMGPU_K_COUNT 8
+#define BEMGPU_K_REFINE_GEMM 8  /* refinement residual: far-part product */
+#define BEMGPU_K_NEAR_SPMM 9    /* FP64 near-part products (residual and trace) */
+#define BEMGPU_K_SLICE 10       /* tensor-core operand slicing */
+#define BEMGPU_K_COUNT 11
 /* Enables (1) or disables (0) event timing of every launch; resets the totals. */
 int bemgpu_prof_enable(bemgpu_ctx_t ctx, int enable);
 /* Totals of one kernel class since the last enable: launches, device ms,
@@ -155,6 +163,20 @@ int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const be
  * for the previous call).  Synchronous: returns once dZ is written. */
 int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
                        const bemgpu_options_t *opt, void *dZ, int64_t ldz, void *stream);
+
+/* ---- dense complex algebra ---- */
+/* C (m x n) = A (m x k) B (k x n) [+ C when accumulate], complex64 device
+ * matrices, column-major with interleaved (re, im).  The product of the
+ * mixed-precision LU and trace (addproduct -> zgemm, src/util/MatrixOperations.cpp:70-74):
+ * engine 1 = tensor cores (bf16x3 split, six products, FP32 accumulate),
+ * 2 = FP32 FMA pipes, 0 = the library's choice.  Synchronous. */
+int bemgpu_cgemm(bemgpu_ctx_t ctx, int m, int n, int k, const float *dA, int64_t lda, const float *dB, int64_t ldb,
+                 float *dC, int64_t ldc, int accumulate, int engine);
+/* The refinement residual's product: C (complex128) = A B [+ C] with
+ * complex64 A and B; products summed in short FP32 runs, the runs in
+ * two-float sums.  engine 1 = tensor cores, 2 = FMA pipes, 0 = choice. */
+int bemgpu_cgemm_acc64(bemgpu_ctx_t ctx, int m, int n, int k, const float *dA, int64_t lda, const float *dB,
+                       int64_t ldb, double *dC, int64_t ldc, int accumulate, int engine);
 
 /* ---- per-frequency solve ---- */
 /* CalcHeatTransfer: top is the two-body tree (s's RWGs first, then t's),

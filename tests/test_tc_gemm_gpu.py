@@ -1,0 +1,146 @@
+"""bemgpu_cgemm: the complex64 product of the mixed-precision LU, solve and
+trace (the reference's addproduct -> zgemm, src/util/MatrixOperations.cpp:70-74).
+
+The tensor-core engine (tcgen05, bf16x3 slices, six products, FP32
+accumulation) and the FP32 FMA engine are both held to the complex128 product
+of the same complex64 inputs: every entry within 2e-6 of sum_k |a_ik| |b_kj|
+(FP32 class; the FP32 FMA reference itself sits near 1e-7)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from bem_gb300 import _lib, api
+
+pytestmark = pytest.mark.gpu
+TOL = 2e-6
+
+
+def _rand(rng, shape, scale=1.0):
+    return (scale * (rng.standard_normal(shape) + 1j * rng.standard_normal(shape))).astype(np.complex64)
+
+
+def _gemm(A, B, C0, accumulate, engine, lda_pad=0, ldb_pad=0, ldc_pad=0):
+    import torch
+    ctx = api.default_context()
+    A, B, C0 = (np.asarray(x, dtype=np.complex64) for x in (A, B, C0))
+    m, k = A.shape
+    n = B.shape[1]
+    assert B.shape[0] == k and C0.shape == (m, n)
+    lda, ldb, ldc = m + lda_pad, k + ldb_pad, m + ldc_pad
+    dA = torch.zeros((k, lda), dtype=torch.complex64, device="cuda")
+    dB = torch.zeros((n, ldb), dtype=torch.complex64, device="cuda")
+    dC = torch.zeros((n, ldc), dtype=torch.complex64, device="cuda")
+    dA[:, :m] = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    dB[:, :k] = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dC[:, :m] = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda()
+    torch.cuda.synchronize()
+    rc = _lib.load().bemgpu_cgemm(ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), lda,
+                                  ctypes.c_void_p(dB.data_ptr()), ldb, ctypes.c_void_p(dC.data_ptr()), ldc,
+                                  int(accumulate), engine)
+    assert rc == 0, _lib.load().bemgpu_ctx_last_error(ctx.handle)
+    out = dC.cpu().numpy()
+    assert np.all(out[:, m:] == 0), "wrote outside the m rows of C"
+    return out[:, :m].T
+
+
+def _check(A, B, C0, accumulate, got):
+    ref = A.astype(np.complex128) @ B.astype(np.complex128)
+    if accumulate:
+        ref = ref + C0.astype(np.complex128)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64) + (np.abs(C0) if accumulate else 0)
+    err = np.max(np.abs(got - ref) / scale)
+    return err
+
+
+@pytest.mark.parametrize("m,n,k", [(64, 64, 16), (100, 130, 37), (257, 129, 200), (1000, 384, 320)])
+@pytest.mark.parametrize("engine", [1, 2])
+def test_cgemm_engines_match_complex128(m, n, k, engine):
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(m * 7 + n * 3 + k)
+    A, B, C0 = _rand(rng, (m, k)), _rand(rng, (k, n)), _rand(rng, (m, n))
+    for acc in (0, 1):
+        got = _gemm(A, B, C0, acc, engine)
+        err = _check(A, B, C0, acc, got)
+        assert err < TOL, (engine, acc, err)
+
+
+def test_tensor_core_gemm_leading_dimensions_and_dynamic_range():
+    """Strided operands (lda, ldb, ldc > rows) and entries spanning 1e-6..1e6,
+    the spread of an impedance block's L and K terms.  With one dominant term
+    per sum, the FP32 accumulator's per-add rounding over the 6 x 2k partial
+    products is what remains: held to 1e-5 (the sequential FP32 bound is
+    ~2k x 6 x 2^-24 = 1e-4), FMA engine alongside for comparison."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(5)
+    m, n, k = 300, 200, 150
+    A = _rand(rng, (m, k)) * (10.0 ** rng.uniform(-6, 6, (m, k))).astype(np.float32)
+    B = _rand(rng, (k, n)) * (10.0 ** rng.uniform(-3, 3, (k, n))).astype(np.float32)
+    C0 = _rand(rng, (m, n))
+    got = _gemm(A, B, C0, 1, 1, lda_pad=5, ldb_pad=3, ldc_pad=7)
+    fma = _gemm(A, B, C0, 1, 2, lda_pad=5, ldb_pad=3, ldc_pad=7)
+    assert _check(A, B, C0, 1, fma) < 1e-5
+    assert _check(A, B, C0, 1, got) < 1e-5
+
+
+def test_tensor_core_gemm_is_deterministic():
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(9)
+    A, B, C0 = _rand(rng, (512, 256)), _rand(rng, (256, 256)), _rand(rng, (512, 256))
+    a = _gemm(A, B, C0, 1, 1)
+    b = _gemm(A, B, C0, 1, 1)
+    assert np.array_equal(a, b)
+
+
+def _gemm64(A, B, C0, accumulate, engine):
+    import torch
+    ctx = api.default_context()
+    A, B = (np.asarray(x, dtype=np.complex64) for x in (A, B))
+    C0 = np.asarray(C0, dtype=np.complex128)
+    m, k = A.shape
+    n = B.shape[1]
+    assert B.shape[0] == k and C0.shape == (m, n)
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dC = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda()
+    torch.cuda.synchronize()
+    rc = _lib.load().bemgpu_cgemm_acc64(ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), m,
+                                        ctypes.c_void_p(dB.data_ptr()), k, ctypes.c_void_p(dC.data_ptr()), m,
+                                        int(accumulate), engine)
+    assert rc == 0, _lib.load().bemgpu_ctx_last_error(ctx.handle)
+    return dC.cpu().numpy().T
+
+
+@pytest.mark.parametrize("m,n,k", [(64, 64, 16), (130, 70, 33), (600, 200, 2000)])
+@pytest.mark.parametrize("engine", [1, 2])
+def test_acc64_residual_product(m, n, k, engine):
+    """The refinement residual's product: complex64 operands, complex128
+    result.  Tensor cores: operands rounded (to nearest) to 25-bit block fixed
+    point, block products summed exactly, so each product carries ~2^-24 of
+    its blocks' largest magnitudes, unbiased; FMA engine: FP32 products, short
+    FP32 runs.  Short sums sit near 2^-24 of sum |a| |b|, long ones far below
+    as the unbiased errors average out."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(m + 11 * n + k)
+    A, B = _rand(rng, (m, k)), _rand(rng, (k, n))
+    C0 = (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n)))
+    for acc in (0, 1):
+        got = _gemm64(A, B, C0, acc, engine)
+        ref = A.astype(np.complex128) @ B.astype(np.complex128) + (C0 if acc else 0)
+        scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+        err = np.max(np.abs(got - ref) / scale)
+        assert err < (3e-7 if k < 256 else 2e-8), (engine, acc, err)
+
+
+def test_acc64_beats_fp32_accumulation_on_long_sums():
+    """K = 8192: the compensated product's error stays well below the plain
+    FP32-accumulated tensor-core product's."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    m, n, k = 256, 128, 8192
+    A, B = _rand(rng, (m, k)), _rand(rng, (k, n))
+    ref = A.astype(np.complex128) @ B.astype(np.complex128)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    e64 = np.max(np.abs(_gemm64(A, B, np.zeros((m, n)), 0, 1) - ref) / scale)
+    e32 = np.max(np.abs(_gemm(A, B, np.zeros((m, n), np.complex64), 0, 1) - ref) / scale)
+    assert e64 < 2e-8 and e64 < 0.25 * e32, (e64, e32)
