@@ -31,7 +31,7 @@ EXPORTED = [
     "bemgpu_geom_create", "bemgpu_geom_destroy", "bemgpu_tree_create", "bemgpu_tree_destroy",
     "bemgpu_tree_size", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
-    "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64",
+    "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64", "bemgpu_zgemm_exact",
 ]
 
 
@@ -96,6 +96,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_zts_noalloc": (i32, [vp, vp, vp, P(Green), P(Options), vp, i64, vp]),
         "bemgpu_cgemm": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_cgemm_acc64": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
+        "bemgpu_zgemm_exact": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_heat_transfer": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(ctypes.c_double), P(SolveInfo)]),
     }
     for name, (res, args) in sig.items():

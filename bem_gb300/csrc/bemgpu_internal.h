@@ -85,7 +85,9 @@ struct bemgpu_ctx_s {
   std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, std::vector<int64_t>> far_rule_cache;
   cudaEvent_t ev[8];
   int64_t launches = 0;  // kernels launched by this context
-  bool tc_ready = false;  // tensor-core GEMM: smem attribute set, error flag zeroed
+  bool tc_ready = false;      // gemm_tc.cu kernels: shared-memory attribute set
+  bool ex_ready = false;      // gemm_exact.cu kernels: shared-memory attribute set
+  bool tc_err_ready = false;  // tensor-core pipeline error flag zeroed
   int gemm_engine = 0;   // complex64 LU/solve GEMMs: 0 tensor cores where possible, 2 FMA pipes only
   int acc_engine = 0;    // residual/trace GEMMs with FP64 output: same choices
   // live kernel statistics
@@ -185,6 +187,24 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
 int bem_cgemm_comp64_fma(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
                          int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,
                          cudaStream_t stream);
+// Operand of the exact complex128 tensor-core GEMM (gemm_exact.cu): block
+// fixed-point bf16 slices of A (m x k, role A) or of B (k x n, role B, `rows`
+// = n), kept on the device so one slicing serves several products.
+struct ExactOperand {
+  void *S = nullptr;    // slices * rows_p * kp bf16
+  int *aux = nullptr;   // [0] scaling exponent, [8..9] largest magnitude (bits)
+  int rows = 0, k = 0, slices = 0;
+  int64_t rows_p = 0, kp = 0;
+  bool is_a = true;
+};
+bool bem_exact_available();
+// Slices sign * M (complex128, column-major, leading dimension ld): role A:
+// M is rows x k; role B: M is k x rows.  Workspace named by `name`.
+int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
+                   double sign, int slices, ExactOperand &op, cudaStream_t st);
+// C (+)= A B from prepared operands (complex128 C, column-major, ldc).
+int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const ExactOperand &b, double *C, int64_t ldc,
+                   int accumulate, cudaStream_t st);
 // Non-zero when a tensor-core pipeline wait ran out since the last reset (synchronizes).
 int bem_tc_error(bemgpu_ctx_s *ctx, bool reset);
 // C (complex128) = alpha A B + beta C, complex64 A and B, products summed

@@ -1,0 +1,465 @@
+// Complex128 GEMM on the tensor cores with FP64-class results, for the
+// refinement residual R = E - W Y and the trace products H X of the
+// mixed-precision solve.
+//
+//   * realified like gemm_tc.cu: D' = A' B'^T, A' (2m x 2k) rows (Ar, -Ai) /
+//     (Ai, Ar), B' (n x 2k) the float view of B's columns; D'(rho, c) is the
+//     double at offset rho + 2 ldc c of the complex column-major C.
+//   * block fixed point: after one exact power-of-two scaling per matrix
+//     (largest magnitude -> below 1), every entry x of a 16-complex block along
+//     K (one kernel K step, the same block for a row of A and a column of B)
+//     is written with the block's exponent E (block max < 2^E) as
+//       x = sum_{l<SL} q_l 2^(E - 8(l+1)) + r,  |q_0| <= 256, |q_l| <= 128,
+//     each q rounded to nearest, |r| <= 2^(E - 8 SL - 1); slice l holds
+//     q_l 2^(E - 8(l+1)) as bf16 (exact: at most 9 significant bits).
+//   * slice products of level L = a + b share one unit per K step, and a
+//     step's level sum stays below 2^24 units (32 products, |q q| <= 2^16), so
+//     the tensor cores sum levels 0..2 EXACTLY into FP32 TMEM buffers
+//     (double-buffered by step parity); levels 3..SL-1 (below 2^-24 of level 0)
+//     run in FP32 TMEM sums over the whole K.  Products of level >= SL are
+//     dropped (below 2^(-8 SL) of the block maxima's product).
+//   * eight epilogue warps drain each step while the next runs: hi + lo += X0
+//     and += X1 (TwoSum each: exact), lo += X2 (rounding ~2^-40 of the sum);
+//     at the end C = 2^-(sa+sb) (hi + lo + levels
+//     3..) [+ C] in FP64.
+//   * pipeline: warp 0 TMA (64-byte swizzle, 32-deep K steps, 3 stages),
+//     warp 1 tcgen05.mma (M=128, N=64, K=16, bf16 -> FP32) and TMEM
+//     allocation, warps 2..9 epilogue.  Every wait is bounded; a wait that
+//     runs out sets the error flag and the CTA finishes.
+#include "bemgpu_internal.h"
+
+#include "tc_common.cuh"
+
+namespace {
+
+constexpr int EX_BM = 128, EX_BN = 64, EX_BK = 32;  // tile of D'; K step (bf16 elements, 64 bytes)
+constexpr int EX_STAGES = 3;
+constexpr int EX_A_TILE = EX_BM * EX_BK * 2;  // 8 KB per slice
+constexpr int EX_B_TILE = EX_BN * EX_BK * 2;  // 4 KB per slice
+constexpr int EX_EPI_WARPS = 8;
+constexpr int EX_THREADS = 64 + 32 * EX_EPI_WARPS;
+constexpr int EX_TMEM_COLS = 512;  // 2 x levels 0..2 x 64 + levels 3, 4 x 64
+constexpr int EX_SCALE_TARGET = 0;  // largest magnitude of a matrix is scaled to below 2^0: slice products
+                                    // and their sums stay inside FP32's range
+constexpr int EX_FLUSH_E = -80;     // blocks whose maximum (scaled) is below 2^-80 are zero (slices >= 2^-120)
+
+template <int SL>
+__host__ __device__ constexpr int ex_stage_bytes() { return SL * (EX_A_TILE + EX_B_TILE); }
+template <int SL>
+__host__ __device__ constexpr int ex_smem_bytes() { return EX_STAGES * ex_stage_bytes<SL>() + 1024 + 256; }
+
+// product p (level-major order) -> level, slice of A, slice of B
+__host__ __device__ constexpr int ex_level(int p) { return p < 1 ? 0 : p < 3 ? 1 : p < 6 ? 2 : p < 10 ? 3 : 4; }
+__host__ __device__ constexpr int ex_first(int level) { return level * (level + 1) / 2; }
+
+struct ExMaps {
+  CUtensorMap a[5];
+  CUtensorMap b[5];
+};
+
+template <int SL>
+__global__ void __launch_bounds__(EX_THREADS, 1)
+    ex_gemm_kernel(const __grid_constant__ ExMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf, int mvalid,
+                   int nvalid, int accumulate, const int *__restrict__ shifts, int *err) {
+  constexpr int NP = SL * (SL + 1) / 2;
+  constexpr int STAGE = ex_stage_bytes<SL>();
+  extern __shared__ unsigned char ex_smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(ex_smem_raw) + 1023) &
+                                                          ~(uintptr_t)1023);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + EX_STAGES * STAGE);
+  uint64_t *empty = full + EX_STAGES;
+  uint64_t *accf = empty + EX_STAGES;  // step buffer b written (MMA -> epilogue)
+  uint64_t *acce = accf + 2;           // step buffer b drained (epilogue -> MMA)
+  uint64_t *fin = acce + 2;            // all MMAs of this CTA complete
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * EX_BM, n0 = blockIdx.y * EX_BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < EX_STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], EX_EPI_WARPS);
+    }
+    mbar_init(fin, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(EX_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int kt = 0; kt < ktiles; kt++) {
+        const int s = kt % EX_STAGES, round = kt / EX_STAGES;
+        if (kt >= EX_STAGES && !mbar_wait(&empty[s], (round - 1) & 1, err)) break;
+        mbar_expect_tx(&full[s], STAGE);
+        unsigned char *st = smem + s * STAGE;
+#pragma unroll
+        for (int a = 0; a < SL; a++) tma_load_2d(st + a * EX_A_TILE, &maps.a[a], kt * EX_BK, m0, &full[s]);
+#pragma unroll
+        for (int b = 0; b < SL; b++)
+          tma_load_2d(st + SL * EX_A_TILE + b * EX_B_TILE, &maps.b[b], kt * EX_BK, n0, &full[s]);
+        issued = kt + 1;
+      }
+      // copies still in flight after an early stop land before the CTA exits
+      for (int kt = issued > EX_STAGES ? issued - EX_STAGES : 0; kt < issued; kt++)
+        if (!mbar_wait(&full[kt % EX_STAGES], (kt / EX_STAGES) & 1, err)) break;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(EX_BM, EX_BN);
+      for (int kt = 0; kt < ktiles; kt++) {
+        const int s = kt % EX_STAGES, round = kt / EX_STAGES, b = kt & 1, use = kt >> 1;
+        if (kt >= 2 && !mbar_wait(&acce[b], (use - 1) & 1, err)) break;
+        if (!mbar_wait(&full[s], round & 1, err)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t st = smem_u32(smem + s * STAGE);
+#pragma unroll
+        for (int ks = 0; ks < EX_BK / 16; ks++) {
+#pragma unroll
+          for (int p = 0; p < NP; p++) {
+            const int level = ex_level(p), a = p - ex_first(level), bb = level - a;
+            const uint64_t da = smem_desc_sw64(st + a * EX_A_TILE + ks * 32);
+            const uint64_t db = smem_desc_sw64(st + SL * EX_A_TILE + bb * EX_B_TILE + ks * 32);
+            const bool first = ks == 0 && p == ex_first(level);
+            if (level <= 2)
+              tc_mma(tmem + (uint32_t)((3 * b + level) * EX_BN), da, db, idesc, first ? 0u : 1u);
+            else
+              tc_mma(tmem + (uint32_t)((3 + level) * EX_BN), da, db, idesc, (first && kt == 0) ? 0u : 1u);
+          }
+        }
+        tc_commit(&empty[s]);
+        tc_commit(&accf[b]);
+      }
+      tc_commit(fin);
+      mbar_wait(fin, 0, err);
+    }
+  } else {
+    const int quarter = warp & 3, group = (warp - 2) >> 2;
+    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(group * 32);
+    float hi[32], lo[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) hi[j] = lo[j] = 0.f;
+    bool ok = true;
+#pragma unroll 1
+    for (int kt = 0; kt < ktiles; kt++) {
+      const int b = kt & 1, use = kt >> 1;
+      int got = 1;
+      if (lane == 0) got = mbar_wait(&accf[b], use & 1, err) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t tx = lane_base + (uint32_t)(3 * b * EX_BN);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        float x[8], y1[8], y2[8];
+        tc_ld8(tx + 8 * q, x);
+        tc_ld8(tx + EX_BN + 8 * q, y1);
+        tc_ld8(tx + 2 * EX_BN + 8 * q, y2);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          two_sum_acc(hi[8 * q + j], lo[8 * q + j], x[j]);
+          two_sum_acc(hi[8 * q + j], lo[8 * q + j], y1[j]);
+          lo[8 * q + j] += y2[j];
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+    }
+    if (ok && SL > 3) {
+      int got = 1;
+      if (lane == 0) got = mbar_wait(fin, 0, err) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, got, 0) != 0;
+    }
+    const int rho = m0 + quarter * 32 + lane;
+    const double scale = ldexp(1.0, -(shifts[0] + shifts[1]));
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      float z3[8], z4[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) z3[j] = z4[j] = 0.f;
+      if (ok && SL > 3) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        tc_ld8(lane_base + (uint32_t)(6 * EX_BN) + 8 * q, z3);
+        if (SL > 4) tc_ld8(lane_base + (uint32_t)(7 * EX_BN) + 8 * q, z4);
+      }
+      if (ok && rho < mvalid) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int c = n0 + group * 32 + 8 * q + j;
+          if (c < nvalid) {
+            double *p = C + rho + ldcf * (int64_t)c;
+            const double v =
+                scale * (((double)hi[8 * q + j] + (double)lo[8 * q + j]) + ((double)z3[j] + (double)z4[j]));
+            *p = accumulate ? *p + v : v;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(EX_TMEM_COLS));
+  }
+}
+
+}  // namespace
+
+namespace {
+
+__device__ __forceinline__ double pow2d(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
+
+// Largest max(|re|, |im|) of a complex128 matrix (m x k, column-major) as the
+// bits of a non-negative double (ordered like the value) -> *out (atomicMax).
+__global__ void ex_absmax_kernel(const double *__restrict__ A, int64_t lda, int m, int k,
+                                 unsigned long long *out) {
+  double mx = 0.0;
+  const int64_t total = (int64_t)m * k;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = i / m, r = i - c * m;
+    const double2 v = reinterpret_cast<const double2 *>(A)[r + lda * c];
+    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+}
+
+// Scaling exponent of the matrix whose largest magnitude has bits *amax: the
+// power of two bringing it just below 2^EX_SCALE_TARGET (0 for a zero matrix).
+__device__ __forceinline__ int ex_matrix_shift(const unsigned long long *amax) {
+  const unsigned long long bits = *amax;
+  if (bits == 0) return 0;
+  const int eb = (int)((bits >> 52) & 0x7ff);  // value in [2^(eb-1023), 2^(eb-1022))
+  if (eb == 0) return EX_SCALE_TARGET + 1022;  // subnormal maximum
+  return EX_SCALE_TARGET - (eb - 1022);
+}
+
+// Block exponent E (block max < 2^E) of a scaled block maximum; flush marker
+// when the block is zero or below 2^EX_FLUSH_E.
+constexpr int EX_ZERO = -100000;
+__device__ __forceinline__ int ex_block_exponent(double mx) {
+  if (!(mx > 0.0)) return EX_ZERO;
+  const int eb = (int)((__double_as_longlong(mx) >> 52) & 0x7ff);
+  const int E = eb - 1022;
+  return (eb == 0 || E < EX_FLUSH_E) ? EX_ZERO : E;
+}
+
+template <int SL>
+__device__ __forceinline__ void ex_split(double x, int E, __nv_bfloat16 *s) {
+  if (E == EX_ZERO) {
+#pragma unroll
+    for (int l = 0; l < SL; l++) s[l] = __float2bfloat16_rn(0.f);
+    return;
+  }
+  double rem = x;
+#pragma unroll
+  for (int l = 0; l < SL; l++) {
+    const int e = E - 8 * (l + 1);
+    const double v = rint(rem * pow2d(-e)) * pow2d(e);
+    rem -= v;  // exact
+    s[l] = __float2bfloat16_rn((float)v);  // exact: <= 9 significant bits, exponent >= -120
+  }
+}
+
+__device__ __forceinline__ double half_warp_max(double v) {
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// A' slices (Mp x Kp) of sign * A (complex128, m x k, column-major), block
+// fixed point over 16-complex blocks of each row (half a warp).  Thread
+// (r, q): complex row r, complex column q (q fast).  Also records the
+// matrix's scaling exponent in *shift.
+template <int SL>
+__global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int m, int k, double sign,
+                                 const unsigned long long *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Mp,
+                                 int64_t Kp) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (2 * q >= Kp) return;  // whole warps: Kp / 2 is a multiple of 32
+  const int g = ex_matrix_shift(amax);
+  if (q == 0 && r == 0) *shift = g;
+  double ar = 0.0, ai = 0.0;
+  if (r < m && q < k) {
+    const double2 v = reinterpret_cast<const double2 *>(A)[r + lda * (int64_t)q];
+    ar = sign * v.x * pow2d(g);
+    ai = sign * v.y * pow2d(g);
+  }
+  const int E = ex_block_exponent(half_warp_max(fmax(fabs(ar), fabs(ai))));
+  __nv_bfloat16 sr[SL], si[SL], sn[SL];
+  ex_split<SL>(ar, E, sr);
+  ex_split<SL>(ai, E, si);
+#pragma unroll
+  for (int l = 0; l < SL; l++) sn[l] = __hneg(si[l]);
+  const int64_t plane = Mp * Kp;
+  const int64_t i0 = (int64_t)(2 * r) * Kp + 2 * q, i1 = i0 + Kp;
+#pragma unroll
+  for (int l = 0; l < SL; l++) {
+    reinterpret_cast<__nv_bfloat162 *>(S + l * plane + i0)[0] = __halves2bfloat162(sr[l], sn[l]);  // (Ar, -Ai)
+    reinterpret_cast<__nv_bfloat162 *>(S + l * plane + i1)[0] = __halves2bfloat162(si[l], sr[l]);  // (Ai, Ar)
+  }
+}
+
+// B' slices (Np x Kp): row c = column c of complex128 B (k x n); blocks of 16
+// complex rows (half a warp).
+template <int SL>
+__global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int k, int n,
+                                 const unsigned long long *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Np,
+                                 int64_t Kp) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (2 * q >= Kp) return;
+  const int g = ex_matrix_shift(amax);
+  if (q == 0 && c == 0) *shift = g;
+  double br = 0.0, bi = 0.0;
+  if (c < n && q < k) {
+    const double2 v = reinterpret_cast<const double2 *>(B)[q + ldb * (int64_t)c];
+    br = v.x * pow2d(g);
+    bi = v.y * pow2d(g);
+  }
+  const int E = ex_block_exponent(half_warp_max(fmax(fabs(br), fabs(bi))));
+  __nv_bfloat16 sr[SL], si[SL];
+  ex_split<SL>(br, E, sr);
+  ex_split<SL>(bi, E, si);
+  const int64_t plane = Np * Kp, i0 = (int64_t)c * Kp + 2 * q;
+#pragma unroll
+  for (int l = 0; l < SL; l++)
+    reinterpret_cast<__nv_bfloat162 *>(S + l * plane + i0)[0] = __halves2bfloat162(sr[l], si[l]);
+}
+
+bool ex_maps(CUtensorMap *maps, const __nv_bfloat16 *S, int slices, int64_t rows, int64_t kp, int box_rows) {
+  for (int l = 0; l < slices; l++)
+    if (!make_map_bf16(&maps[l], S + l * rows * kp, rows, kp, EX_BK, box_rows, CU_TENSOR_MAP_SWIZZLE_64B))
+      return false;
+  return true;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+
+bool bem_exact_available() { return encode_fn() != nullptr; }
+
+int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
+                   double sign, int slices, ExactOperand &op, cudaStream_t st) {
+  if (slices != 4 && slices != 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
+  if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
+  const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
+                          : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
+  const int64_t kp = ((2 * (int64_t)k + 63) / 64) * 64;  // K steps of 32; whole warps in the slicing
+  if ((is_a ? rp / 2 : rp) > 65535) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d rows too many", rows);
+  const std::string base = std::string("ex_") + name;
+  op.S = bem_workspace(ctx, base, sizeof(__nv_bfloat16) * (size_t)slices * rp * kp);
+  op.aux = (int *)bem_workspace(ctx, base + "_aux", 64);
+  if (!op.S || !op.aux) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
+  op.rows = rows;
+  op.k = k;
+  op.rows_p = rp;
+  op.kp = kp;
+  op.slices = slices;
+  op.is_a = is_a;
+  unsigned long long *amax = reinterpret_cast<unsigned long long *>(op.aux + 8);
+  {
+    ProfScope ps(ctx, BEMGPU_K_SLICE, st, 0.0, 16.0 * (double)rows * k * 2 + 4.0 * slices * (double)rp * kp);
+    BEM_CUDA_TRY(ctx, cudaMemsetAsync(amax, 0, sizeof(unsigned long long), st));
+    ex_absmax_kernel<<<2 * 152, 256, 0, st>>>(M, ld, is_a ? rows : k, is_a ? k : rows, amax);
+    ctx->launches++;
+    const dim3 grid((unsigned)((kp / 2 + 127) / 128), (unsigned)(is_a ? rp / 2 : rp));
+    __nv_bfloat16 *S = (__nv_bfloat16 *)op.S;
+    if (is_a) {
+      if (slices == 5)
+        ex_prep_a_kernel<5><<<grid, 128, 0, st>>>(M, ld, rows, k, sign, amax, op.aux, S, rp, kp);
+      else
+        ex_prep_a_kernel<4><<<grid, 128, 0, st>>>(M, ld, rows, k, sign, amax, op.aux, S, rp, kp);
+    } else {
+      if (slices == 5)
+        ex_prep_b_kernel<5><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
+      else
+        ex_prep_b_kernel<4><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
+    }
+    ctx->launches++;
+  }
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const ExactOperand &b, double *C, int64_t ldc,
+                   int accumulate, cudaStream_t st) {
+  if (!a.is_a || b.is_a || a.k != b.k || a.kp != b.kp || a.slices != b.slices)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: operands do not match");
+  const int m = a.rows, n = b.rows, SL = a.slices;
+  ExMaps maps;
+  if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SL, a.rows_p, a.kp, EX_BM) ||
+      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SL, b.rows_p, b.kp, EX_BN))
+    return bem_fail(ctx, BEMGPU_ERR_CUDA, "exact gemm: tensor map encoding failed");
+  int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
+  if (!err) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
+  if (!ctx->ex_ready) {
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<5>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<4>()));
+    ctx->ex_ready = true;
+  }
+  if (!ctx->tc_err_ready) {
+    BEM_CUDA_TRY(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
+    ctx->tc_err_ready = true;
+  }
+  // shifts of A and B side by side for the kernel
+  int *shifts = (int *)bem_workspace(ctx, "ex_shifts", 2 * sizeof(int));
+  if (!shifts) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(shifts, a.aux, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(shifts + 1, b.aux, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  const int np = SL * (SL + 1) / 2;
+  ProfScope ps(ctx, kind, st, 8.0 * m * (double)n * a.k,
+               2.0 * SL * ((double)a.rows_p * a.kp * ((b.rows_p + EX_BN - 1) / EX_BN) / 8.0 + (double)b.rows_p * b.kp) +
+                   16.0 * m * (double)n * (accumulate ? 2 : 1));
+  (void)np;
+  const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / EX_BN));
+  const int ktiles = (int)(a.kp / EX_BK);
+  if (SL == 5)
+    ex_gemm_kernel<5><<<grid, EX_THREADS, ex_smem_bytes<5>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
+                                                                    shifts, err);
+  else
+    ex_gemm_kernel<4><<<grid, EX_THREADS, ex_smem_bytes<4>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
+                                                                    shifts, err);
+  ctx->launches++;
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+extern "C" int bemgpu_zgemm_exact(bemgpu_ctx_t ctx, int m, int n, int k, const double *dA, int64_t lda,
+                                  const double *dB, int64_t ldb, double *dC, int64_t ldc, int accumulate, int slices) {
+  if (!ctx || !dA || !dB || !dC || m < 1 || n < 1 || k < 1 || lda < m || ldb < k || ldc < m)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "zgemm_exact: bad arguments");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (!bem_exact_available()) return bem_fail(ctx, BEMGPU_ERR_CUDA, "zgemm_exact: tensor maps unavailable");
+  ExactOperand a, b;
+  int rc = bem_exact_prep(ctx, "cabi_a", true, dA, lda, m, k, 1.0, slices, a, ctx->stream);
+  if (!rc) rc = bem_exact_prep(ctx, "cabi_b", false, dB, ldb, n, k, 1.0, slices, b, ctx->stream);
+  if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRACE, a, b, dC, ldc, accumulate, ctx->stream);
+  if (rc) return rc;
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (bem_tc_error(ctx, true)) return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "zgemm_exact: a pipeline wait ran out");
+  return BEMGPU_OK;
+}

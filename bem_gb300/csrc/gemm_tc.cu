@@ -19,9 +19,9 @@
 //     finishes, frees its TMEM and the host returns BEMGPU_ERR_TIMEOUT.
 #include "bemgpu_internal.h"
 
-#include <cuda.h>
-#include <cuda_bf16.h>
 #include <algorithm>
+
+#include "tc_common.cuh"
 
 namespace {
 
@@ -32,126 +32,14 @@ constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;      // 16 KB per slice tile (A
 constexpr int TC_STAGE_BYTES = 2 * TC_SLICES * TC_TILE_BYTES;  // 96 KB
 constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 192;
-constexpr unsigned TC_WAIT_LIMIT = 1u << 26;
 
 // products (a, b) with a + b <= 2 (0-based slice indices)
 __constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
 __constant__ int c_prod_b[6] = {0, 1, 0, 2, 1, 0};
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// Bounded wait on phase parity; returns false (and flags) if the limit is hit.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
-  const uint32_t a = smem_u32(bar);
-  for (unsigned it = 0; it < TC_WAIT_LIMIT; it++) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  atomicExch(err, 1);
-  return false;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-// Copies still in flight when a pipeline stops early land before the CTA
-// exits: wait (bounded) for the last TC_STAGES stages the producer issued.
-__device__ __forceinline__ void drain_copies(uint64_t *full, int issued, int *err);
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
-  d |= (uint64_t)1 << 16;                         // leading byte offset (unused with swizzle)
-  d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset
-  d |= (uint64_t)1 << 46;                         // descriptor version
-  d |= (uint64_t)2 << 61;                         // 128-byte swizzle
-  return d;
-}
-
-// Instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, both K-major.
-__host__ __device__ constexpr uint32_t tc_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t accum) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-          tmem_d),
-      "l"(da), "l"(db), "r"(idesc), "r"(accum));
-}
-
-__device__ __forceinline__ void tc_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-
 __device__ __forceinline__ void drain_copies(uint64_t *full, int issued, int *err) {
   for (int kt = issued > TC_STAGES ? issued - TC_STAGES : 0; kt < issued; kt++)
     if (!mbar_wait(&full[kt % TC_STAGES], (kt / TC_STAGES) & 1, err)) return;
-}
-
-__device__ __forceinline__ void tc_ld8(uint32_t taddr, float *v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
-      "[%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
 struct TcMaps {
@@ -279,13 +167,6 @@ constexpr int TCC_EPI_WARPS = 8;
 constexpr int TCC_TMEM_COLS = 512;  // 2 x (X, Y1, Y2) x 64 columns, rounded to a power of two
 constexpr int TCC_THREADS = 64 + 32 * TCC_EPI_WARPS;
 
-// hi + lo += p (Knuth's TwoSum: the rounding error of hi + p goes to lo).
-__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float p) {
-  const float s = hi + p;
-  const float bp = s - hi;
-  lo += (hi - (s - bp)) + (p - bp);
-  hi = s;
-}
 
 // One 128 x 64 tile of D' summed exactly enough for a refinement residual.
 // The operands arrive as block fixed-point slices (one exponent per row and
@@ -546,35 +427,8 @@ __global__ void tc_prep_b_kernel(const float *__restrict__ B, int64_t ldb, int k
   reinterpret_cast<__nv_bfloat162 *>(S + 2 * plane + idx)[0] = __halves2bfloat162(a3, b3);
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-  }
-  return fn;
-}
-
 bool make_map(CUtensorMap *map, const void *base, int64_t rows, int64_t kp, int box_rows = TC_BM) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)(kp * 2)};
-  cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return make_map_bf16(map, base, rows, kp, TC_BK, box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 }  // namespace
@@ -608,14 +462,15 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
                                            TC_SMEM_BYTES));
     BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(tc_gemm_comp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            TCC_SMEM_BYTES));
+    ctx->tc_ready = true;
   }
   __nv_bfloat16 *SA = (__nv_bfloat16 *)bem_workspace(ctx, "tc_A", sizeof(__nv_bfloat16) * TC_SLICES * Mp * Kp);
   __nv_bfloat16 *SB = (__nv_bfloat16 *)bem_workspace(ctx, "tc_B", sizeof(__nv_bfloat16) * TC_SLICES * Np * Kp);
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
   if (!SA || !SB || !err) return bem_fail(ctx, BEMGPU_ERR_OOM, "cgemm_tc: workspace");
-  if (!ctx->tc_ready) {
+  if (!ctx->tc_err_ready) {
     BEM_CUDA_TRY(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
-    ctx->tc_ready = true;
+    ctx->tc_err_ready = true;
   }
   TcMaps maps;
   for (int i = 0; i < TC_SLICES; i++) {
@@ -653,8 +508,13 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
   return BEMGPU_OK;
 }
 
+// The tensor-core kernels keep one 128-wide tile per SM and stream C once, so
+// they pay off from a few K steps on; rank-64 updates (LU, triangular
+// solves) run faster on the FMA pipes.
+constexpr int TC_MIN_K = 256;
+
 static bool tc_usable(int engine, int m, int n, int k) {
-  return engine != 2 && m >= 64 && n >= 64 && k >= 16 && 2 * (int64_t)m <= 2 * 65535 &&
+  return engine != 2 && (engine == 1 || k >= TC_MIN_K) && m >= 64 && n >= 64 && k >= 16 && 2 * (int64_t)m <= 2 * 65535 &&
          (int64_t)n <= 65535 - TC_BN && encode_fn() != nullptr;
 }
 

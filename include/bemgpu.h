@@ -178,6 +178,14 @@ int bemgpu_cgemm(bemgpu_ctx_t ctx, int m, int n, int k, const float *dA, int64_t
 int bemgpu_cgemm_acc64(bemgpu_ctx_t ctx, int m, int n, int k, const float *dA, int64_t lda, const float *dB,
                        int64_t ldb, double *dC, int64_t ldc, int accumulate, int engine);
 
+/* C (complex128) = A B [+ C] with FP64-class accuracy on the tensor cores:
+ * A, B complex128, cut into `slices` (4 or 5) block fixed-point bf16 slices
+ * whose products the tensor cores sum exactly per K step; error ~2^(-8 slices)
+ * of the K-blocks' largest magnitudes.  The product of the refinement
+ * residual and the trace (src/HeatTransfer.cpp:40-58).  Synchronous. */
+int bemgpu_zgemm_exact(bemgpu_ctx_t ctx, int m, int n, int k, const double *dA, int64_t lda, const double *dB,
+                       int64_t ldb, double *dC, int64_t ldc, int accumulate, int slices);
+
 /* ---- per-frequency solve ---- */
 /* CalcHeatTransfer: top is the two-body tree (s's RWGs first, then t's),
  * s and t the one-body trees, all over one geometry.  Writes the spectral

@@ -144,3 +144,59 @@ def test_acc64_beats_fp32_accumulation_on_long_sums():
     e64 = np.max(np.abs(_gemm64(A, B, np.zeros((m, n)), 0, 1) - ref) / scale)
     e32 = np.max(np.abs(_gemm(A, B, np.zeros((m, n), np.complex64), 0, 1) - ref) / scale)
     assert e64 < 2e-8 and e64 < 0.25 * e32, (e64, e32)
+
+
+def _zgemm_exact(A, B, C0, accumulate, slices):
+    import torch
+    ctx = api.default_context()
+    A, B, C0 = (np.asarray(x, dtype=np.complex128) for x in (A, B, C0))
+    m, k = A.shape
+    n = B.shape[1]
+    assert B.shape[0] == k and C0.shape == (m, n)
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dC = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda()
+    torch.cuda.synchronize()
+    rc = _lib.load().bemgpu_zgemm_exact(ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), m,
+                                        ctypes.c_void_p(dB.data_ptr()), k, ctypes.c_void_p(dC.data_ptr()), m,
+                                        int(accumulate), slices)
+    assert rc == 0, _lib.load().bemgpu_ctx_last_error(ctx.handle)
+    return dC.cpu().numpy().T
+
+
+@pytest.mark.parametrize("m,n,k", [(64, 64, 16), (100, 70, 37), (300, 200, 1000)])
+@pytest.mark.parametrize("slices", [4, 5])
+def test_exact_gemm_matches_fp64(m, n, k, slices):
+    """Block fixed point with `slices` slices: each entry is represented to
+    2^(-8 slices - 1) of its 16-entry K-block's largest magnitude and the
+    tensor cores sum the slice products exactly, so the product is within a
+    few 2^(-8 slices) of sum_k |a| |b| -- far beyond FP32 for 5 slices."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(m * 3 + n + k + slices)
+    A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    C0 = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    scale = np.abs(A) @ np.abs(B)
+    tol = {4: 2e-9, 5: 1e-11}[slices]
+    for acc in (0, 1):
+        got = _zgemm_exact(A, B, C0, acc, slices)
+        ref = A @ B + (C0 if acc else 0)
+        err = np.max(np.abs(got - ref) / scale)
+        assert err < tol, (slices, acc, err)
+
+
+def test_exact_gemm_dynamic_range_and_scaling():
+    """Entries of A spanning 1e-8..1e8 along its rows, an overall scale of
+    1e-200 (the per-matrix power-of-two scaling) and a zero block: the error
+    stays at 2^-41 of each K-block's largest term."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    m, n, k = 256, 128, 512
+    A = (rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))) * 10.0 ** rng.uniform(-8, 8, (m, k))
+    B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    A[:, 32:64] = 0
+    A *= 1e-200
+    got = _zgemm_exact(A, B, np.zeros((m, n)), 0, 5)
+    ref = A @ B
+    scale = np.abs(A) @ np.abs(B)
+    assert np.max(np.abs(got - ref) / scale) < 1e-9
