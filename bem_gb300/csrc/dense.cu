@@ -185,6 +185,213 @@ __global__ void laswp_kernel(T *A, int64_t lda, int c0, int c1, int k1, int k2, 
   }
 }
 
+
+// ---------------- cooperative panel factorization ----------------
+// The whole panel [k0, k0 + w) in one cooperative launch: CTA g keeps rows
+// [k0 + g chunk, k0 + (g+1) chunk) of the panel in shared memory (row-major),
+// and per column j: (1) each CTA publishes its local pivot candidate (value,
+// row, the row's w entries) and, if it owns the diagonal row, that row;
+// (2) one grid barrier; (3) every CTA reduces the G candidates to the same
+// pivot, the owners of the diagonal and pivot rows exchange them, and each
+// CTA scales column j and applies the rank-1 update to its own rows.  One
+// barrier per column (candidate slots double-buffered by column parity); the
+// barrier's spin is bounded and sets *err when it runs out.  Same pivots and
+// arithmetic as the one-launch-per-column kernel above.
+constexpr int COOP_THREADS = 256;
+constexpr unsigned COOP_SPIN_LIMIT = 1u << 24;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(COOP_THREADS)
+    panel_coop_kernel(T *A, int64_t lda, int n, int k0, int w, int chunk, int *ipiv, int *info, double *cval,
+                      int *crow, T *cdata_raw, T *drow_raw, unsigned *counter, int *err) {
+  typedef typename V2<T>::type T2;
+  extern __shared__ __align__(16) unsigned char coop_smem[];
+  T2 *P = reinterpret_cast<T2 *>(coop_smem);  // chunk x w, P[i * w + c]
+  T2 *prow = P + (int64_t)chunk * w;           // the pivot (U) row of the current column
+  T2 *A2 = reinterpret_cast<T2 *>(A);
+  T2 *cdata = reinterpret_cast<T2 *>(cdata_raw);
+  T2 *drow = reinterpret_cast<T2 *>(drow_raw);
+  __shared__ double red_v[COOP_THREADS / 32];
+  __shared__ int red_i[COOP_THREADS / 32], red_w[COOP_THREADS / 32];
+  __shared__ int s_row, s_win;
+  __shared__ bool s_abort, s_zero;
+  const int G = gridDim.x, g = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int rbeg = k0 + g * chunk, rend = min(n, rbeg + chunk);
+  const int nloc = max(0, rend - rbeg);
+  for (int idx = tid; idx < nloc * w; idx += COOP_THREADS) {
+    const int i = idx % nloc, c = idx / nloc;
+    P[i * w + c] = A2[(rbeg + i) + lda * (int64_t)(k0 + c)];
+  }
+  if (tid == 0) s_abort = false;
+  __syncthreads();
+  for (int j = 0; j < w; j++) {
+    const int dr = k0 + j, par = j & 1;
+    // (1) local candidate: first row of largest |re| + |im| in column j, rows >= dr
+    double bv = -1.0;
+    int bi = 0x7fffffff;
+    for (int i = tid; i < nloc; i += COOP_THREADS) {
+      const int r = rbeg + i;
+      if (r < dr) continue;
+      const T2 a = P[i * w + j];
+      const double v = fabs((double)a.x) + fabs((double)a.y);
+      if (v > bv || (v == bv && r < bi)) {
+        bv = v;
+        bi = r;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (v2 > bv || (v2 == bv && i2 < bi)) {
+        bv = v2;
+        bi = i2;
+      }
+    }
+    if (lane == 0) {
+      red_v[wid] = bv;
+      red_i[wid] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int q = 1; q < COOP_THREADS / 32; q++)
+        if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) {
+          bv = red_v[q];
+          bi = red_i[q];
+        }
+      cval[par * G + g] = bv;
+      crow[par * G + g] = bi;
+      s_row = bi;
+    }
+    __syncthreads();
+    if (s_row != 0x7fffffff)
+      for (int c = tid; c < w; c += COOP_THREADS) cdata[(int64_t)(par * G + g) * w + c] = P[(s_row - rbeg) * w + c];
+    if (dr >= rbeg && dr < rend)
+      for (int c = tid; c < w; c += COOP_THREADS) drow[par * w + c] = P[(dr - rbeg) * w + c];
+    __syncthreads();
+    // (2) grid barrier
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(counter, 1u);
+      const unsigned target = (unsigned)G * (unsigned)(j + 1);
+      unsigned it = 0;
+      while (ld_acquire_u32(counter) < target) {
+        if (++it > COOP_SPIN_LIMIT) {
+          atomicExch(err, 1);
+          s_abort = true;
+          break;
+        }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (s_abort) return;
+    // (3) the pivot: every CTA reduces the same candidates in the same way
+    bv = -1.0;
+    bi = 0x7fffffff;
+    int bw = 0;
+    for (int q = tid; q < G; q += COOP_THREADS) {
+      const double v = __ldcg(cval + par * G + q);
+      const int r = __ldcg(crow + par * G + q);
+      if (r == 0x7fffffff) continue;
+      if (v > bv || (v == bv && r < bi)) {
+        bv = v;
+        bi = r;
+        bw = q;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      const int w2 = __shfl_xor_sync(0xffffffffu, bw, o);
+      if (v2 > bv || (v2 == bv && i2 < bi)) {
+        bv = v2;
+        bi = i2;
+        bw = w2;
+      }
+    }
+    if (lane == 0) {
+      red_v[wid] = bv;
+      red_i[wid] = bi;
+      red_w[wid] = bw;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int win = bw;
+      for (int q = 1; q < COOP_THREADS / 32; q++)
+        if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) {
+          bv = red_v[q];
+          bi = red_i[q];
+          win = red_w[q];
+        }
+      if (bi == 0x7fffffff) win = -1;
+      const bool zero = !(bv > 0.0);
+      if (zero) bi = dr;
+      s_zero = zero;
+      s_row = bi;
+      s_win = win;
+      if (g == 0) {
+        ipiv[dr] = bi;
+        if (zero && *info == 0) *info = dr + 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_row;
+    const bool zero = s_zero;
+    for (int c = tid; c < w; c += COOP_THREADS) {
+      T2 v;
+      if (p == dr || s_win < 0) {
+        const T2 *src = drow + par * w + c;
+        v = __ldcg(src);
+      } else {
+        v = __ldcg(cdata + (int64_t)(par * G + s_win) * w + c);
+      }
+      prow[c] = v;
+    }
+    __syncthreads();
+    if (p != dr) {
+      if (dr >= rbeg && dr < rend)
+        for (int c = tid; c < w; c += COOP_THREADS) P[(dr - rbeg) * w + c] = prow[c];
+      if (p >= rbeg && p < rend)
+        for (int c = tid; c < w; c += COOP_THREADS) P[(p - rbeg) * w + c] = __ldcg(drow + par * w + c);
+    }
+    __syncthreads();
+    // scale column j below the diagonal, then the rank-1 update of columns > j
+    const T2 pv = prow[j];
+    const cx<T> rp = zero ? cx<T>{0, 0} : crecip(cx<T>{pv.x, pv.y});
+    for (int i = tid; i < nloc; i += COOP_THREADS) {
+      if (rbeg + i <= dr || zero) continue;
+      const T2 a = P[i * w + j];
+      const cx<T> l = cmul(cx<T>{a.x, a.y}, rp);
+      P[i * w + j] = V2<T>::make(l.r, l.i);
+    }
+    __syncthreads();
+    const int wr = w - j - 1;
+    if (wr > 0)
+      for (int idx = tid; idx < nloc * wr; idx += COOP_THREADS) {
+        const int i = idx / wr, c = j + 1 + idx % wr;
+        if (rbeg + i <= dr) continue;
+        const T2 l = P[i * w + j], u = prow[c];
+        T2 a = P[i * w + c];
+        a.x -= l.x * u.x - l.y * u.y;
+        a.y -= l.x * u.y + l.y * u.x;
+        P[i * w + c] = a;
+      }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < nloc * w; idx += COOP_THREADS) {
+    const int i = idx % nloc, c = idx / nloc;
+    A2[(rbeg + i) + lda * (int64_t)(k0 + c)] = P[i * w + c];
+  }
+}
+
 // B[0:w, :] <- L11^{-1} B (unit lower) or U11^{-1} B (upper) with the w x w
 // diagonal block in shared memory; one warp per right-hand-side column, lane
 // holds rows lane and lane+32.
@@ -472,6 +679,66 @@ int gemm_any<float>(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, 
   return bem_cgemm(ctx, kind, opA, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream);
 }
 
+constexpr int COOP_MAX_SMEM = 200 * 1024;
+
+// Factors the panel [k0, k0 + w) with one cooperative launch; returns false
+// (nothing launched) when the panel does not fit the cooperative kernel.
+template <typename T>
+bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int *d_ipiv, int *d_info,
+                cudaStream_t stream, int &rc) {
+  typedef typename V2<T>::type T2;
+  rc = BEMGPU_OK;
+  const int rows = n - k0;
+  const int G = std::max(1, std::min(ctx->num_sms, (rows + 15) / 16));
+  const int chunk = (rows + G - 1) / G;
+  const size_t smem = sizeof(T2) * (size_t)(chunk + 1) * w;
+  if (smem > (size_t)COOP_MAX_SMEM) return false;
+  static bool attr[64][2] = {};
+  const int ti = sizeof(T) == 8 ? 1 : 0;
+  if (!attr[ctx->device][ti]) {
+    if (cudaFuncSetAttribute(panel_coop_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, COOP_MAX_SMEM) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    attr[ctx->device][ti] = true;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_coop_kernel<T>, COOP_THREADS, smem) !=
+          cudaSuccess ||
+      per_sm * ctx->num_sms < G) {
+    cudaGetLastError();
+    return false;
+  }
+  double *cval = (double *)bem_workspace(ctx, "coop_cval", sizeof(double) * 2 * 1024);
+  int *crow = (int *)bem_workspace(ctx, "coop_crow", sizeof(int) * 2 * 1024);
+  T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * 1024 * (size_t)NB);
+  T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)NB);
+  unsigned *counter = (unsigned *)bem_workspace(ctx, "coop_counter", sizeof(unsigned));
+  int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
+  if (!cval || !crow || !cdata || !drow || !counter || !err || G > 1024 || w > NB) {
+    rc = bem_fail(ctx, BEMGPU_ERR_OOM, "getrf: panel workspace");
+    return true;
+  }
+  if (!ctx->tc_err_ready) {
+    cudaMemsetAsync(err, 0, sizeof(int), stream);
+    ctx->tc_err_ready = true;
+  }
+  cudaMemsetAsync(counter, 0, sizeof(unsigned), stream);
+  int n_ = n, k0_ = k0, w_ = w, chunk_ = chunk;
+  void *args[] = {&A, &lda, &n_, &k0_, &w_, &chunk_, &d_ipiv, &d_info, &cval, &crow, &cdata, &drow, &counter, &err};
+  const double cb = 2.0 * sizeof(T);
+  ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 4.0 * (double)rows * w * w, cb * 2.0 * rows * w);
+  const cudaError_t e = cudaLaunchCooperativeKernel((const void *)panel_coop_kernel<T>, dim3(G), dim3(COOP_THREADS),
+                                                    args, smem, stream);
+  ctx->launches++;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    rc = bem_fail(ctx, BEMGPU_ERR_CUDA, "getrf: cooperative panel launch: %s", cudaGetErrorString(e));
+  }
+  return true;
+}
+
 template <typename T>
 int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
   if (int rc0 = set_trsm_attrs<T>(ctx)) return rc0;
@@ -486,7 +753,10 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
     const int w = std::min(NB, n - k0);
     const int rows = n - k0;
     const int blocks = std::max(1, std::min(ctx->num_sms * 2, (rows + PANEL_THREADS - 1) / PANEL_THREADS));
-    for (int jj = 0; jj <= w; jj++) {
+    int prc = BEMGPU_OK;
+    const bool coop = ctx->coop_panel && panel_coop<T>(ctx, A, lda, n, k0, w, d_ipiv, d_info, stream, prc);
+    if (prc) return prc;
+    for (int jj = 0; !coop && jj <= w; jj++) {
       ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 8.0 * (rows - jj) * (w - jj), cb * 2 * (rows - jj) * (w - jj));
       panel_step_kernel<T><<<blocks, PANEL_THREADS, 0, stream>>>(A, lda, n, k0, w, jj, d_ipiv, d_info, cand, counter);
       ctx->launches++;

@@ -199,6 +199,8 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(S, dS, sizeof S, cudaMemcpyDeviceToHost, st));
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
   BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if (bem_tc_error(ctx, true))
+    return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "heat_transfer: a grid-barrier or pipeline wait ran out");
   if (hinfo != 0) return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "heat_transfer: zero pivot at column %d", hinfo);
   *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
   if (info) {
