@@ -176,6 +176,13 @@ int bem_zgetrs(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int
 int bem_cgetrf(bemgpu_ctx_s *ctx, float *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream);
 int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int *d_ipiv, float *B, int64_t ldb,
                int nrhs, cudaStream_t stream);
+// L^{-1} (unit lower) and U^{-1} (upper) of a packed complex64 LU (n x n,
+// leading dimension ld), each stored dense (n x n, zeros in the other triangle).
+int bem_ctri_inverses(bemgpu_ctx_s *ctx, const float *LU, int64_t ld, int n, float *Linv, float *Uinv,
+                      cudaStream_t st);
+// B <- U^{-1} L^{-1} P B with the explicit inverses (tmp: n x nrhs complex64).
+int bem_capply_inverse(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv, float *B,
+                       int64_t ldb, int nrhs, float *tmp, cudaStream_t st);
 // complex64 GEMM: tensor cores where the shape allows (gemm_tc.cu), else FMA pipes.
 int bem_cgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const float alpha[2], const float *A,
               int64_t lda, const float *B, int64_t ldb, const float beta[2], float *C, int64_t ldc,

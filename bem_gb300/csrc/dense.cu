@@ -860,3 +860,154 @@ int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int 
                int nrhs, cudaStream_t stream) {
   return getrs_impl<float>(ctx, A, lda, n, d_ipiv, B, ldb, nrhs, stream);
 }
+
+// ---------------- explicit triangular inverses (complex64 mixed path) ----------------
+// The correction solves of the refinement apply W32^{-1} = U^{-1} L^{-1} P to
+// n_t right-hand sides several times per frequency.  Forming L^{-1} and U^{-1}
+// once (recursive blocked inversion, ztrtri-style, whose work is large GEMMs)
+// turns every solve into two large tensor-core GEMMs instead of 2 n / 64
+// dependent rank-64 steps.
+namespace {
+
+// In-place inverses of the 64 x 64 diagonal blocks of X (n x n, ld ldx; the
+// last block may be smaller): unit lower (UPPER = false) or upper.  CTA b
+// inverts block b; thread j computes column j.
+constexpr int TRI_INV_SMEM = 2 * 64 * 65 * 8;
+
+template <bool UPPER>
+__global__ void __launch_bounds__(64) tri_inv_block_kernel(float *X0, int64_t ldx, int n) {
+  extern __shared__ float2 tri_smem[];
+  float2(*T)[65] = reinterpret_cast<float2(*)[65]>(tri_smem);            // T[col][row]
+  float2(*R)[65] = reinterpret_cast<float2(*)[65]>(tri_smem + 64 * 65);  // R[col][row]
+  const int o = blockIdx.x * 64, w = min(64, n - o);
+  float *X = X0 + 2 * ((int64_t)o + ldx * o);
+  const int j = threadIdx.x;
+  for (int c = 0; c < w; c++)
+    if (j < w) T[c][j] = reinterpret_cast<const float2 *>(X)[j + ldx * (int64_t)c];
+  __syncthreads();
+  if (j < w) {
+    if (!UPPER) {
+      for (int i = 0; i < w; i++) R[j][i] = make_float2(i == j ? 1.f : 0.f, 0.f);
+      for (int i = j + 1; i < w; i++) {  // x_i = -sum_{j <= k < i} L_ik x_k
+        float sr = 0.f, si = 0.f;
+        for (int k = j; k < i; k++) {
+          const float2 l = T[k][i], x = R[j][k];
+          sr += l.x * x.x - l.y * x.y;
+          si += l.x * x.y + l.y * x.x;
+        }
+        R[j][i] = make_float2(-sr, -si);
+      }
+    } else {
+      for (int i = 0; i < w; i++) R[j][i] = make_float2(0.f, 0.f);
+      {
+        const float2 d = T[j][j];
+        const float dd = d.x * d.x + d.y * d.y;
+        R[j][j] = make_float2(d.x / dd, -d.y / dd);
+      }
+      for (int i = j - 1; i >= 0; i--) {  // x_i = -(sum_{i < k <= j} U_ik x_k) / U_ii
+        float sr = 0.f, si = 0.f;
+        for (int k = i + 1; k <= j; k++) {
+          const float2 u = T[k][i], x = R[j][k];
+          sr += u.x * x.x - u.y * x.y;
+          si += u.x * x.y + u.y * x.x;
+        }
+        const float2 d = T[i][i];
+        const float dd = d.x * d.x + d.y * d.y;
+        // -(s / d) = -(s conj(d)) / |d|^2
+        R[j][i] = make_float2(-(sr * d.x + si * d.y) / dd, -(si * d.x - sr * d.y) / dd);
+      }
+    }
+  }
+  __syncthreads();
+  for (int c = 0; c < w; c++)
+    if (j < w) reinterpret_cast<float2 *>(X)[j + ldx * (int64_t)c] = R[c][j];
+}
+
+// Copies the unit-lower factor (UPPER = false: ones on the diagonal, zeros
+// above) or the upper factor (zeros below) of the packed LU into D.
+template <bool UPPER>
+__global__ void tri_extract_kernel(const float *__restrict__ LU, int64_t ld, int n, float *__restrict__ D) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (r >= n) return;
+  float2 v = reinterpret_cast<const float2 *>(LU)[r + ld * (int64_t)c];
+  if (!UPPER) {
+    if (r < c) v = make_float2(0.f, 0.f);
+    if (r == c) v = make_float2(1.f, 0.f);
+  } else if (r > c) {
+    v = make_float2(0.f, 0.f);
+  }
+  reinterpret_cast<float2 *>(D)[r + (int64_t)n * c] = v;
+}
+
+// Recursive in-place inversion of the triangular block X[o:o+m, o:o+m] (ld n).
+int tri_inv_rec(bemgpu_ctx_s *ctx, bool upper, float *X, int64_t n, int o, int m, float *tmp, cudaStream_t st) {
+  float *Xo = X + 2 * ((int64_t)o + n * o);
+  if (m <= NB) return BEMGPU_OK;  // diagonal blocks are inverted up front (tri_inv_block_kernel)
+  const int m1 = ((m / 2 + NB - 1) / NB) * NB, m2 = m - m1;
+  int rc = tri_inv_rec(ctx, upper, X, n, o, m1, tmp, st);
+  if (!rc) rc = tri_inv_rec(ctx, upper, X, n, o + m1, m2, tmp, st);
+  if (rc) return rc;
+  const float one[2] = {1.f, 0.f}, mone[2] = {-1.f, 0.f}, zero[2] = {0.f, 0.f};
+  float *X11 = Xo, *X22 = X + 2 * ((int64_t)(o + m1) + n * (o + m1));
+  if (!upper) {
+    // X21 = -X22 (L21 X11): tmp (m2 x m1) = L21 X11, then X21 = -X22 tmp
+    float *X21 = X + 2 * ((int64_t)(o + m1) + n * o);
+    rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m2, m1, m1, one, X21, n, X11, n, zero, tmp, m2, st);
+    if (!rc) rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m2, m1, m2, mone, X22, n, tmp, m2, zero, X21, n, st);
+  } else {
+    // X12 = -X11 (U12 X22): tmp (m1 x m2) = U12 X22, then X12 = -X11 tmp
+    float *X12 = X + 2 * ((int64_t)o + n * (o + m1));
+    rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m1, m2, m2, one, X12, n, X22, n, zero, tmp, m1, st);
+    if (!rc) rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m1, m2, m1, mone, X11, n, tmp, m1, zero, X12, n, st);
+  }
+  return rc;
+}
+
+}  // namespace
+
+int bem_ctri_inverses(bemgpu_ctx_s *ctx, const float *LU, int64_t ld, int n, float *Linv, float *Uinv,
+                      cudaStream_t st) {
+  float *tmp = (float *)bem_workspace(ctx, "tri_tmp", 8 * (size_t)(n / 2 + NB) * (size_t)(n / 2 + NB));
+  if (!tmp) return bem_fail(ctx, BEMGPU_ERR_OOM, "tri_inverses: workspace");
+  {
+    ProfScope ps(ctx, BEMGPU_K_TRSM, st, 0.0, 32.0 * (double)n * n);
+    const dim3 g((n + 255) / 256, n);
+    tri_extract_kernel<false><<<g, 256, 0, st>>>(LU, ld, n, Linv);
+    tri_extract_kernel<true><<<g, 256, 0, st>>>(LU, ld, n, Uinv);
+    ctx->launches += 2;
+  }
+  {
+    static bool attr[64] = {false};
+    if (!attr[ctx->device]) {
+      BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(tri_inv_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             TRI_INV_SMEM));
+      BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(tri_inv_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             TRI_INV_SMEM));
+      attr[ctx->device] = true;
+    }
+    const int nb = (n + NB - 1) / NB;
+    ProfScope ps(ctx, BEMGPU_K_TRSM, st, 2.0 * nb * 4.0 * NB * NB * NB / 3.0, 2.0 * 16.0 * NB * (double)n);
+    tri_inv_block_kernel<false><<<nb, 64, TRI_INV_SMEM, st>>>(Linv, n, n);
+    tri_inv_block_kernel<true><<<nb, 64, TRI_INV_SMEM, st>>>(Uinv, n, n);
+    ctx->launches += 2;
+  }
+  int rc = tri_inv_rec(ctx, false, Linv, n, 0, n, tmp, st);
+  if (!rc) rc = tri_inv_rec(ctx, true, Uinv, n, 0, n, tmp, st);
+  if (rc) return rc;
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return BEMGPU_OK;
+}
+
+int bem_capply_inverse(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv, float *B,
+                       int64_t ldb, int nrhs, float *tmp, cudaStream_t st) {
+  {
+    ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, 32.0 * (double)n * nrhs);
+    laswp_kernel<float><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, 0, nrhs, 0, n, d_ipiv);
+    ctx->launches++;
+  }
+  const float one[2] = {1.f, 0.f}, zero[2] = {0.f, 0.f};
+  int rc = bem_cgemm(ctx, BEMGPU_K_SOLVE_GEMM, 'N', n, nrhs, n, one, Linv, n, B, ldb, zero, tmp, n, st);
+  if (!rc) rc = bem_cgemm(ctx, BEMGPU_K_SOLVE_GEMM, 'N', n, nrhs, n, one, Uinv, n, tmp, n, zero, B, ldb, st);
+  return rc;
+}

@@ -4,11 +4,15 @@
 // (FP64).  The reference inverts W in FP64 (src/util/DenseMatrix.cpp:65-77) and
 // forms S = 1/4 tr(B2^H B1) (src/HeatTransfer.cpp:36-58).  Here:
 //
-//   1. W32 = fl32(W); LU of W32 in complex64 (tensor-core trailing updates).
+//   1. W32 = fl32(W); LU of W32 in complex64, then L^{-1} and U^{-1} explicitly
+//      (recursive blocked inversion: large tensor-core GEMMs), so that every
+//      solve below is two GEMMs: W32^{-1} B = U^{-1} (L^{-1} (P B)).
 //   2. Y0 = W32^{-1} E_t (E_t: the t columns of the identity), widened to FP64.
 //   3. Iterative refinement: R = E_t - W Y with W and Y in FP64 on the tensor
 //      cores (gemm_exact.cu: 5-slice block fixed point, exact slice sums, error
 //      ~2^-41 of each K-block's largest term); Y += fl64(W32^{-1} fl32(R)).
+//      The refinement's fixed point depends only on this residual; the
+//      complex64 inverse sets how fast it is reached.
 //      W is sliced once per solve, Y once per step.  A residual accurate only to
 //      FP32 (2^-24 of |W||Y|) leaves the spectral power off by up to ~1e-6 at
 //      low loss; the 41-bit product brings that to ~1e-9.
@@ -155,7 +159,7 @@ __global__ void trace_final_kernel(const double *partial, int np, double *out) {
 namespace {
 
 struct MixedBufs {
-  float *W32, *R32;
+  float *W32, *R32, *Linv, *Uinv, *T32;
   double *H1, *H2, *Y, *R64, *XH, *B1, *C, *partial;
   int *ipiv, *info;
   int ntiles;
@@ -207,6 +211,9 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   b.ntiles = ((ns2 + 31) / 32) * ((nt2 + 31) / 32);
   b.W32 = (float *)bem_workspace(ctx, "m_W32", 8 * nn);
   b.R32 = (float *)bem_workspace(ctx, "m_R32", 8 * nm);
+  b.Linv = (float *)bem_workspace(ctx, "m_Linv", 8 * nn);
+  b.Uinv = (float *)bem_workspace(ctx, "m_Uinv", 8 * nn);
+  b.T32 = (float *)bem_workspace(ctx, "m_T32", 8 * nm);
   b.H1 = (double *)bem_workspace(ctx, "m_H1", 16 * (size_t)ns2 * ns2);
   b.H2 = (double *)bem_workspace(ctx, "m_H2", 16 * (size_t)nt2 * nt2);
   b.Y = (double *)bem_workspace(ctx, "m_Y", 16 * nm);
@@ -217,7 +224,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   b.partial = (double *)bem_workspace(ctx, "m_partial", 16 * (size_t)b.ntiles + 64);
   b.ipiv = (int *)bem_workspace(ctx, "m_ipiv", 4 * (size_t)n);
   b.info = (int *)bem_workspace(ctx, "m_info", 16);
-  const bool ok = b.W32 && b.R32 && b.H1 && b.H2 && b.Y && b.R64 && b.XH && b.B1 && b.C && b.partial && b.ipiv &&
+  const bool ok = b.W32 && b.R32 && b.Linv && b.Uinv && b.T32 && b.H1 && b.H2 && b.Y && b.R64 && b.XH && b.B1 && b.C && b.partial && b.ipiv &&
                   b.info;
   if (!ok) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: workspace allocation failed (n=%d)", n);
   cudaEvent_t *ev = ctx->ev;
@@ -239,11 +246,12 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   if (rc) return rc;
   cudaEventRecord(ev[1], st);
   rc = bem_cgetrf(ctx, b.W32, n, n, b.ipiv, b.info, st);
+  if (!rc) rc = bem_ctri_inverses(ctx, b.W32, n, n, b.Linv, b.Uinv, st);
   if (rc) return rc;
   cudaEventRecord(ev[2], st);
   identity_cols_c64_kernel<<<gm, 256, 0, st>>>(b.R32, n, n, ns2, nt2);
   ctx->launches++;
-  rc = bem_cgetrs(ctx, b.W32, n, n, b.ipiv, b.R32, n, nt2, st);
+  rc = bem_capply_inverse(ctx, b.Linv, b.Uinv, n, b.ipiv, b.R32, n, nt2, b.T32, st);
   if (rc) return rc;
   update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 0);
   ctx->launches++;
@@ -265,7 +273,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
     if (rc) return rc;
     residual_finish_kernel<<<gm, 256, 0, st>>>(b.R64, b.R32, n, n, ns2);
     ctx->launches++;
-    rc = bem_cgetrs(ctx, b.W32, n, n, b.ipiv, b.R32, n, nt2, st);
+    rc = bem_capply_inverse(ctx, b.Linv, b.Uinv, n, b.ipiv, b.R32, n, nt2, b.T32, st);
     if (rc) return rc;
     update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 1);
     ctx->launches++;
