@@ -6,19 +6,22 @@
 //     (Ai, Ar), B' (n x 2k) the float view of B's columns; D'(rho, c) is the
 //     double at offset rho + 2 ldc c of the complex column-major C.
 //   * block fixed point: after one exact power-of-two scaling per matrix
-//     (largest magnitude -> below 1), every entry x of a 16-complex block along
-//     K (one kernel K step, the same block for a row of A and a column of B)
+//     (largest magnitude -> below 1), every entry x of a 64-complex block along
+//     K (one drain step = four 32-deep TMA stages; the same block for a row of
+//     A and a column of B)
 //     is written with the block's exponent E (block max < 2^E) as
 //       x = sum_{l<SL} q_l 2^(E - 8(l+1)) + r,  |q_0| <= 256, |q_l| <= 128,
 //     each q rounded to nearest, |r| <= 2^(E - 8 SL - 1); slice l holds
 //     q_l 2^(E - 8(l+1)) as bf16 (exact: at most 9 significant bits).
-//   * slice products of level L = a + b share one unit per K step, and a
-//     step's level sum stays below 2^24 units (32 products, |q q| <= 2^16), so
+//   * slice products of level L = a + b share one unit per drain step, and a
+//     step's level sum stays below 2^24 units (128 products of |q q| <= 2^16
+//     for level 0, 128 x (2^15 + 2^14 + 2^15) for level 2), so
 //     the tensor cores sum levels 0..2 EXACTLY into FP32 TMEM buffers
 //     (double-buffered by step parity); levels 3..SL-1 (below 2^-24 of level 0)
 //     run in FP32 TMEM sums over the whole K.  Products of level >= SL are
 //     dropped (below 2^(-8 SL) of the block maxima's product).
-//   * eight epilogue warps drain each step while the next runs: hi + lo += X0
+//   * eight epilogue warps drain each step while the next runs (three TMEM
+//     loads behind one wait per 8 columns): hi + lo += X0
 //     and += X1 (TwoSum each: exact), lo += X2 (rounding ~2^-40 of the sum);
 //     at the end C = 2^-(sa+sb) (hi + lo + levels
 //     3..) [+ C] in FP64.
@@ -34,6 +37,7 @@ namespace {
 
 constexpr int EX_BM = 128, EX_BN = 64, EX_BK = 32;  // tile of D'; K step (bf16 elements, 64 bytes)
 constexpr int EX_STAGES = 3;
+constexpr int EX_DRAIN = 4;  // TMA stages per drain step (one exponent block of 64 complex)
 constexpr int EX_A_TILE = EX_BM * EX_BK * 2;  // 8 KB per slice
 constexpr int EX_B_TILE = EX_BN * EX_BK * 2;  // 4 KB per slice
 constexpr int EX_EPI_WARPS = 8;
@@ -73,7 +77,9 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   uint64_t *fin = acce + 2;            // all MMAs of this CTA complete
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * EX_BM, n0 = blockIdx.y * EX_BN;
+  int mt, nt;
+  grouped_tile(TC_RASTER_GROUP, mt, nt);
+  const int m0 = mt * EX_BM, n0 = nt * EX_BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < EX_STAGES; s++) {
@@ -120,8 +126,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = tc_idesc(EX_BM, EX_BN);
       for (int kt = 0; kt < ktiles; kt++) {
-        const int s = kt % EX_STAGES, round = kt / EX_STAGES, b = kt & 1, use = kt >> 1;
-        if (kt >= 2 && !mbar_wait(&acce[b], (use - 1) & 1, err)) break;
+        // drain step dt = kt / EX_DRAIN covers EX_DRAIN stages (one exponent block)
+        const int s = kt % EX_STAGES, round = kt / EX_STAGES, dt = kt / EX_DRAIN, b = dt & 1, use = dt >> 1;
+        const bool opening = kt % EX_DRAIN == 0, closing = kt % EX_DRAIN == EX_DRAIN - 1;
+        if (opening && dt >= 2 && !mbar_wait(&acce[b], (use - 1) & 1, err)) break;
         if (!mbar_wait(&full[s], round & 1, err)) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t st = smem_u32(smem + s * STAGE);
@@ -132,7 +140,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
             const int level = ex_level(p), a = p - ex_first(level), bb = level - a;
             const uint64_t da = smem_desc_sw64(st + a * EX_A_TILE + ks * 32);
             const uint64_t db = smem_desc_sw64(st + SL * EX_A_TILE + bb * EX_B_TILE + ks * 32);
-            const bool first = ks == 0 && p == ex_first(level);
+            const bool first = opening && ks == 0 && p == ex_first(level);
             if (level <= 2)
               tc_mma(tmem + (uint32_t)((3 * b + level) * EX_BN), da, db, idesc, first ? 0u : 1u);
             else
@@ -140,7 +148,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
           }
         }
         tc_commit(&empty[s]);
-        tc_commit(&accf[b]);
+        if (closing) tc_commit(&accf[b]);
       }
       tc_commit(fin);
       mbar_wait(fin, 0, err);
@@ -153,8 +161,8 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     for (int j = 0; j < 32; j++) hi[j] = lo[j] = 0.f;
     bool ok = true;
 #pragma unroll 1
-    for (int kt = 0; kt < ktiles; kt++) {
-      const int b = kt & 1, use = kt >> 1;
+    for (int dt = 0; dt < ktiles / EX_DRAIN; dt++) {
+      const int b = dt & 1, use = dt >> 1;
       int got = 1;
       if (lane == 0) got = mbar_wait(&accf[b], use & 1, err) ? 1 : 0;
       got = __shfl_sync(0xffffffffu, got, 0);
@@ -165,16 +173,20 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t tx = lane_base + (uint32_t)(3 * b * EX_BN);
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        float x[8], y1[8], y2[8];
-        tc_ld8(tx + 8 * q, x);
-        tc_ld8(tx + EX_BN + 8 * q, y1);
-        tc_ld8(tx + 2 * EX_BN + 8 * q, y2);
+      for (int h = 0; h < 2; h++) {  // two halves of 16 columns, six loads behind one wait each
+        uint32_t x[16], y1[16], y2[16];
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          two_sum_acc(hi[8 * q + j], lo[8 * q + j], x[j]);
-          two_sum_acc(hi[8 * q + j], lo[8 * q + j], y1[j]);
-          lo[8 * q + j] += y2[j];
+        for (int q = 0; q < 2; q++) {
+          tc_ld8_nowait(tx + 16 * h + 8 * q, x + 8 * q);
+          tc_ld8_nowait(tx + EX_BN + 16 * h + 8 * q, y1 + 8 * q);
+          tc_ld8_nowait(tx + 2 * EX_BN + 16 * h + 8 * q, y2 + 8 * q);
+        }
+        tc_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          two_sum_acc(hi[16 * h + j], lo[16 * h + j], __uint_as_float(x[j]));
+          two_sum_acc(hi[16 * h + j], lo[16 * h + j], __uint_as_float(y1[j]));
+          lo[16 * h + j] += __uint_as_float(y2[j]);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
@@ -279,14 +291,20 @@ __device__ __forceinline__ void ex_split(double x, int E, __nv_bfloat16 *s) {
   }
 }
 
-__device__ __forceinline__ double half_warp_max(double v) {
+// Maximum over the 64 consecutive threads (two warps) holding one exponent
+// block; the CTA is 128 threads and every thread calls it.
+__device__ __forceinline__ double block64_max(double v) {
+  __shared__ double wm[4];
 #pragma unroll
-  for (int o = 8; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) wm[w] = v;
+  __syncthreads();
+  return fmax(wm[w & ~1], wm[w | 1]);
 }
 
 // A' slices (Mp x Kp) of sign * A (complex128, m x k, column-major), block
-// fixed point over 16-complex blocks of each row (half a warp).  Thread
+// fixed point over 64-complex blocks of each row (two warps, one drain step).  Thread
 // (r, q): complex row r, complex column q (q fast).  Also records the
 // matrix's scaling exponent in *shift.
 template <int SL>
@@ -295,16 +313,17 @@ __global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int 
                                  int64_t Kp) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y;
-  if (2 * q >= Kp) return;  // whole warps: Kp / 2 is a multiple of 32
+  const bool active = 2 * q < Kp;
   const int g = ex_matrix_shift(amax);
   if (q == 0 && r == 0) *shift = g;
   double ar = 0.0, ai = 0.0;
-  if (r < m && q < k) {
+  if (active && r < m && q < k) {
     const double2 v = reinterpret_cast<const double2 *>(A)[r + lda * (int64_t)q];
     ar = sign * v.x * pow2d(g);
     ai = sign * v.y * pow2d(g);
   }
-  const int E = ex_block_exponent(half_warp_max(fmax(fabs(ar), fabs(ai))));
+  const int E = ex_block_exponent(block64_max(fmax(fabs(ar), fabs(ai))));
+  if (!active) return;
   __nv_bfloat16 sr[SL], si[SL], sn[SL];
   ex_split<SL>(ar, E, sr);
   ex_split<SL>(ai, E, si);
@@ -319,24 +338,25 @@ __global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int 
   }
 }
 
-// B' slices (Np x Kp): row c = column c of complex128 B (k x n); blocks of 16
-// complex rows (half a warp).
+// B' slices (Np x Kp): row c = column c of complex128 B (k x n); blocks of 64
+// complex rows (two warps).
 template <int SL>
 __global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int k, int n,
                                  const unsigned long long *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Np,
                                  int64_t Kp) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
-  if (2 * q >= Kp) return;
+  const bool active = 2 * q < Kp;
   const int g = ex_matrix_shift(amax);
   if (q == 0 && c == 0) *shift = g;
   double br = 0.0, bi = 0.0;
-  if (c < n && q < k) {
+  if (active && c < n && q < k) {
     const double2 v = reinterpret_cast<const double2 *>(B)[q + ldb * (int64_t)c];
     br = v.x * pow2d(g);
     bi = v.y * pow2d(g);
   }
-  const int E = ex_block_exponent(half_warp_max(fmax(fabs(br), fabs(bi))));
+  const int E = ex_block_exponent(block64_max(fmax(fabs(br), fabs(bi))));
+  if (!active) return;
   __nv_bfloat16 sr[SL], si[SL];
   ex_split<SL>(br, E, sr);
   ex_split<SL>(bi, E, si);
@@ -365,7 +385,7 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
   if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
                           : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
-  const int64_t kp = ((2 * (int64_t)k + 63) / 64) * 64;  // K steps of 32; whole warps in the slicing
+  const int64_t kp = ((2 * (int64_t)k + 127) / 128) * 128;  // whole drain steps (4 x 32)
   if ((is_a ? rp / 2 : rp) > 65535) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d rows too many", rows);
   const std::string base = std::string("ex_") + name;
   op.S = bem_workspace(ctx, base, sizeof(__nv_bfloat16) * (size_t)slices * rp * kp);

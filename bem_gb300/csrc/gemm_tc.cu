@@ -66,7 +66,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint64_t *accum_bar = empty + TC_STAGES;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum_bar + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
+  int mt, nt;
+  grouped_tile(TC_RASTER_GROUP, mt, nt);
+  const int m0 = mt * TC_BM, n0 = nt * TC_BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; s++) {
@@ -194,7 +196,9 @@ __global__ void __launch_bounds__(TCC_THREADS, 1)
   uint64_t *fin = acce + 2;             // all MMAs of this CTA complete
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TCC_BN;
+  int mt, nt;
+  grouped_tile(TC_RASTER_GROUP, mt, nt);
+  const int m0 = mt * TC_BM, n0 = nt * TCC_BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TCC_STAGES; s++) {

@@ -142,15 +142,29 @@ __global__ void identity_cols_c64_kernel(float *Y, int64_t ld, int n, int row0, 
   reinterpret_cast<float2 *>(Y)[r + ld * (int64_t)c] = make_float2(r == row0 + c ? 1.f : 0.f, 0.f);
 }
 
-__global__ void trace_final_kernel(const double *partial, int np, double *out) {
-  if (threadIdx.x != 0) return;
+// out = 1/4 sum of the np partial (re, im) pairs; one CTA of 256 threads, fixed
+// summation order (deterministic).
+__global__ void __launch_bounds__(256) trace_final_kernel(const double *partial, int np, double *out) {
+  __shared__ double sr[256], si[256];
   double r = 0, i = 0;
-  for (int k = 0; k < np; k++) {
+  for (int k = threadIdx.x; k < np; k += 256) {
     r += partial[2 * k];
     i += partial[2 * k + 1];
   }
-  out[0] = 0.25 * r;
-  out[1] = 0.25 * i;
+  sr[threadIdx.x] = r;
+  si[threadIdx.x] = i;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = 0.25 * sr[0];
+    out[1] = 0.25 * si[0];
+  }
 }
 
 }  // namespace
@@ -191,7 +205,7 @@ int spectral_trace(bemgpu_ctx_s *ctx, MixedBufs &b, int n, int ns2, int nt2, cud
     ProfScope ps(ctx, BEMGPU_K_TRACE, st, 8.0 * ns2 * nt2, 32.0 * ns2 * nt2);
     trace_tiles_kernel<<<tg, dim3(32, 8), 0, st>>>(b.B1, b.C, ns2, nt2, b.partial);
     ctx->launches++;
-    trace_final_kernel<<<1, 32, 0, st>>>(b.partial, b.ntiles, b.partial + 2 * b.ntiles);
+    trace_final_kernel<<<1, 256, 0, st>>>(b.partial, b.ntiles, b.partial + 2 * b.ntiles);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(S, b.partial + 2 * b.ntiles, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -98,6 +98,15 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float *v) {
 }
 
 
+// TMEM load of 8 columns without the wait (pair with tc_wait_ld before use).
+__device__ __forceinline__ void tc_ld8_nowait(uint32_t taddr, uint32_t *r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void tc_ld8(uint32_t taddr, float *v) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
@@ -132,6 +141,22 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
   d |= (uint64_t)4 << 61;  // 64-byte swizzle
   return d;
 }
+
+// Grouped rasterization of a (gridDim.x M-tiles) x (gridDim.y N-tiles) grid:
+// CTAs launched consecutively (linear id, x fastest) cover a band of `group`
+// M-tiles across the N-tiles, so the band's A tiles are re-read from L2, not
+// HBM, by every N-tile passing them.
+__device__ __forceinline__ void grouped_tile(int group, int &mt, int &nt) {
+  const int nM = gridDim.x, nN = gridDim.y;
+  const int L = blockIdx.y * nM + blockIdx.x;
+  const int per = group * nN;
+  const int g = L / per, first = g * group;
+  const int gm = min(nM - first, group);
+  const int local = L - g * per;
+  mt = first + local % gm;
+  nt = local / gm;
+}
+constexpr int TC_RASTER_GROUP = 8;
 
 // hi + lo += p (Knuth's TwoSum: the rounding error of hi + p goes to lo).
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float p) {
