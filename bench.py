@@ -238,11 +238,7 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
         "data": "synthetic (seeded jittered icospheres; no dataset)",
-        "config": {"workload": f"{args.workload}: two r=1um icospheres L3 (1280 tris, 1920 RWGs each), N={n_unknowns}, SiC, "
-                               f"gaps {wl['gaps']} um x {len(wl['freqs'])} f in 0.08-0.13 eV" if args.workload == "ico3"
-                   else args.workload,
-                   "precision": args.precision, "N": n_unknowns, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_unknowns ** 2 * 16 / 1e6)},
+        "config": workload_config(args, n_unknowns, world),
         "fill_gentries_per_s": entries / (fill_ms / 1e3) / 1e9,
         "stage_ms": {k: sum(i[k] for i in infos) / len(infos)
                      for k in ("ms_fill", "ms_lu", "ms_solve", "ms_trace", "ms_refine")},
@@ -256,6 +252,15 @@ def run_ours(args, rank, world):
         "P_sample": Ps[:2],
     }
     return out
+
+
+def workload_config(args, n_unknowns, world):
+    wl = WORKLOADS[args.workload]
+    name = (f"{args.workload}: two r=1um icospheres L3 (1280 tris, 1920 RWGs each), N={n_unknowns}, SiC, "
+            f"gaps {wl['gaps']} um x {len(wl['freqs'])} f in 0.08-0.13 eV" if args.workload == "ico3"
+            else args.workload)
+    return {"workload": name, "precision": args.precision, "N": n_unknowns, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_unknowns ** 2 * 16 / 1e6)}
 
 
 def run_reference_sample(wl_name, threads=None, frac=None):
@@ -291,7 +296,7 @@ def run_reference_sample(wl_name, threads=None, frac=None):
     B2 = (Wi[:, ns2:] @ W[ns2:, ns2:])[:ns2, :]
     _ = np.trace(B2.conj().T @ B1)
     t_la = time.perf_counter() - t0
-    return {"solve_s": t_fill + t_la, "fill_s": t_fill, "la_s": t_la, "threads": threads,
+    return {"solve_s": t_fill + t_la, "fill_s": t_fill, "la_s": t_la, "threads": threads, "n": n,
             "sample": f"fills over {k}/{ntri} test triangles (x{ntri / k:.1f}) + full-size inverse/products, "
                       f"n={n}, one frequency"}
 
@@ -308,7 +313,7 @@ def run_reference(args, rank, world):
     return {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded meshes; no dataset)",
-            "config": {"workload": args.workload, "N": None}, "impl": "reference",
+            "config": workload_config(args, samples[0]["n"], world), "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": samples[0]["threads"], "kind": "port",
                              "sample": samples[0]["sample"]},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
