@@ -22,8 +22,10 @@
 //     coalesced stores (src/Impedance.cpp:365-384).
 #include "bemgpu_internal.h"
 #include "quadrature_tables.h"
+#include "df64.cuh"
 
 #include <cmath>
+#include <vector>
 
 namespace {
 
@@ -37,6 +39,10 @@ struct FarOpts {
   double th6, th10, th15, th21;
 };
 
+// Fill arithmetic: FP64 (parity path), FP32 far pairs beyond 3 edge lengths,
+// or double-float for every quadrature node pair.
+enum { FILL_FP64 = 0, FILL_FP32_FAR = 1, FILL_DF = 2 };
+
 __constant__ double c_rule6[6][3];
 __constant__ double c_rule10[10][3];
 __constant__ double c_rule15[15][3];
@@ -45,6 +51,13 @@ __constant__ double c_rule36[36][3];
 __constant__ double c_rule91[91][3];
 __constant__ double c_rule105[105][3];
 __constant__ double c_line15[15][2];
+// The triangle rules as double-float (xi1, xi2, w) -> (hi, lo) x 3, for the df fill.
+__constant__ float c_rdf6[6][6];
+__constant__ float c_rdf10[10][6];
+__constant__ float c_rdf15[15][6];
+__constant__ float c_rdf21[21][6];
+__constant__ float c_rdf36[36][6];
+__constant__ float c_rdf91[91][6];
 
 // ---------------- small FP64 vector / complex helpers ----------------
 struct d3 {
@@ -94,11 +107,13 @@ __device__ __forceinline__ z3 rcross(d3 a, z3 b) {
 }
 __device__ __forceinline__ void zacc(z1 &a, z1 b) { a.r += b.r; a.i += b.i; }
 
-// exp(ikR) for real R: exp(Re(ik) R) * (cos(Im(ik) R), sin(Im(ik) R))
+// exp(ikR) for real R: exp(Re(ik) R) * (cos(Im(ik) R), sin(Im(ik) R)).  A
+// lossless medium (real k: the exterior fill) skips the exp, whose value is 1.
 __device__ __forceinline__ z1 zexp_ikR(const GreenDev &g, double R) {
-  double m = exp(g.ikr * R);
   double s, c;
   sincos(g.iki * R, &s, &c);
+  if (g.ikr == 0.0) return {c, s};
+  const double m = exp(g.ikr * R);
   return {m * c, m * s};
 }
 
@@ -126,6 +141,33 @@ __device__ __forceinline__ void store_block(HalfPairBlock *H, int ntr, int i, in
 __device__ __forceinline__ double scatter_coef(const TriRec &T, int i, const TriRec &S, int j) {
   double c = BEM_ONEOVER4PI * T.helen[i] * S.helen[j];
   return (T.hneg[i] != S.hneg[j]) ? -c : c;
+}
+
+// The nine (c L_ij, c K_ij) of a far pair from its outer moments (closed form
+// beside far_pair()).
+__device__ __forceinline__ void far_contract(const TriRec &T, const TriRec &S, const GreenDev &g, z1 U0, z1 U1, z3 U2,
+                                             z3 U3, z1 V0, z3 V1, z3 V2, z3 V3, HalfPairBlock *H, int ntr) {
+  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+  const z1 ksq = {g.ksqr, g.ksqi};
+  for (int i = 0; i < T.nh; i++) {
+    const d3 p0i = ld3(T.hp0[i]);
+    const d3 ei = p0i - Pt;
+    for (int j = 0; j < S.nh; j++) {
+      const d3 p0j = ld3(S.hp0[j]);
+      const d3 dj = p0j - Ps;
+      const d3 D = p0i - p0j;
+      // L_ij
+      z1 bracket = zsub(zsub(U1, rdot(dj, U2)), rdot(ei, U3));
+      zacc(bracket, zscale(dot(ei, dj), U0));
+      const z1 L = zsub(zscale(0.25, zmul(ksq, bracket)), U0);
+      // K_ij
+      z3 X = z3sub(z3sub(V1, zcross(V2, ei)), rcross(dj, V3));
+      X = z3add(X, zs_v(V0, cross(dj, ei)));
+      const z1 K = zscale(-0.25, rdot(D, X));
+      const double c = scatter_coef(T, i, S, j);
+      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, L), zscale(c, K));
+    }
+  }
 }
 
 // ---------------- far pairs ----------------
@@ -180,26 +222,108 @@ __device__ __noinline__ void far_pair(const TriRec &T, const TriRec &S, const Gr
     V2 = z3add(V2, z3scale(w, Q1));
     V3 = z3add(V3, zs_v(zscale(w, Q0), rho));
   }
-  const z1 ksq = {g.ksqr, g.ksqi};
-  for (int i = 0; i < T.nh; i++) {
-    const d3 p0i = ld3(T.hp0[i]);
-    const d3 ei = p0i - Pt;
-    for (int j = 0; j < S.nh; j++) {
-      const d3 p0j = ld3(S.hp0[j]);
-      const d3 dj = p0j - Ps;
-      const d3 D = p0i - p0j;
-      // L_ij
-      z1 bracket = zsub(zsub(U1, rdot(dj, U2)), rdot(ei, U3));
-      zacc(bracket, zscale(dot(ei, dj), U0));
-      const z1 L = zsub(zscale(0.25, zmul(ksq, bracket)), U0);
-      // K_ij
-      z3 X = z3sub(z3sub(V1, zcross(V2, ei)), rcross(dj, V3));
-      X = z3add(X, zs_v(V0, cross(dj, ei)));
-      const z1 K = zscale(-0.25, rdot(D, X));
-      const double c = scatter_coef(T, i, S, j);
-      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, L), zscale(c, K));
-    }
+  far_contract(T, S, g, U0, U1, U2, U3, V0, V1, V2, V3, H, ntr);
+}
+
+// ---------------- far pairs in double-float (FP64-class on the FP32 pipes) ----------------
+//
+// far_pair() with the inner rule (the nr x nr node pairs, where the time goes)
+// in double-float: pair-centred coordinates x = (D0 + rho) - l with D0 = P_t -
+// P_s, e^{ikR} from df sincos / exp (quadrant and ln2 reductions in FP64), the
+// four inner moments summed in df and widened to FP64 for the outer moments
+// and the closed-form contraction, which stay as in far_pair().
+struct df3 {
+  df x, y, z;
+};
+__device__ __forceinline__ df3 df3_make(d3 a) { return {df_make(a.x), df_make(a.y), df_make(a.z)}; }
+
+// e^{ikR} for the df distance R: (cos, sin)(Im(ik) R) e^{Re(ik) R}, all in df on
+// the FP32 pipes (FP64 reductions for phases of 200 rad and more).
+__device__ __forceinline__ void df_exp_ikR(const GreenDev &g, df ikr, df iki, df R, df &er, df &ei) {
+  df sn, cs;
+  const df th = df_mul(iki, R);
+  if (fabsf(th.hi) < 200.f)
+    df_sincos_df(th, sn, cs);
+  else
+    df_sincos(df_to_double(th), sn, cs);
+  if (g.ikr == 0.0) {
+    er = cs;
+    ei = sn;
+    return;
   }
+  const df a = df_mul(ikr, R);
+  if (a.hi < -85.f) {  // below FP32's range: e^-85 of the neighbouring nodes' size
+    er = {0.f, 0.f};
+    ei = {0.f, 0.f};
+    return;
+  }
+  const df m = df_exp_df(a);
+  er = df_mul(m, cs);
+  ei = df_mul(m, sn);
+}
+
+__device__ __noinline__ void far_pair_df(const TriRec &T, const TriRec &S, const GreenDev &g,
+                                         const double (*rule)[3], const float (*rdf)[6], int nr, HalfPairBlock *H,
+                                         int ntr) {
+  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+  const d3 v01t = ld3(T.v01), v02t = ld3(T.v02);
+  const df3 v01s = df3_make(ld3(S.v01)), v02s = df3_make(ld3(S.v02));
+  const d3 D0 = Pt - Ps;
+  const df ikr = df_make(g.ikr), iki = df_make(g.iki);
+  z1 U0 = {0, 0}, U1 = {0, 0}, V0 = {0, 0};
+  z3 U2 = z3zero(), U3 = z3zero(), V1 = z3zero(), V2 = z3zero(), V3 = z3zero();
+  for (int q = 0; q < nr; q++) {
+    const double a = rule[q][0], b = rule[q][1], w = rule[q][2];
+    const d3 rho = a * v01t + b * v02t;
+    const df3 rts = df3_make(D0 + rho);  // r_t - P_s
+    df I0r = {0.f, 0.f}, I0i = {0.f, 0.f}, Q0r = {0.f, 0.f}, Q0i = {0.f, 0.f};
+    df Ar[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Ai[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    df Qr[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Qi[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int u = 0; u < nr; u++) {
+      const df as = {rdf[u][0], rdf[u][1]}, bs = {rdf[u][2], rdf[u][3]}, ws = {rdf[u][4], rdf[u][5]};
+      const df l[3] = {df_add(df_mul(as, v01s.x), df_mul(bs, v02s.x)), df_add(df_mul(as, v01s.y), df_mul(bs, v02s.y)),
+                       df_add(df_mul(as, v01s.z), df_mul(bs, v02s.z))};
+      const df xx = df_sub(rts.x, l[0]), xy = df_sub(rts.y, l[1]), xz = df_sub(rts.z, l[2]);
+      const df R2 = df_add(df_add(df_sqr(xx), df_sqr(xy)), df_sqr(xz));
+      const df R = df_sqrt(R2);
+      const df Ri = df_rcp(R);
+      df er, ei;
+      df_exp_ikR(g, ikr, iki, R, er, ei);
+      // scalar_gradient, src/GreensFunction.cpp:41-52: g = e / R, q = g (1 - ikR) / R^2
+      const df gr = df_mul(er, Ri), gi = df_mul(ei, Ri);
+      const df zr = df_mul(ikr, R), zi = df_mul(iki, R);
+      const df mr = df_add_f(df_neg(zr), 1.f), mi = df_neg(zi);  // 1 - ikR
+      const df Ri2 = df_sqr(Ri);
+      const df qr0 = df_sub(df_mul(gr, mr), df_mul(gi, mi)), qi0 = df_add(df_mul(gr, mi), df_mul(gi, mr));
+      const df qr = df_mul(qr0, Ri2), qi = df_mul(qi0, Ri2);
+      const df gwr = df_mul(ws, gr), gwi = df_mul(ws, gi), qwr = df_mul(ws, qr), qwi = df_mul(ws, qi);
+      I0r = df_add(I0r, gwr);
+      I0i = df_add(I0i, gwi);
+      Q0r = df_add(Q0r, qwr);
+      Q0i = df_add(Q0i, qwi);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        Ar[c] = df_add(Ar[c], df_mul(gwr, l[c]));
+        Ai[c] = df_add(Ai[c], df_mul(gwi, l[c]));
+        Qr[c] = df_add(Qr[c], df_mul(qwr, l[c]));
+        Qi[c] = df_add(Qi[c], df_mul(qwi, l[c]));
+      }
+    }
+    const z1 I0 = {df_to_double(I0r), df_to_double(I0i)}, Q0 = {df_to_double(Q0r), df_to_double(Q0i)};
+    const z3 A = {{df_to_double(Ar[0]), df_to_double(Ai[0])}, {df_to_double(Ar[1]), df_to_double(Ai[1])},
+                  {df_to_double(Ar[2]), df_to_double(Ai[2])}};
+    const z3 Q1 = {{df_to_double(Qr[0]), df_to_double(Qi[0])}, {df_to_double(Qr[1]), df_to_double(Qi[1])},
+                   {df_to_double(Qr[2]), df_to_double(Qi[2])}};
+    zacc(U0, zscale(w, I0));
+    zacc(U1, zscale(w, rdot(rho, A)));
+    U2 = z3add(U2, zs_v(zscale(w, I0), rho));
+    U3 = z3add(U3, z3scale(w, A));
+    zacc(V0, zscale(w, Q0));
+    V1 = z3add(V1, z3scale(w, zcross(Q1, rho)));
+    V2 = z3add(V2, z3scale(w, Q1));
+    V3 = z3add(V3, zs_v(zscale(w, Q0), rho));
+  }
+  far_contract(T, S, g, U0, U1, U2, U3, V0, V1, V2, V3, H, ntr);
 }
 
 // ---------------- far pairs in FP32 (mixed precision) ----------------
@@ -325,7 +449,7 @@ __device__ __noinline__ void far_pair_fp32(const TriRec &T, const TriRec &S, con
 // of the two triangles' longest edges) are integrated in FP32.
 __global__ void __launch_bounds__(128) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
                                                         const TriRec *__restrict__ Sr, int ntS, GreenDev g,
-                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mixed) {
+                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mode) {
   const int sb = blockIdx.x * blockDim.x + threadIdx.x;
   const int ta = blockIdx.y * blockDim.y + threadIdx.y;
   if (sb >= ntS || ta >= ntT) return;
@@ -336,7 +460,15 @@ __global__ void __launch_bounds__(128) far_pairs_kernel(const TriRec *__restrict
   const double d = dist2_rn(T.c, S.c);
   const double e = fmax(T.emax, S.emax);
   const double emax2 = __dmul_rn(e, e);
-  if (mixed && d > 9.0 * emax2) {
+  if (mode == FILL_DF) {
+    if (__dmul_rn(d, o.th6) > emax2) far_pair_df(T, S, g, c_rule6, c_rdf6, 6, H, ntr);
+    else if (__dmul_rn(d, o.th10) > emax2) far_pair_df(T, S, g, c_rule10, c_rdf10, 10, H, ntr);
+    else if (__dmul_rn(d, o.th15) > emax2) far_pair_df(T, S, g, c_rule15, c_rdf15, 15, H, ntr);
+    else if (__dmul_rn(d, o.th21) > emax2) far_pair_df(T, S, g, c_rule21, c_rdf21, 21, H, ntr);
+    else far_pair_df(T, S, g, c_rule36, c_rdf36, 36, H, ntr);
+    return;
+  }
+  if (mode == FILL_FP32_FAR && d > 9.0 * emax2) {
     // beyond 3 edge lengths every default threshold selects the 6-point rule;
     // the cascade is kept for non-default Options
     if (__dmul_rn(d, o.th6) > emax2) far_pair_fp32(T, S, g, c_rule6, 6, H, ntr);
@@ -437,13 +569,72 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 constexpr int NEAR_WARPS = 4;
 
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_fp64_kernel(
+// Smooth inner rule of a near pair at one outer node, double-float version:
+// the same moments as the FP64 loop in near_pairs_kernel (LKSmoothInnerIntegrand,
+// src/Impedance.cpp:93-105, with scalar_gradient_smooth, src/GreensFunction.cpp:54-69),
+// summed in df from df nodes (l, w) and widened to FP64.
+__device__ __noinline__ void near_inner_df(const float (*nd)[8], d3 rts, const GreenDev &g, z1 &I0o, z3 &Ao,
+                                              z1 &Q0o, z3 &Q1o) {
+  const df3 r = df3_make(rts);
+  const df ikr = df_make(g.ikr), iki = df_make(g.iki), k2r = df_make(g.k2r), k2i = df_make(g.k2i);
+  df I0r = {0.f, 0.f}, I0i = {0.f, 0.f}, Q0r = {0.f, 0.f}, Q0i = {0.f, 0.f};
+  df Ar[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Ai[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  df Qr[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Qi[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
+    const float4 n0 = *reinterpret_cast<const float4 *>(&nd[u][0]);
+    const float4 n1 = *reinterpret_cast<const float4 *>(&nd[u][4]);
+    const df l[3] = {{n0.x, n0.y}, {n0.z, n0.w}, {n1.x, n1.y}};
+    const df ws = {n1.z, n1.w};
+    const df xx = df_sub(r.x, l[0]), xy = df_sub(r.y, l[1]), xz = df_sub(r.z, l[2]);
+    const df R2 = df_add(df_add(df_sqr(xx), df_sqr(xy)), df_sqr(xz));
+    const df R = df_sqrt(R2);
+    const df Ri = df_rcp(R);
+    df er, ei;
+    df_exp_ikR(g, ikr, iki, R, er, ei);
+    // g~ = (e - 1)/R - k2 R
+    const df gr = df_sub(df_mul(df_add_f(er, -1.f), Ri), df_mul(k2r, R));
+    const df gi = df_sub(df_mul(ei, Ri), df_mul(k2i, R));
+    // q~ = (e (1 - ikR) + R^2 k2 - 1) / R^3
+    const df zr = df_mul(ikr, R), zi = df_mul(iki, R);
+    const df mr = df_add_f(df_neg(zr), 1.f), mi = df_neg(zi);
+    df nr = df_sub(df_mul(er, mr), df_mul(ei, mi));
+    df ni = df_add(df_mul(er, mi), df_mul(ei, mr));
+    nr = df_add_f(df_add(nr, df_mul(R2, k2r)), -1.f);
+    ni = df_add(ni, df_mul(R2, k2i));
+    const df Ri3 = df_mul(df_sqr(Ri), Ri);
+    const df qr = df_mul(Ri3, nr), qi = df_mul(Ri3, ni);
+    const df gwr = df_mul(ws, gr), gwi = df_mul(ws, gi), qwr = df_mul(ws, qr), qwi = df_mul(ws, qi);
+    I0r = df_add(I0r, gwr);
+    I0i = df_add(I0i, gwi);
+    Q0r = df_add(Q0r, qwr);
+    Q0i = df_add(Q0i, qwi);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      Ar[c] = df_add(Ar[c], df_mul(gwr, l[c]));
+      Ai[c] = df_add(Ai[c], df_mul(gwi, l[c]));
+      Qr[c] = df_add(Qr[c], df_mul(qwr, l[c]));
+      Qi[c] = df_add(Qi[c], df_mul(qwi, l[c]));
+    }
+  }
+  I0o = {df_to_double(I0r), df_to_double(I0i)};
+  Q0o = {df_to_double(Q0r), df_to_double(Q0i)};
+  Ao = {{df_to_double(Ar[0]), df_to_double(Ai[0])}, {df_to_double(Ar[1]), df_to_double(Ai[1])},
+        {df_to_double(Ar[2]), df_to_double(Ai[2])}};
+  Q1o = {{df_to_double(Qr[0]), df_to_double(Qi[0])}, {df_to_double(Qr[1]), df_to_double(Qi[1])},
+         {df_to_double(Qr[2]), df_to_double(Qi[2])}};
+}
+
+// DF: the smooth inner rule in double-float (near_inner_df), else FP64.
+template <bool DF>
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
     GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
-  __shared__ double s_nodes[NEAR_WARPS][BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
+  __shared__ double s_nodes[NEAR_WARPS][DF ? 1 : BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
+  __shared__ __align__(16) float s_nodes_df[NEAR_WARPS][DF ? BEMGPU_TRI_RULE91_N : 1][8];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   double(*nodes)[4] = s_nodes[wid];
+  float(*nodes_df)[8] = s_nodes_df[wid];
   const z1 ksq = {g.ksqr, g.ksqi};
   const z1 k2 = {g.k2r, g.k2i};
   for (int64_t p = (int64_t)blockIdx.x * NEAR_WARPS + wid; p < npairs; p += (int64_t)gridDim.x * NEAR_WARPS) {
@@ -456,8 +647,18 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_fp64_kernel(
       const d3 v01s = ld3(S.v01), v02s = ld3(S.v02);
       for (int u = lane; u < BEMGPU_TRI_RULE91_N; u += 32) {
         const d3 l = c_rule91[u][0] * v01s + c_rule91[u][1] * v02s;
-        nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
-        nodes[u][3] = c_rule91[u][2];
+        if (DF) {
+          const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            const df v = df_make(vals[c]);
+            nodes_df[u][2 * c] = v.hi;
+            nodes_df[u][2 * c + 1] = v.lo;
+          }
+        } else {
+          nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
+          nodes[u][3] = c_rule91[u][2];
+        }
       }
     }
     __syncwarp();
@@ -476,7 +677,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_fp64_kernel(
       // LKSmoothInnerIntegrand over s[0] (src/Impedance.cpp:93-105) as moments
       z1 I0 = {0, 0}, Q0 = {0, 0};
       z3 A = z3zero(), Q1 = z3zero();
-      for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
+      if (DF) near_inner_df(nodes_df, rts, g, I0, A, Q0, Q1);
+      for (int u = 0; !DF && u < BEMGPU_TRI_RULE91_N; u++) {
         const d3 l = {nodes[u][0], nodes[u][1], nodes[u][2]};
         const double ws = nodes[u][3];
         const d3 x = rts - l;
@@ -490,7 +692,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_fp64_kernel(
         z1 num = zmul(e, z1{1.0 - ikR.r, -ikR.i});
         num = zadd(num, zscale(R2, k2));
         num.r -= 1.0;
-        const z1 qq = zscale(Ri / R2, num);
+        const z1 qq = zscale(Ri * Ri * Ri, num);
         const z1 gw = zscale(ws, gs), qw = zscale(ws, qq);
         zacc(I0, gw);
         A = z3add(A, zs_v(gw, l));
@@ -707,6 +909,30 @@ int load_tables(bemgpu_ctx_s *ctx) {
   BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule91, bemgpu_tri_rule91, sizeof(bemgpu_tri_rule91)));
   BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule105, bemgpu_tri_rule105, sizeof(bemgpu_tri_rule105)));
   BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_line15, bemgpu_line_rule15, sizeof(bemgpu_line_rule15)));
+  {
+    auto split = [](const double (*rule)[3], int n, std::vector<float> &out) {
+      out.resize(6 * (size_t)n);
+      for (int i = 0; i < n; i++)
+        for (int c = 0; c < 3; c++) {
+          const float h = (float)rule[i][c];
+          out[6 * i + 2 * c] = h;
+          out[6 * i + 2 * c + 1] = (float)(rule[i][c] - (double)h);
+        }
+    };
+    std::vector<float> v;
+    split(bemgpu_tri_rule6, 6, v);
+    BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf6, v.data(), sizeof(float) * v.size()));
+    split(bemgpu_tri_rule10, 10, v);
+    BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf10, v.data(), sizeof(float) * v.size()));
+    split(bemgpu_tri_rule15, 15, v);
+    BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf15, v.data(), sizeof(float) * v.size()));
+    split(bemgpu_tri_rule21, 21, v);
+    BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf21, v.data(), sizeof(float) * v.size()));
+    split(bemgpu_tri_rule36, 36, v);
+    BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf36, v.data(), sizeof(float) * v.size()));
+    split(bemgpu_tri_rule91, 91, v);
+    BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf91, v.data(), sizeof(float) * v.size()));
+  }
   g_tables_loaded[ctx->device] = true;
   return BEMGPU_OK;
 }
@@ -722,6 +948,7 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
   if (!nl) return bem_fail(ctx, BEMGPU_ERR_OOM, "near list allocation failed");
   GreenDev gd = to_dev(g);
   FarOpts fo = {opt->farThresh6, opt->farThresh10, opt->farThresh15, opt->farThresh21};
+  const int mode = precision == BEMGPU_PREC_MIXED ? FILL_FP32_FAR : precision == BEMGPU_PREC_MIXED_LA ? FILL_DF : FILL_FP64;
   dim3 blk(32, 4);
   dim3 grd((s->ntri + 31) / 32, (t->ntri + 3) / 4);
   double far_flops = 0, far_bytes = 0, near_flops = 0, near_bytes = 0;
@@ -737,8 +964,7 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
   }
   {
     ProfScope ps(ctx, BEMGPU_K_FILL_FAR, stream, far_flops, far_bytes);
-    far_pairs_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg,
-                                              precision == BEMGPU_PREC_MIXED ? 1 : 0);
+    far_pairs_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, mode);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -746,7 +972,10 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
     int64_t blocks = (nl->n + NEAR_WARPS - 1) / NEAR_WARPS;
     int nb = (int)std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 16);
     ProfScope ps(ctx, BEMGPU_K_FILL_NEAR, stream, near_flops, near_bytes);
-    near_pairs_fp64_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
+    if (mode == FILL_DF)
+      near_pairs_kernel<true><<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
+    else
+      near_pairs_kernel<false><<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -786,7 +1015,7 @@ extern "C" int bemgpu_zts(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, co
   if (!ctx || !t || !s || !g || !dZ) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: null argument");
   if (t->geom != s->geom) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: t and s must share one geometry");
   if (ldz < 2 * (int64_t)t->nrwg) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: ldz < 2*size(t)");
-  if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED)
+  if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED && precision != BEMGPU_PREC_MIXED_LA)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "zts: unknown precision %d", precision);
   bemgpu_options_t o;
   if (opt) o = *opt; else bemgpu_options_default(&o);
@@ -894,7 +1123,7 @@ extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree
   if (!pairs.empty()) {
     const int64_t np = (int64_t)pairs.size();
     const int nb = (int)std::min<int64_t>((np + NEAR_WARPS - 1) / NEAR_WARPS, (int64_t)ctx->num_sms * 16);
-    near_pairs_fp64_kernel<<<nb, 32 * NEAR_WARPS, 0, st>>>(t->d_rec, s->d_rec, dnear, np, gd, H, t->nrwg);
+    near_pairs_kernel<false><<<nb, 32 * NEAR_WARPS, 0, st>>>(t->d_rec, s->d_rec, dnear, np, gd, H, t->nrwg);
     ctx->launches++;
   }
   dim3 gblk(128);

@@ -101,7 +101,7 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: size(top) != size(s) + size(t)");
   if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED && precision != BEMGPU_PREC_MIXED_LA)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: unknown precision %d", precision);
-  const int fill_prec = precision == BEMGPU_PREC_MIXED ? BEMGPU_PREC_MIXED : BEMGPU_PREC_FP64;
+  const int fill_prec = precision;  // FP64, FP32 far pairs, or double-float (fill.cu)
   bemgpu_options_t o;
   if (opt) o = *opt; else bemgpu_options_default(&o);
   std::lock_guard<std::mutex> lk(ctx->mu);

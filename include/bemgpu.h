@@ -41,7 +41,9 @@ extern "C" {
 #define BEMGPU_PREC_FP64 0    /* plain path: every stage in FP64 / complex128 */
 #define BEMGPU_PREC_MIXED 1   /* FP32 far pairs (centroid distance > 3 edge lengths), FP64
                                  near/singular; complex64 tensor-core LU + FP64 refinement */
-#define BEMGPU_PREC_MIXED_LA 2 /* FP64 fill, mixed-precision solve as in BEMGPU_PREC_MIXED */
+#define BEMGPU_PREC_MIXED_LA 2 /* FP64-class fill in double-float arithmetic (pairs of FP32,
+                                  ~48 bits, on the FP32 pipes; ~1e-13 of the FP64 fill's row
+                                  scale), mixed-precision solve as in BEMGPU_PREC_MIXED */
 
 typedef struct bemgpu_ctx_s *bemgpu_ctx_t;
 typedef struct bemgpu_geom_s *bemgpu_geom_t;

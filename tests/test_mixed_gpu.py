@@ -24,6 +24,19 @@ def _pair(level, gap, seed=12345):
     return api.parseShapes(b1, b2, d, d)
 
 
+def test_double_float_fill_matches_fp64():
+    """BEMGPU_PREC_MIXED_LA fills every quadrature node pair in double-float
+    (FP32 pairs, ~48 bits) on the FP32 pipes: entries within 1e-11 of their
+    row's scale of the FP64 fill, exterior (lossless) and interior (lossy)
+    media, the two-body tree and a one-body tree; the reference's cube4
+    golden matrix likewise."""
+    top, s, t = _pair(2, 0.05)
+    g = api.GreensFunction(1.0, 1.0, 0.55, True)
+    assert row_scaled_err(api.Zts(top, top, g, precision=_lib.PREC_MIXED_LA), api.Zts(top, top, g)) < 1e-11
+    gi = api.GreensFunction(api.FixedLorentz(*api.SIC_CONFIG).eps(0.1), 1.0, 0.5)
+    assert row_scaled_err(api.Zts(s, s, gi, precision=_lib.PREC_MIXED_LA), api.Zts(s, s, gi)) < 1e-11
+
+
 def test_mixed_fill_close_to_fp64():
     top, s, t = _pair(2, 0.05)
     g = api.GreensFunction(1.0, 1.0, 0.55, True)
