@@ -326,6 +326,165 @@ __device__ __noinline__ void far_pair_df(const TriRec &T, const TriRec &S, const
   far_contract(T, S, g, U0, U1, U2, U3, V0, V1, V2, V3, H, ntr);
 }
 
+// ---------------- far pairs entirely in double-float ----------------
+//
+// Per triangle a double-float record (edge vectors, half-RWG free vertices
+// relative to p0, scaled edge lengths) is built once per fill; the far pair
+// then runs both rules, the outer moments and the closed-form contraction in
+// df, and only widens the nine (c L, c K) products to FP64 for the store.
+struct TriDF {
+  float v01[3][2], v02[3][2];  // df edge vectors of the first half-RWG's frame
+  float e[3][3][2];            // df hp0[i] - p0
+  float hs[3][2];              // df helen[i] / sqrt(4 pi)
+};
+
+__global__ void tri_df_kernel(const TriRec *__restrict__ R, int n, TriDF *__restrict__ D) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const TriRec &T = R[i];
+  TriDF o;
+  const double sc = sqrt(BEM_ONEOVER4PI);
+  for (int c = 0; c < 3; c++) {
+    const df a = df_make(T.v01[c]), b = df_make(T.v02[c]);
+    o.v01[c][0] = a.hi; o.v01[c][1] = a.lo;
+    o.v02[c][0] = b.hi; o.v02[c][1] = b.lo;
+  }
+  for (int h = 0; h < 3; h++) {
+    for (int c = 0; c < 3; c++) {
+      const df e = df_make(h < T.nh ? T.hp0[h][c] - T.p0[c] : 0.0);
+      o.e[h][c][0] = e.hi; o.e[h][c][1] = e.lo;
+    }
+    const df l = df_make(h < T.nh ? T.helen[h] * sc : 0.0);
+    o.hs[h][0] = l.hi; o.hs[h][1] = l.lo;
+  }
+  D[i] = o;
+}
+
+struct cdf {
+  df r, i;
+};
+struct cdf3 {
+  cdf x, y, z;
+};
+__device__ __forceinline__ df3 ld_df3(const float (*v)[2]) { return {{v[0][0], v[0][1]}, {v[1][0], v[1][1]}, {v[2][0], v[2][1]}}; }
+__device__ __forceinline__ df3 df3_add(df3 a, df3 b) { return {df_add(a.x, b.x), df_add(a.y, b.y), df_add(a.z, b.z)}; }
+__device__ __forceinline__ df3 df3_sub(df3 a, df3 b) { return {df_sub(a.x, b.x), df_sub(a.y, b.y), df_sub(a.z, b.z)}; }
+__device__ __forceinline__ df3 df3_scale(df s, df3 a) { return {df_mul(s, a.x), df_mul(s, a.y), df_mul(s, a.z)}; }
+__device__ __forceinline__ df df3_dot(df3 a, df3 b) {
+  return df_add(df_add(df_mul(a.x, b.x), df_mul(a.y, b.y)), df_mul(a.z, b.z));
+}
+__device__ __forceinline__ df3 df3_cross(df3 a, df3 b) {
+  return {df_sub(df_mul(a.y, b.z), df_mul(a.z, b.y)), df_sub(df_mul(a.z, b.x), df_mul(a.x, b.z)),
+          df_sub(df_mul(a.x, b.y), df_mul(a.y, b.x))};
+}
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return {df_add(a.r, b.r), df_add(a.i, b.i)}; }
+__device__ __forceinline__ cdf cdf_sub(cdf a, cdf b) { return {df_sub(a.r, b.r), df_sub(a.i, b.i)}; }
+__device__ __forceinline__ cdf cdf_scale(df s, cdf a) { return {df_mul(s, a.r), df_mul(s, a.i)}; }
+__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
+  return {df_sub(df_mul(a.r, b.r), df_mul(a.i, b.i)), df_add(df_mul(a.r, b.i), df_mul(a.i, b.r))};
+}
+__device__ __forceinline__ cdf3 cdf3_add(cdf3 a, cdf3 b) { return {cdf_add(a.x, b.x), cdf_add(a.y, b.y), cdf_add(a.z, b.z)}; }
+__device__ __forceinline__ cdf3 cdf3_sub(cdf3 a, cdf3 b) { return {cdf_sub(a.x, b.x), cdf_sub(a.y, b.y), cdf_sub(a.z, b.z)}; }
+__device__ __forceinline__ cdf3 cdf_v(cdf c, df3 v) { return {cdf_scale(v.x, c), cdf_scale(v.y, c), cdf_scale(v.z, c)}; }
+__device__ __forceinline__ cdf3 cdf3_scale(df s, cdf3 a) { return {cdf_scale(s, a.x), cdf_scale(s, a.y), cdf_scale(s, a.z)}; }
+__device__ __forceinline__ cdf cdf_rdot(df3 a, cdf3 b) {
+  return cdf_add(cdf_add(cdf_scale(a.x, b.x), cdf_scale(a.y, b.y)), cdf_scale(a.z, b.z));
+}
+// (complex vector) x (real vector)
+__device__ __forceinline__ cdf3 cdf_zcross(cdf3 a, df3 b) {
+  return {cdf_sub(cdf_scale(b.z, a.y), cdf_scale(b.y, a.z)), cdf_sub(cdf_scale(b.x, a.z), cdf_scale(b.z, a.x)),
+          cdf_sub(cdf_scale(b.y, a.x), cdf_scale(b.x, a.y))};
+}
+// (real vector) x (complex vector)
+__device__ __forceinline__ cdf3 cdf_rcross(df3 a, cdf3 b) {
+  return {cdf_sub(cdf_scale(a.y, b.z), cdf_scale(a.z, b.y)), cdf_sub(cdf_scale(a.z, b.x), cdf_scale(a.x, b.z)),
+          cdf_sub(cdf_scale(a.x, b.y), cdf_scale(a.y, b.x))};
+}
+__device__ __forceinline__ cdf3 cdf3_zero() {
+  const df z = {0.f, 0.f};
+  return {{z, z}, {z, z}, {z, z}};
+}
+
+__device__ __noinline__ void far_pair_df2(const TriRec &T, const TriRec &S, const TriDF &TD, const TriDF &SD,
+                                          const GreenDev &g, const float (*rdf)[6], int nr, HalfPairBlock *H,
+                                          int ntr) {
+  const df3 D0 = df3_make(ld3(T.p0) - ld3(S.p0));  // P_t - P_s
+  const df3 v01t = ld_df3(TD.v01), v02t = ld_df3(TD.v02), v01s = ld_df3(SD.v01), v02s = ld_df3(SD.v02);
+  const df ikr = df_make(g.ikr), iki = df_make(g.iki);
+  const df z0 = {0.f, 0.f};
+  cdf U0 = {z0, z0}, U1 = {z0, z0}, V0 = {z0, z0};
+  cdf3 U2 = cdf3_zero(), U3 = cdf3_zero(), V1 = cdf3_zero(), V2 = cdf3_zero(), V3 = cdf3_zero();
+  for (int q = 0; q < nr; q++) {
+    const df a = {rdf[q][0], rdf[q][1]}, b = {rdf[q][2], rdf[q][3]}, w = {rdf[q][4], rdf[q][5]};
+    const df3 rho = df3_add(df3_scale(a, v01t), df3_scale(b, v02t));
+    const df3 rts = df3_add(D0, rho);  // r_t - P_s
+    df I0r = z0, I0i = z0, Q0r = z0, Q0i = z0;
+    df Ar[3] = {z0, z0, z0}, Ai[3] = {z0, z0, z0}, Qr[3] = {z0, z0, z0}, Qi[3] = {z0, z0, z0};
+    for (int u = 0; u < nr; u++) {
+      const df as = {rdf[u][0], rdf[u][1]}, bs = {rdf[u][2], rdf[u][3]}, ws = {rdf[u][4], rdf[u][5]};
+      const df l[3] = {df_add(df_mul(as, v01s.x), df_mul(bs, v02s.x)), df_add(df_mul(as, v01s.y), df_mul(bs, v02s.y)),
+                       df_add(df_mul(as, v01s.z), df_mul(bs, v02s.z))};
+      const df xx = df_sub(rts.x, l[0]), xy = df_sub(rts.y, l[1]), xz = df_sub(rts.z, l[2]);
+      const df R2 = df_add(df_add(df_sqr(xx), df_sqr(xy)), df_sqr(xz));
+      const df R = df_sqrt(R2);
+      const df Ri = df_rcp(R);
+      df er, ei;
+      df_exp_ikR(g, ikr, iki, R, er, ei);
+      const df gr = df_mul(er, Ri), gi = df_mul(ei, Ri);
+      const df zr = df_mul(ikr, R), zi = df_mul(iki, R);
+      const df mr = df_add_f(df_neg(zr), 1.f), mi = df_neg(zi);
+      const df Ri2 = df_sqr(Ri);
+      const df qr = df_mul(df_sub(df_mul(gr, mr), df_mul(gi, mi)), Ri2);
+      const df qi = df_mul(df_add(df_mul(gr, mi), df_mul(gi, mr)), Ri2);
+      const df gwr = df_mul(ws, gr), gwi = df_mul(ws, gi), qwr = df_mul(ws, qr), qwi = df_mul(ws, qi);
+      I0r = df_add(I0r, gwr);
+      I0i = df_add(I0i, gwi);
+      Q0r = df_add(Q0r, qwr);
+      Q0i = df_add(Q0i, qwi);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        Ar[c] = df_add(Ar[c], df_mul(gwr, l[c]));
+        Ai[c] = df_add(Ai[c], df_mul(gwi, l[c]));
+        Qr[c] = df_add(Qr[c], df_mul(qwr, l[c]));
+        Qi[c] = df_add(Qi[c], df_mul(qwi, l[c]));
+      }
+    }
+    const cdf I0 = {I0r, I0i}, Q0 = {Q0r, Q0i};
+    const cdf3 A = {{Ar[0], Ai[0]}, {Ar[1], Ai[1]}, {Ar[2], Ai[2]}};
+    const cdf3 Q1 = {{Qr[0], Qi[0]}, {Qr[1], Qi[1]}, {Qr[2], Qi[2]}};
+    const cdf wI0 = cdf_scale(w, I0), wQ0 = cdf_scale(w, Q0);
+    U0 = cdf_add(U0, wI0);
+    U1 = cdf_add(U1, cdf_scale(w, cdf_rdot(rho, A)));
+    U2 = cdf3_add(U2, cdf_v(wI0, rho));
+    U3 = cdf3_add(U3, cdf3_scale(w, A));
+    V0 = cdf_add(V0, wQ0);
+    V1 = cdf3_add(V1, cdf3_scale(w, cdf_zcross(Q1, rho)));
+    V2 = cdf3_add(V2, cdf3_scale(w, Q1));
+    V3 = cdf3_add(V3, cdf_v(wQ0, rho));
+  }
+  // the closed form of far_pair(), in df
+  const cdf ksq = {df_make(g.ksqr), df_make(g.ksqi)};
+  const df quarter = {0.25f, 0.f};
+  for (int i = 0; i < T.nh; i++) {
+    const df3 ei = ld_df3(TD.e[i]);
+    for (int j = 0; j < S.nh; j++) {
+      const df3 dj = ld_df3(SD.e[j]);
+      const df3 D = df3_sub(df3_add(D0, ei), dj);  // p0_i - p0_j
+      cdf br = cdf_sub(cdf_sub(U1, cdf_rdot(dj, U2)), cdf_rdot(ei, U3));
+      br = cdf_add(br, cdf_scale(df3_dot(ei, dj), U0));
+      const cdf L = cdf_sub(cdf_scale(quarter, cdf_mul(ksq, br)), U0);
+      cdf3 X = cdf3_sub(cdf3_sub(V1, cdf_zcross(V2, ei)), cdf_rcross(dj, V3));
+      X = cdf3_add(X, cdf_v(V0, df3_cross(dj, ei)));
+      const cdf K = cdf_scale(df_neg(quarter), cdf_rdot(D, X));
+      df c = df_mul({TD.hs[i][0], TD.hs[i][1]}, {SD.hs[j][0], SD.hs[j][1]});
+      if (T.hneg[i] != S.hneg[j]) c = df_neg(c);
+      const cdf cL = cdf_scale(c, L), cK = cdf_scale(c, K);
+      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], z1{df_to_double(cL.r), df_to_double(cL.i)},
+                  z1{df_to_double(cK.r), df_to_double(cK.i)});
+    }
+  }
+}
+
 // ---------------- far pairs in FP32 (mixed precision) ----------------
 //
 // Same closed form as far_pair(), evaluated in FP32 with a pair-centred
@@ -449,7 +608,8 @@ __device__ __noinline__ void far_pair_fp32(const TriRec &T, const TriRec &S, con
 // of the two triangles' longest edges) are integrated in FP32.
 __global__ void __launch_bounds__(128) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
                                                         const TriRec *__restrict__ Sr, int ntS, GreenDev g,
-                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mode) {
+                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mode,
+                                                        const TriDF *__restrict__ TDr, const TriDF *__restrict__ SDr) {
   const int sb = blockIdx.x * blockDim.x + threadIdx.x;
   const int ta = blockIdx.y * blockDim.y + threadIdx.y;
   if (sb >= ntS || ta >= ntT) return;
@@ -461,11 +621,12 @@ __global__ void __launch_bounds__(128) far_pairs_kernel(const TriRec *__restrict
   const double e = fmax(T.emax, S.emax);
   const double emax2 = __dmul_rn(e, e);
   if (mode == FILL_DF) {
-    if (__dmul_rn(d, o.th6) > emax2) far_pair_df(T, S, g, c_rule6, c_rdf6, 6, H, ntr);
-    else if (__dmul_rn(d, o.th10) > emax2) far_pair_df(T, S, g, c_rule10, c_rdf10, 10, H, ntr);
-    else if (__dmul_rn(d, o.th15) > emax2) far_pair_df(T, S, g, c_rule15, c_rdf15, 15, H, ntr);
-    else if (__dmul_rn(d, o.th21) > emax2) far_pair_df(T, S, g, c_rule21, c_rdf21, 21, H, ntr);
-    else far_pair_df(T, S, g, c_rule36, c_rdf36, 36, H, ntr);
+    const TriDF &TD = TDr[ta], &SD = SDr[sb];
+    if (__dmul_rn(d, o.th6) > emax2) far_pair_df2(T, S, TD, SD, g, c_rdf6, 6, H, ntr);
+    else if (__dmul_rn(d, o.th10) > emax2) far_pair_df2(T, S, TD, SD, g, c_rdf10, 10, H, ntr);
+    else if (__dmul_rn(d, o.th15) > emax2) far_pair_df2(T, S, TD, SD, g, c_rdf15, 15, H, ntr);
+    else if (__dmul_rn(d, o.th21) > emax2) far_pair_df2(T, S, TD, SD, g, c_rdf21, 21, H, ntr);
+    else far_pair_df2(T, S, TD, SD, g, c_rdf36, 36, H, ntr);
     return;
   }
   if (mode == FILL_FP32_FAR && d > 9.0 * emax2) {
@@ -964,7 +1125,17 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
   }
   {
     ProfScope ps(ctx, BEMGPU_K_FILL_FAR, stream, far_flops, far_bytes);
-    far_pairs_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, mode);
+    TriDF *tdf = nullptr, *sdf = nullptr;
+    if (mode == FILL_DF) {
+      tdf = (TriDF *)bem_workspace(ctx, "fill_tdf", sizeof(TriDF) * (size_t)t->ntri);
+      sdf = (TriDF *)bem_workspace(ctx, "fill_sdf", sizeof(TriDF) * (size_t)s->ntri);
+      if (!tdf || !sdf) return bem_fail(ctx, BEMGPU_ERR_OOM, "fill: double-float records");
+      tri_df_kernel<<<(t->ntri + 127) / 128, 128, 0, stream>>>(t->d_rec, t->ntri, tdf);
+      tri_df_kernel<<<(s->ntri + 127) / 128, 128, 0, stream>>>(s->d_rec, s->ntri, sdf);
+      ctx->launches += 2;
+    }
+    far_pairs_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, mode, tdf,
+                                              sdf);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -1118,7 +1289,8 @@ extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree
   const FarOpts fo = {o.farThresh6, o.farThresh10, o.farThresh15, o.farThresh21};
   dim3 blk(32, 4);
   dim3 grd((s->ntri + 31) / 32, (t->ntri + 3) / 4);
-  far_pairs_kernel<<<grd, blk, 0, st>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, 0);
+  far_pairs_kernel<<<grd, blk, 0, st>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, FILL_FP64, nullptr,
+                                        nullptr);
   ctx->launches++;
   if (!pairs.empty()) {
     const int64_t np = (int64_t)pairs.size();
