@@ -236,71 +236,78 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 
 namespace {
 
-__device__ __forceinline__ double pow2d(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
-
-// Largest max(|re|, |im|) of a complex128 matrix (m x k, column-major) as the
-// bits of a non-negative double (ordered like the value) -> *out (atomicMax).
-__global__ void ex_absmax_kernel(const double *__restrict__ A, int64_t lda, int m, int k,
-                                 unsigned long long *out) {
-  double mx = 0.0;
+// Largest FP64 exponent field of max(|re|, |im|) over a complex128 matrix
+// (m x k, column-major) -> *out (atomicMax).
+__global__ void ex_absmax_kernel(const double *__restrict__ A, int64_t lda, int m, int k, unsigned *out) {
+  unsigned mx = 0;
   const int64_t total = (int64_t)m * k;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = i / m, r = i - c * m;
-    const double2 v = reinterpret_cast<const double2 *>(A)[r + lda * c];
-    mx = fmax(mx, fmax(fabs(v.x), fabs(v.y)));
+    const longlong2 v = reinterpret_cast<const longlong2 *>(A)[r + lda * c];
+    mx = max(mx, (unsigned)max((v.x >> 52) & 0x7ff, (v.y >> 52) & 0x7ff));
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0 && mx > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if ((threadIdx.x & 31) == 0 && mx > 0) atomicMax(out, mx);
 }
 
-// Scaling exponent of the matrix whose largest magnitude has bits *amax: the
-// power of two bringing it just below 2^EX_SCALE_TARGET (0 for a zero matrix).
-__device__ __forceinline__ int ex_matrix_shift(const unsigned long long *amax) {
-  const unsigned long long bits = *amax;
-  if (bits == 0) return 0;
-  const int eb = (int)((bits >> 52) & 0x7ff);  // value in [2^(eb-1023), 2^(eb-1022))
-  if (eb == 0) return EX_SCALE_TARGET + 1022;  // subnormal maximum
-  return EX_SCALE_TARGET - (eb - 1022);
+// Scaling exponent g of the matrix whose largest exponent field is *amax:
+// values times 2^g stay below 2^EX_SCALE_TARGET (0 for a zero matrix).
+__device__ __forceinline__ int ex_matrix_shift(const unsigned *amax) {
+  const int eb = (int)*amax;  // largest magnitude in [2^(eb-1023), 2^(eb-1022))
+  return eb == 0 ? 0 : EX_SCALE_TARGET - (eb - 1022);
 }
 
-// Block exponent E (block max < 2^E) of a scaled block maximum; flush marker
-// when the block is zero or below 2^EX_FLUSH_E.
 constexpr int EX_ZERO = -100000;
-__device__ __forceinline__ int ex_block_exponent(double mx) {
-  if (!(mx > 0.0)) return EX_ZERO;
-  const int eb = (int)((__double_as_longlong(mx) >> 52) & 0x7ff);
-  const int E = eb - 1022;
-  return (eb == 0 || E < EX_FLUSH_E) ? EX_ZERO : E;
-}
 
+__device__ __forceinline__ int fp64_expfield(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // e in [-126, 127]
+
+// Block fixed point by integer arithmetic on the FP64 fields: with x 2^g = M
+// 2^(eb + g - 1075) and the block exponent E, N = round(x 2^(g + 8 SL - E))
+// (|N| <= 2^(8 SL)), written in balanced base-256 digits q_0..q_{SL-1}
+// (|q_0| <= 256, |q_l| <= 128); slice l holds q_l 2^(E - 8(l+1)) as bf16
+// (exact: at most 8 significant bits).  FP64 subnormals count as zero.
 template <int SL>
-__device__ __forceinline__ void ex_split(double x, int E, __nv_bfloat16 *s) {
-  if (E == EX_ZERO) {
-#pragma unroll
-    for (int l = 0; l < SL; l++) s[l] = __float2bfloat16_rn(0.f);
-    return;
+__device__ __forceinline__ void ex_split(double x, int g, int E, __nv_bfloat16 *s) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int eb = (int)((bits >> 52) & 0x7ff);
+  long long N = 0;
+  if (E != EX_ZERO && eb != 0) {
+    const long long mant = (long long)((bits & ((1ull << 52) - 1)) | (1ull << 52));
+    const int rs = -(eb + g - 1075 + 8 * SL - E);  // >= 13 since |x 2^g| < 2^E
+    if (rs < 55) N = (mant + (1ll << (rs - 1))) >> rs;
+    if (bits >> 63) N = -N;
   }
-  double rem = x;
+  int q[SL];
 #pragma unroll
-  for (int l = 0; l < SL; l++) {
-    const int e = E - 8 * (l + 1);
-    const double v = rint(rem * pow2d(-e)) * pow2d(e);
-    rem -= v;  // exact
-    s[l] = __float2bfloat16_rn((float)v);  // exact: <= 9 significant bits, exponent >= -120
+  for (int l = SL - 1; l >= 1; l--) {
+    int d = (int)(N & 255);
+    if (d >= 128) d -= 256;
+    q[l] = d;
+    N = (N - d) >> 8;
   }
+  q[0] = (int)N;
+#pragma unroll
+  for (int l = 0; l < SL; l++)
+    s[l] = __float2bfloat16_rn(E == EX_ZERO ? 0.f : (float)q[l] * pow2f(E - 8 * (l + 1)));
 }
 
 // Maximum over the 64 consecutive threads (two warps) holding one exponent
 // block; the CTA is 128 threads and every thread calls it.
-__device__ __forceinline__ double block64_max(double v) {
-  __shared__ double wm[4];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+__device__ __forceinline__ unsigned block64_max(unsigned v) {
+  __shared__ unsigned wm[4];
+  v = __reduce_max_sync(0xffffffffu, v);
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) wm[w] = v;
   __syncthreads();
-  return fmax(wm[w & ~1], wm[w | 1]);
+  return max(wm[w & ~1], wm[w | 1]);
+}
+
+// Block exponent E (block max of x 2^g below 2^E) from the block's largest
+// exponent field; flush marker for zero blocks and blocks below 2^EX_FLUSH_E.
+__device__ __forceinline__ int ex_block_exponent(unsigned ebmax, int g) {
+  const int E = (int)ebmax + g - 1022;
+  return (ebmax == 0 || E < EX_FLUSH_E) ? EX_ZERO : E;
 }
 
 // A' slices (Mp x Kp) of sign * A (complex128, m x k, column-major), block
@@ -309,7 +316,7 @@ __device__ __forceinline__ double block64_max(double v) {
 // matrix's scaling exponent in *shift.
 template <int SL>
 __global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int m, int k, double sign,
-                                 const unsigned long long *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Mp,
+                                 const unsigned *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Mp,
                                  int64_t Kp) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int r = blockIdx.y;
@@ -319,14 +326,14 @@ __global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int 
   double ar = 0.0, ai = 0.0;
   if (active && r < m && q < k) {
     const double2 v = reinterpret_cast<const double2 *>(A)[r + lda * (int64_t)q];
-    ar = sign * v.x * pow2d(g);
-    ai = sign * v.y * pow2d(g);
+    ar = sign * v.x;
+    ai = sign * v.y;
   }
-  const int E = ex_block_exponent(block64_max(fmax(fabs(ar), fabs(ai))));
+  const int E = ex_block_exponent(block64_max((unsigned)max(fp64_expfield(ar), fp64_expfield(ai))), g);
   if (!active) return;
   __nv_bfloat16 sr[SL], si[SL], sn[SL];
-  ex_split<SL>(ar, E, sr);
-  ex_split<SL>(ai, E, si);
+  ex_split<SL>(ar, g, E, sr);
+  ex_split<SL>(ai, g, E, si);
 #pragma unroll
   for (int l = 0; l < SL; l++) sn[l] = __hneg(si[l]);
   const int64_t plane = Mp * Kp;
@@ -342,7 +349,7 @@ __global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int 
 // complex rows (two warps).
 template <int SL>
 __global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int k, int n,
-                                 const unsigned long long *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Np,
+                                 const unsigned *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Np,
                                  int64_t Kp) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
@@ -352,14 +359,14 @@ __global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int 
   double br = 0.0, bi = 0.0;
   if (active && c < n && q < k) {
     const double2 v = reinterpret_cast<const double2 *>(B)[q + ldb * (int64_t)c];
-    br = v.x * pow2d(g);
-    bi = v.y * pow2d(g);
+    br = v.x;
+    bi = v.y;
   }
-  const int E = ex_block_exponent(block64_max(fmax(fabs(br), fabs(bi))));
+  const int E = ex_block_exponent(block64_max((unsigned)max(fp64_expfield(br), fp64_expfield(bi))), g);
   if (!active) return;
   __nv_bfloat16 sr[SL], si[SL];
-  ex_split<SL>(br, E, sr);
-  ex_split<SL>(bi, E, si);
+  ex_split<SL>(br, g, E, sr);
+  ex_split<SL>(bi, g, E, si);
   const int64_t plane = Np * Kp, i0 = (int64_t)c * Kp + 2 * q;
 #pragma unroll
   for (int l = 0; l < SL; l++)
@@ -397,10 +404,10 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
   op.kp = kp;
   op.slices = slices;
   op.is_a = is_a;
-  unsigned long long *amax = reinterpret_cast<unsigned long long *>(op.aux + 8);
+  unsigned *amax = reinterpret_cast<unsigned *>(op.aux + 8);
   {
     ProfScope ps(ctx, BEMGPU_K_SLICE, st, 0.0, 16.0 * (double)rows * k * 2 + 4.0 * slices * (double)rp * kp);
-    BEM_CUDA_TRY(ctx, cudaMemsetAsync(amax, 0, sizeof(unsigned long long), st));
+    BEM_CUDA_TRY(ctx, cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
     ex_absmax_kernel<<<2 * 152, 256, 0, st>>>(M, ld, is_a ? rows : k, is_a ? k : rows, amax);
     ctx->launches++;
     const dim3 grid((unsigned)((kp / 2 + 127) / 128), (unsigned)(is_a ? rp / 2 : rp));
