@@ -189,8 +189,11 @@ int bem_cgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const 
               cudaStream_t stream);
 // Tensor-core complex64 GEMM: C (+)= sign * A B (A m x k, B k x n, column-major).
 enum { TC_OUT_F32 = 0, TC_OUT_F64 = 1, TC_OUT_F64_COMP = 2 };
+// tri: 0 general A, 1 lower-triangular A, 2 upper-triangular A (complex, square
+// m = k; the zero triangle is skipped, F32 and F64 outputs only).
 int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, const float *A, int64_t lda,
-                 const float *B, int64_t ldb, void *C, int64_t ldc, int out, int accumulate, cudaStream_t st);
+                 const float *B, int64_t ldb, void *C, int64_t ldc, int out, int accumulate, cudaStream_t st,
+                 int tri = 0);
 // The same product on the FP32 FMA pipes (any alpha, beta).
 int bem_cgemm_comp64_fma(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const float alpha[2], const float *A,
                          int64_t lda, const float *B, int64_t ldb, const double beta[2], double *C, int64_t ldc,

@@ -1006,6 +1006,11 @@ int bem_capply_inverse(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, 
     laswp_kernel<float><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, 0, nrhs, 0, n, d_ipiv);
     ctx->launches++;
   }
+  if (ctx->gemm_engine != 2 && n >= 64 && nrhs >= 64) {  // tensor cores, zero triangles skipped
+    int rc = bem_cgemm_tc(ctx, BEMGPU_K_SOLVE_GEMM, n, nrhs, n, 1.f, Linv, n, B, ldb, tmp, n, TC_OUT_F32, 0, st, 1);
+    if (!rc) rc = bem_cgemm_tc(ctx, BEMGPU_K_SOLVE_GEMM, n, nrhs, n, 1.f, Uinv, n, tmp, n, B, ldb, TC_OUT_F32, 0, st, 2);
+    return rc;
+  }
   const float one[2] = {1.f, 0.f}, zero[2] = {0.f, 0.f};
   int rc = bem_cgemm(ctx, BEMGPU_K_SOLVE_GEMM, 'N', n, nrhs, n, one, Linv, n, B, ldb, zero, tmp, n, st);
   if (!rc) rc = bem_cgemm(ctx, BEMGPU_K_SOLVE_GEMM, 'N', n, nrhs, n, one, Uinv, n, tmp, n, zero, B, ldb, st);

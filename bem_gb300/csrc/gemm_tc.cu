@@ -57,7 +57,7 @@ namespace {
 template <typename TOUT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ TcMaps maps, int ktiles, TOUT *__restrict__ C, int64_t ldcf, int mvalid,
-                   int nvalid, int accumulate, int *err) {
+                   int nvalid, int accumulate, int tri, int *err) {
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) &
                                                           ~(uintptr_t)1023);
@@ -88,12 +88,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
+  // K range: all of it, or for a triangular complex A only the K steps that
+  // meet nonzero entries of this tile's rows (lower: columns <= row, upper:
+  // columns >= row; realified row rho and column kappa belong to complex
+  // row rho / 2 and column kappa / 2).
+  const int kb = tri == 2 ? m0 / TC_BK : 0;
+  const int ke = tri == 1 ? min(ktiles, (m0 + TC_BM + TC_BK - 1) / TC_BK) : ktiles;
+  const int nk = max(0, ke - kb);
   if (warp == 0) {
     if (lane == 0) {
       int issued = 0;
-      for (int kt = 0; kt < ktiles; kt++) {
-        const int s = kt % TC_STAGES, round = kt / TC_STAGES;
-        if (kt >= TC_STAGES && !mbar_wait(&empty[s], (round - 1) & 1, err)) break;
+      for (int j = 0; j < nk; j++) {
+        const int kt = kb + j, s = j % TC_STAGES, round = j / TC_STAGES;
+        if (j >= TC_STAGES && !mbar_wait(&empty[s], (round - 1) & 1, err)) break;
         mbar_expect_tx(&full[s], TC_STAGE_BYTES);
         unsigned char *st = smem + s * TC_STAGE_BYTES;
 #pragma unroll
@@ -101,7 +108,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int b = 0; b < TC_SLICES; b++)
           tma_load_2d(st + (TC_SLICES + b) * TC_TILE_BYTES, &maps.b[b], kt * TC_BK, n0, &full[s]);
-        issued = kt + 1;
+        issued = j + 1;
       }
       drain_copies(full, issued, err);
     }
@@ -109,8 +116,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
       bool ok = true;
-      for (int kt = 0; kt < ktiles && ok; kt++) {
-        const int s = kt % TC_STAGES, round = kt / TC_STAGES;
+      for (int j = 0; j < nk && ok; j++) {
+        const int s = j % TC_STAGES, round = j / TC_STAGES;
         ok = mbar_wait(&full[s], round & 1, err);
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
@@ -121,7 +128,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           for (int p = 0; p < 6; p++) {
             const uint64_t da = smem_desc_sw128(st + c_prod_a[p] * TC_TILE_BYTES + ks * 32);
             const uint64_t db = smem_desc_sw128(st + (TC_SLICES + c_prod_b[p]) * TC_TILE_BYTES + ks * 32);
-            tc_mma(tmem, da, db, idesc, (kt | ks | p) != 0 ? 1u : 0u);
+            tc_mma(tmem, da, db, idesc, (j | ks | p) != 0 ? 1u : 0u);
           }
         }
         tc_commit(&empty[s]);
@@ -139,6 +146,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int c0 = 0; c0 < TC_BN; c0 += 32) {
       float v[32];
       tc_ld32(tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)c0, v);
+      if (nk == 0) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = 0.f;
+      }
       if (ok && rho < mvalid) {
 #pragma unroll
         for (int j = 0; j < 32; j++) {
@@ -451,7 +462,8 @@ int bem_tc_error(bemgpu_ctx_s *ctx, bool reset) {
 // TC_OUT_F64 (complex128 C, FP32 accumulation), TC_OUT_F64_COMP (complex128
 // C, per-K-step FP32 sums accumulated as two-float sums).  Column-major, ldc.
 int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, const float *A, int64_t lda,
-                 const float *B, int64_t ldb, void *C, int64_t ldc, int out, int accumulate, cudaStream_t st) {
+                 const float *B, int64_t ldb, void *C, int64_t ldc, int out, int accumulate, cudaStream_t st,
+                 int tri) {
   if (m <= 0 || n <= 0) return BEMGPU_OK;
   if (k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "cgemm_tc: k = %d", k);
   const int64_t Mp = ((2 * (int64_t)m + TC_BM - 1) / TC_BM) * TC_BM;
@@ -502,10 +514,10 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
                                                                     accumulate, err);
     else if (out == TC_OUT_F64)
       tc_gemm_kernel<double><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(maps, kt, (double *)C, 2 * ldc, 2 * m, n,
-                                                                      accumulate, err);
+                                                                      accumulate, tri, err);
     else
       tc_gemm_kernel<float><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(maps, kt, (float *)C, 2 * ldc, 2 * m, n,
-                                                                     accumulate, err);
+                                                                     accumulate, tri, err);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
