@@ -144,6 +144,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int rho = m0 + sub * 32 + lane;
 #pragma unroll 1
     for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+      // the chunk's old C values first, all loads in flight together
+      TOUT old[32];
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const int c = n0 + c0 + j;
+        old[j] = (accumulate && ok && rho < mvalid && c < nvalid) ? C[rho + ldcf * (int64_t)c] : (TOUT)0;
+      }
       float v[32];
       tc_ld32(tmem + ((uint32_t)(sub * 32) << 16) + (uint32_t)c0, v);
       if (nk == 0) {
@@ -154,10 +161,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
         for (int j = 0; j < 32; j++) {
           const int c = n0 + c0 + j;
-          if (c < nvalid) {
-            TOUT *p = C + rho + ldcf * (int64_t)c;
-            *p = accumulate ? (TOUT)(*p + (TOUT)v[j]) : (TOUT)v[j];
-          }
+          if (c < nvalid) C[rho + ldcf * (int64_t)c] = old[j] + (TOUT)v[j];
         }
       }
     }
@@ -524,10 +528,9 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
   return BEMGPU_OK;
 }
 
-// The tensor-core kernels keep one 128-wide tile per SM and stream C once, so
-// they pay off from a few K steps on; rank-64 updates (LU, triangular
-// solves) run faster on the FMA pipes.
-constexpr int TC_MIN_K = 256;
+// Below 64 (complex) K the FMA pipes win; from rank-64 updates on (the LU
+// trailing matrix: 66 TF/s vs 28 at 7680^2 x 64) the tensor cores do.
+constexpr int TC_MIN_K = 64;
 
 static bool tc_usable(int engine, int m, int n, int k) {
   return engine != 2 && (engine == 1 || k >= TC_MIN_K) && m >= 64 && n >= 64 && k >= 16 && 2 * (int64_t)m <= 2 * 65535 &&
