@@ -200,6 +200,10 @@ __global__ void laswp_kernel(T *A, int64_t lda, int c0, int c1, int k1, int k2, 
 constexpr int COOP_THREADS = 256;
 constexpr unsigned COOP_SPIN_LIMIT = 1u << 24;
 
+__device__ __forceinline__ void arrive_release_u32(unsigned *p) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(p) : "memory");
+}
+
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -277,8 +281,9 @@ __global__ void __launch_bounds__(COOP_THREADS)
     __syncthreads();
     // (2) grid barrier
     if (tid == 0) {
-      __threadfence();
-      atomicAdd(counter, 1u);
+      // the CTA's publishing writes (ordered before by the bar.sync above) are
+      // released with the arrival; the acquire load orders the reads below
+      arrive_release_u32(counter);
       const unsigned target = (unsigned)G * (unsigned)(j + 1);
       unsigned it = 0;
       while (ld_acquire_u32(counter) < target) {
@@ -288,7 +293,6 @@ __global__ void __launch_bounds__(COOP_THREADS)
           break;
         }
       }
-      __threadfence();
     }
     __syncthreads();
     if (s_abort) return;
