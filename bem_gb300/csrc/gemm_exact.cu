@@ -132,14 +132,16 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         if (opening && dt >= 2 && !mbar_wait(&acce[b], (use - 1) & 1, err)) break;
         if (!mbar_wait(&full[s], round & 1, err)) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t st = smem_u32(smem + s * STAGE);
+        // descriptors: one per stage, the tiles and K steps as compile-time
+        // offsets added to its address field (which never carries: smem < 256 KB)
+        const uint64_t dbase = smem_desc_sw64(smem_u32(smem + s * STAGE));
 #pragma unroll
         for (int ks = 0; ks < EX_BK / 16; ks++) {
 #pragma unroll
           for (int p = 0; p < NP; p++) {
             const int level = ex_level(p), a = p - ex_first(level), bb = level - a;
-            const uint64_t da = smem_desc_sw64(st + a * EX_A_TILE + ks * 32);
-            const uint64_t db = smem_desc_sw64(st + SL * EX_A_TILE + bb * EX_B_TILE + ks * 32);
+            const uint64_t da = dbase + (uint64_t)((a * EX_A_TILE + ks * 32) >> 4);
+            const uint64_t db = dbase + (uint64_t)((SL * EX_A_TILE + bb * EX_B_TILE + ks * 32) >> 4);
             const bool first = opening && ks == 0 && p == ex_first(level);
             if (level <= 2)
               tc_mma(tmem + (uint32_t)((3 * b + level) * EX_BN), da, db, idesc, first ? 0u : 1u);

@@ -33,9 +33,11 @@ constexpr int TC_STAGE_BYTES = 2 * TC_SLICES * TC_TILE_BYTES;  // 96 KB
 constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 192;
 
-// products (a, b) with a + b <= 2 (0-based slice indices)
-__constant__ int c_prod_a[6] = {0, 0, 1, 0, 1, 2};
-__constant__ int c_prod_b[6] = {0, 1, 0, 2, 1, 0};
+// products (a, b) with a + b <= 2 (0-based slice indices), level-major:
+// (0,0) (0,1) (1,0) (0,2) (1,1) (2,0)
+__host__ __device__ constexpr int tc_level(int p) { return p < 1 ? 0 : p < 3 ? 1 : 2; }
+__host__ __device__ constexpr int tc_prod_a(int p) { return p - tc_level(p) * (tc_level(p) + 1) / 2; }
+__host__ __device__ constexpr int tc_prod_b(int p) { return tc_level(p) - tc_prod_a(p); }
 
 __device__ __forceinline__ void drain_copies(uint64_t *full, int issued, int *err) {
   for (int kt = issued > TC_STAGES ? issued - TC_STAGES : 0; kt < issued; kt++)
@@ -121,13 +123,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         ok = mbar_wait(&full[s], round & 1, err);
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t st = smem_u32(smem + s * TC_STAGE_BYTES);
+        const uint64_t dbase = smem_desc_sw128(smem_u32(smem + s * TC_STAGE_BYTES));
 #pragma unroll
         for (int ks = 0; ks < TC_BK / 16; ks++) {
 #pragma unroll
           for (int p = 0; p < 6; p++) {
-            const uint64_t da = smem_desc_sw128(st + c_prod_a[p] * TC_TILE_BYTES + ks * 32);
-            const uint64_t db = smem_desc_sw128(st + (TC_SLICES + c_prod_b[p]) * TC_TILE_BYTES + ks * 32);
+            const uint64_t da = dbase + (uint64_t)((tc_prod_a(p) * TC_TILE_BYTES + ks * 32) >> 4);
+            const uint64_t db = dbase + (uint64_t)(((TC_SLICES + tc_prod_b(p)) * TC_TILE_BYTES + ks * 32) >> 4);
             tc_mma(tmem, da, db, idesc, (j | ks | p) != 0 ? 1u : 0u);
           }
         }
@@ -269,9 +271,9 @@ __global__ void __launch_bounds__(TCC_THREADS, 1)
         for (int ks = 0; ks < TC_BK / 16; ks++) {
 #pragma unroll
           for (int p = 0; p < 6; p++) {
-            const uint64_t da = smem_desc_sw128(st + c_prod_a[p] * TC_TILE_BYTES + ks * 32);
+            const uint64_t da = smem_desc_sw128(st + tc_prod_a(p) * TC_TILE_BYTES + ks * 32);
             const uint64_t db =
-                smem_desc_sw128(st + TC_SLICES * TC_TILE_BYTES + c_prod_b[p] * TCC_B_TILE_BYTES + ks * 32);
+                smem_desc_sw128(st + TC_SLICES * TC_TILE_BYTES + tc_prod_b(p) * TCC_B_TILE_BYTES + ks * 32);
             const int level = p == 0 ? 0 : (p < 3 ? 1 : 2);
             const int first = p == 0 ? 0 : (p < 3 ? 1 : 3);  // first product of its level
             tc_mma(tx + (uint32_t)(level * TCC_BN), da, db, idesc, (ks != 0 || p != first) ? 1u : 0u);
