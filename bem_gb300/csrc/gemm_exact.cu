@@ -390,7 +390,7 @@ bool bem_exact_available() { return encode_fn() != nullptr; }
 
 int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
                    double sign, int slices, ExactOperand &op, cudaStream_t st) {
-  if (slices != 4 && slices != 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
+  if (slices < 3 || slices > 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
   if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
                           : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
@@ -417,13 +417,17 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
     if (is_a) {
       if (slices == 5)
         ex_prep_a_kernel<5><<<grid, 128, 0, st>>>(M, ld, rows, k, sign, amax, op.aux, S, rp, kp);
-      else
+      else if (slices == 4)
         ex_prep_a_kernel<4><<<grid, 128, 0, st>>>(M, ld, rows, k, sign, amax, op.aux, S, rp, kp);
+      else
+        ex_prep_a_kernel<3><<<grid, 128, 0, st>>>(M, ld, rows, k, sign, amax, op.aux, S, rp, kp);
     } else {
       if (slices == 5)
         ex_prep_b_kernel<5><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
-      else
+      else if (slices == 4)
         ex_prep_b_kernel<4><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
+      else
+        ex_prep_b_kernel<3><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
     }
     ctx->launches++;
   }
@@ -433,9 +437,11 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
 
 int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const ExactOperand &b, double *C, int64_t ldc,
                    int accumulate, cudaStream_t st) {
-  if (!a.is_a || b.is_a || a.k != b.k || a.kp != b.kp || a.slices != b.slices)
+  // SL = the slices of B; A may carry more (its leading SL slices are used:
+  // products of levels < SL, error ~2^(-8 SL) of the blocks' maxima)
+  if (!a.is_a || b.is_a || a.k != b.k || a.kp != b.kp || a.slices < b.slices)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: operands do not match");
-  const int m = a.rows, n = b.rows, SL = a.slices;
+  const int m = a.rows, n = b.rows, SL = b.slices;
   ExMaps maps;
   if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SL, a.rows_p, a.kp, EX_BM) ||
       !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SL, b.rows_p, b.kp, EX_BN))
@@ -447,6 +453,8 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
                                            ex_smem_bytes<5>()));
     BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            ex_smem_bytes<4>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<3>()));
     ctx->ex_ready = true;
   }
   if (!ctx->tc_err_ready) {
@@ -468,8 +476,11 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   if (SL == 5)
     ex_gemm_kernel<5><<<grid, EX_THREADS, ex_smem_bytes<5>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
                                                                     shifts, err);
-  else
+  else if (SL == 4)
     ex_gemm_kernel<4><<<grid, EX_THREADS, ex_smem_bytes<4>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
+                                                                    shifts, err);
+  else
+    ex_gemm_kernel<3><<<grid, EX_THREADS, ex_smem_bytes<3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
                                                                     shifts, err);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());

@@ -31,6 +31,8 @@
 namespace {
 
 constexpr int MIXED_SLICES = 5;  // block fixed-point slices of the refinement and trace products
+constexpr int DELTA_SLICES = 3;  // slices of a correction (~1e-4 of the iterate): its products carry
+                                 // 2^-24 of their own size, far below 2^-41 of the whole
 
 __global__ void c128_to_c64_kernel(const double *__restrict__ S, int64_t lds, float *__restrict__ D, int64_t ldd, int m,
                                    int n) {
@@ -110,8 +112,9 @@ __global__ void sym64_kernel(const double *__restrict__ G, int64_t ld, int m, do
   reinterpret_cast<double2 *>(H)[i + (int64_t)m * j] = make_double2(a.x + b.x, a.y - b.y);
 }
 
-// Y64 (+)= widen(D32).
-__global__ void update_kernel(double *__restrict__ Y, const float *__restrict__ D, int64_t ld, int n, int accumulate) {
+// Y64 (+)= widen(D32); dY64 = widen(D32) when dY is given.
+__global__ void update_kernel(double *__restrict__ Y, const float *__restrict__ D, int64_t ld, int n, int accumulate,
+                              double *__restrict__ dY) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (r >= n) return;
@@ -121,6 +124,7 @@ __global__ void update_kernel(double *__restrict__ Y, const float *__restrict__ 
   y.x += (double)d.x;
   y.y += (double)d.y;
   reinterpret_cast<double2 *>(Y)[idx] = y;
+  if (dY) reinterpret_cast<double2 *>(dY)[idx] = make_double2((double)d.x, (double)d.y);
 }
 
 // R32 = fl32(E_t + R64), E_t(r, c) = [r == row0 + c].
@@ -174,7 +178,7 @@ namespace {
 
 struct MixedBufs {
   float *W32, *R32, *Linv, *Uinv, *T32;
-  double *H1, *H2, *Y, *R64, *XH, *B1, *C, *partial;
+  double *H1, *H2, *Y, *dY, *R64, *XH, *B1, *C, *partial;
   int *ipiv, *info;
   int ntiles;
   ExactOperand opW, opH1, opH2;
@@ -186,19 +190,25 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
-int spectral_trace(bemgpu_ctx_s *ctx, MixedBufs &b, int n, int ns2, int nt2, cudaStream_t st, double S[2]) {
-  const double *X = b.Y;  // rows [0, ns2) of Y, leading dimension n
+// S from B1 = H1 X and C = H2 X^H.  incremental: X moved by the correction
+// dY of the last step, so B1 += H1 dX and C += H2 dX^H (3-slice products of
+// the small correction) instead of the full 5-slice products.
+int spectral_trace(bemgpu_ctx_s *ctx, MixedBufs &b, int n, int ns2, int nt2, cudaStream_t st, double S[2],
+                   bool incremental) {
+  const double *X = incremental ? b.dY : b.Y;  // rows [0, ns2), leading dimension n
+  const int sl = incremental ? DELTA_SLICES : MIXED_SLICES;
+  const int acc = incremental ? 1 : 0;
   ExactOperand opX, opXH;
-  int rc = bem_exact_prep(ctx, "X", false, X, n, nt2, ns2, 1.0, MIXED_SLICES, opX, st);
-  if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRACE, b.opH1, opX, b.B1, ns2, 0, st);
+  int rc = bem_exact_prep(ctx, "X", false, X, n, nt2, ns2, 1.0, sl, opX, st);
+  if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRACE, b.opH1, opX, b.B1, ns2, acc, st);
   if (rc) return rc;
   {
     ProfScope ps(ctx, BEMGPU_K_TRACE, st, 0.0, 32.0 * ns2 * (double)nt2);
     conj_transpose_kernel<<<dim3((ns2 + 31) / 32, (nt2 + 31) / 32), dim3(32, 8), 0, st>>>(X, n, ns2, nt2, b.XH);
     ctx->launches++;
   }
-  rc = bem_exact_prep(ctx, "XH", false, b.XH, nt2, ns2, nt2, 1.0, MIXED_SLICES, opXH, st);
-  if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRACE, b.opH2, opXH, b.C, nt2, 0, st);
+  rc = bem_exact_prep(ctx, "XH", false, b.XH, nt2, ns2, nt2, 1.0, sl, opXH, st);
+  if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRACE, b.opH2, opXH, b.C, nt2, acc, st);
   if (rc) return rc;
   const dim3 tg((ns2 + 31) / 32, (nt2 + 31) / 32);
   {
@@ -231,6 +241,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   b.H1 = (double *)bem_workspace(ctx, "m_H1", 16 * (size_t)ns2 * ns2);
   b.H2 = (double *)bem_workspace(ctx, "m_H2", 16 * (size_t)nt2 * nt2);
   b.Y = (double *)bem_workspace(ctx, "m_Y", 16 * nm);
+  b.dY = (double *)bem_workspace(ctx, "m_dY", 16 * nm);
   b.R64 = (double *)bem_workspace(ctx, "m_R64", 16 * nm);
   b.XH = (double *)bem_workspace(ctx, "m_XH", 16 * st2);
   b.B1 = (double *)bem_workspace(ctx, "m_B1", 16 * st2);
@@ -238,7 +249,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   b.partial = (double *)bem_workspace(ctx, "m_partial", 16 * (size_t)b.ntiles + 64);
   b.ipiv = (int *)bem_workspace(ctx, "m_ipiv", 4 * (size_t)n);
   b.info = (int *)bem_workspace(ctx, "m_info", 16);
-  const bool ok = b.W32 && b.R32 && b.Linv && b.Uinv && b.T32 && b.H1 && b.H2 && b.Y && b.R64 && b.XH && b.B1 && b.C && b.partial && b.ipiv &&
+  const bool ok = b.W32 && b.R32 && b.Linv && b.Uinv && b.T32 && b.H1 && b.H2 && b.Y && b.dY && b.R64 && b.XH && b.B1 && b.C && b.partial && b.ipiv &&
                   b.info;
   if (!ok) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: workspace allocation failed (n=%d)", n);
   cudaEvent_t *ev = ctx->ev;
@@ -267,7 +278,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   ctx->launches++;
   rc = bem_capply_inverse(ctx, b.Linv, b.Uinv, n, b.ipiv, b.R32, n, nt2, b.T32, st);
   if (rc) return rc;
-  update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 0);
+  update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 0, nullptr);
   ctx->launches++;
   cudaEventRecord(ev[3], st);
   int hinfo = 0;
@@ -280,21 +291,27 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   double err = 1.0, err_prev = 1.0;
   const int max_iters = 4;
   while (iters < max_iters) {
-    // R = E_t - W Y
+    // R = E_t - W Y: R64 holds -W Y; the first step forms it from Y, later
+    // steps add -W dY of the last correction (3-slice product)
     ExactOperand opY;
-    rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, MIXED_SLICES, opY, st);
-    if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
+    if (iters == 0) {
+      rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, MIXED_SLICES, opY, st);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
+    } else {
+      rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opY, st);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 1, st);
+    }
     if (rc) return rc;
     residual_finish_kernel<<<gm, 256, 0, st>>>(b.R64, b.R32, n, n, ns2);
     ctx->launches++;
     rc = bem_capply_inverse(ctx, b.Linv, b.Uinv, n, b.ipiv, b.R32, n, nt2, b.T32, st);
     if (rc) return rc;
-    update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 1);
+    update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 1, b.dY);
     ctx->launches++;
     iters++;
     Sprev[0] = S[0];
     Sprev[1] = S[1];
-    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S);
+    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, iters > 1);
     if (rc) return rc;
     if (bem_tc_error(ctx, true))
       return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "mixed solve: a tensor-core pipeline wait ran out");
