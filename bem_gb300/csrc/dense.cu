@@ -212,7 +212,7 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
 
 template <typename T>
 __global__ void __launch_bounds__(COOP_THREADS)
-    panel_coop_kernel(T *A, int64_t lda, int n, int k0, int w, int chunk, int *ipiv, int *info, double *cval,
+    panel_coop_kernel(T *A, int64_t lda, int n, int k0, int w, int chunk, int *ipiv, int *info, T *cval,
                       int *crow, T *cdata_raw, T *drow_raw, unsigned *counter, int *err) {
   typedef typename V2<T>::type T2;
   extern __shared__ __align__(16) unsigned char coop_smem[];
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(COOP_THREADS)
   T2 *A2 = reinterpret_cast<T2 *>(A);
   T2 *cdata = reinterpret_cast<T2 *>(cdata_raw);
   T2 *drow = reinterpret_cast<T2 *>(drow_raw);
-  __shared__ double red_v[COOP_THREADS / 32];
+  __shared__ T red_v[COOP_THREADS / 32];
   __shared__ int red_i[COOP_THREADS / 32], red_w[COOP_THREADS / 32];
   __shared__ int s_row, s_win;
   __shared__ bool s_abort, s_zero;
@@ -237,13 +237,13 @@ __global__ void __launch_bounds__(COOP_THREADS)
   for (int j = 0; j < w; j++) {
     const int dr = k0 + j, par = j & 1;
     // (1) local candidate: first row of largest |re| + |im| in column j, rows >= dr
-    double bv = -1.0;
+    T bv = T(-1);
     int bi = 0x7fffffff;
     for (int i = tid; i < nloc; i += COOP_THREADS) {
       const int r = rbeg + i;
       if (r < dr) continue;
       const T2 a = P[i * w + j];
-      const double v = fabs((double)a.x) + fabs((double)a.y);
+      const T v = fabs(a.x) + fabs(a.y);
       if (v > bv || (v == bv && r < bi)) {
         bv = v;
         bi = r;
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(COOP_THREADS)
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
+      const T v2 = __shfl_xor_sync(0xffffffffu, bv, o);
       const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
       if (v2 > bv || (v2 == bv && i2 < bi)) {
         bv = v2;
@@ -297,11 +297,11 @@ __global__ void __launch_bounds__(COOP_THREADS)
     __syncthreads();
     if (s_abort) return;
     // (3) the pivot: every CTA reduces the same candidates in the same way
-    bv = -1.0;
+    bv = T(-1);
     bi = 0x7fffffff;
     int bw = 0;
     for (int q = tid; q < G; q += COOP_THREADS) {
-      const double v = __ldcg(cval + par * G + q);
+      const T v = __ldcg(cval + par * G + q);
       const int r = __ldcg(crow + par * G + q);
       if (r == 0x7fffffff) continue;
       if (v > bv || (v == bv && r < bi)) {
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(COOP_THREADS)
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
+      const T v2 = __shfl_xor_sync(0xffffffffu, bv, o);
       const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
       const int w2 = __shfl_xor_sync(0xffffffffu, bw, o);
       if (v2 > bv || (v2 == bv && i2 < bi)) {
@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(COOP_THREADS)
           win = red_w[q];
         }
       if (bi == 0x7fffffff) win = -1;
-      const bool zero = !(bv > 0.0);
+      const bool zero = !(bv > T(0));
       if (zero) bi = dr;
       s_zero = zero;
       s_row = bi;
@@ -714,7 +714,7 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
     cudaGetLastError();
     return false;
   }
-  double *cval = (double *)bem_workspace(ctx, "coop_cval", sizeof(double) * 2 * 1024);
+  T *cval = (T *)bem_workspace(ctx, "coop_cval", sizeof(T) * 2 * 1024);
   int *crow = (int *)bem_workspace(ctx, "coop_crow", sizeof(int) * 2 * 1024);
   T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * 1024 * (size_t)NB);
   T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)NB);
