@@ -734,8 +734,8 @@ constexpr int NEAR_WARPS = 4;
 // the same moments as the FP64 loop in near_pairs_kernel (LKSmoothInnerIntegrand,
 // src/Impedance.cpp:93-105, with scalar_gradient_smooth, src/GreensFunction.cpp:54-69),
 // summed in df from df nodes (l, w) and widened to FP64.
-__device__ __noinline__ void near_inner_df(const float (*nd)[8], d3 rts, const GreenDev &g, z1 &I0o, z3 &Ao,
-                                              z1 &Q0o, z3 &Q1o) {
+__device__ __noinline__ void near_inner_df(const float (*nd)[8], d3 rts, const GreenDev &g, cdf &I0o, cdf3 &Ao,
+                                             cdf &Q0o, cdf3 &Q1o) {
   const df3 r = df3_make(rts);
   const df ikr = df_make(g.ikr), iki = df_make(g.iki), k2r = df_make(g.k2r), k2i = df_make(g.k2i);
   df I0r = {0.f, 0.f}, I0i = {0.f, 0.f}, Q0r = {0.f, 0.f}, Q0i = {0.f, 0.f};
@@ -777,12 +777,98 @@ __device__ __noinline__ void near_inner_df(const float (*nd)[8], d3 rts, const G
       Qi[c] = df_add(Qi[c], df_mul(qwi, l[c]));
     }
   }
-  I0o = {df_to_double(I0r), df_to_double(I0i)};
-  Q0o = {df_to_double(Q0r), df_to_double(Q0i)};
-  Ao = {{df_to_double(Ar[0]), df_to_double(Ai[0])}, {df_to_double(Ar[1]), df_to_double(Ai[1])},
-        {df_to_double(Ar[2]), df_to_double(Ai[2])}};
-  Q1o = {{df_to_double(Qr[0]), df_to_double(Qi[0])}, {df_to_double(Qr[1]), df_to_double(Qi[1])},
-         {df_to_double(Qr[2]), df_to_double(Qi[2])}};
+  I0o = {I0r, I0i};
+  Q0o = {Q0r, Q0i};
+  Ao = {{Ar[0], Ai[0]}, {Ar[1], Ai[1]}, {Ar[2], Ai[2]}};
+  Q1o = {{Qr[0], Qi[0]}, {Qr[1], Qi[1]}, {Qr[2], Qi[2]}};
+}
+
+// Per-pair double-float constants of the close-pair contraction, relative to
+// the test triangle's frame origin P_t: e_i = p0_i - P_t, f_j = p0_j - P_t,
+// d_j = p0_j - P_s.
+struct NearPairDF {
+  df3 e[3], f[3], d[3], nS;
+  df Ai2;
+  cdf ksq, k2, k2_3;
+};
+// The nine L and K sums of a near pair (complex df).
+struct NearAccDF {
+  cdf L[9], K[9];
+};
+
+// One outer node of a near pair in double-float: the smooth inner rule
+// (near_inner_df), the analytic singular terms (eh_nonsmooth, FP64) and the
+// close-pair contraction of src/Impedance.cpp:194-250 in df, added to acc.
+__device__ __noinline__ void near_outer_df(const float (*nd)[8], const TriRec &T, const TriRec &S, const GreenDev &g,
+                                           const NearPairDF &pc, d3 rt, double w, NearAccDF &acc) {
+  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+  cdf I0, Q0;
+  cdf3 A, Q1;
+  near_inner_df(nd, rt - Ps, g, I0, A, Q0, Q1);
+  double ISn3h_d, ISn1_d, IS1_d;
+  d3 IL1_d, IL3_d;
+  eh_nonsmooth(S, rt, ISn3h_d, ISn1_d, IS1_d, IL1_d, IL3_d);
+  const double h_d = dot(rt - Ps, ld3(S.n));
+  const df3 rt1 = df3_make(rt - Pt);
+  const df3 IL1 = df3_make(IL1_d), IL3 = df3_make(IL3_d);
+  const df ISn1 = df_make(ISn1_d), IS1 = df_make(IS1_d), wd = df_make(w);
+  // IL13 = Ai2 (k2/3 IL3 + IL1), ISn11 = Ai2 (ISn1 + k2 IS1), L2 = 2 ISn11 + I0
+  cdf3 IL13 = cdf_v(pc.k2_3, IL3);
+  IL13.x.r = df_add(IL13.x.r, IL1.x);
+  IL13.y.r = df_add(IL13.y.r, IL1.y);
+  IL13.z.r = df_add(IL13.z.r, IL1.z);
+  IL13 = cdf3_scale(pc.Ai2, IL13);
+  const cdf ISn11 = cdf_scale(pc.Ai2, cdf{df_add(ISn1, df_mul(pc.k2.r, IS1)), df_mul(pc.k2.i, IS1)});
+  const cdf L2 = cdf_add(cdf_add(ISn11, ISn11), I0);
+  const df half = {0.5f, 0.f};
+  const int nht = T.nh, nhs = S.nh;
+  if (fabs(h_d) < 1e-8 * S.elen0) {
+    for (int j = 0; j < nhs; j++) {
+      const cdf3 Gphij = cdf3_scale(half, cdf3_sub(A, cdf_v(I0, pc.d[j])));
+      const cdf3 K21 = cdf3_add(IL13, cdf_v(ISn11, df3_sub(rt1, pc.f[j])));
+      const cdf3 GK = cdf3_add(Gphij, K21);
+      for (int i = 0; i < nht; i++) {
+        const df3 phi = df3_scale(half, df3_sub(rt1, pc.e[i]));
+        const cdf t = cdf_sub(cdf_mul(pc.ksq, cdf_rdot(phi, GK)), L2);
+        acc.L[i * 3 + j] = cdf_add(acc.L[i * 3 + j], cdf_scale(wd, t));
+      }
+    }
+  } else {
+    const df h = df_make(h_d);
+    const df3 ISn3hn = df3_scale(df_mul(pc.Ai2, df_make(ISn3h_d)), pc.nS);
+    const df3 rho1 = df3_sub(rt1, df3_scale(h, pc.nS));
+    const cdf Ai2k2 = cdf_scale(pc.Ai2, pc.k2);
+    const cdf3 K31 = cdf_v(Ai2k2, df3_sub(IL1, df3_scale(df_mul(h, ISn1), pc.nS)));
+    for (int j = 0; j < nhs; j++) {
+      const df3 rf = df3_sub(rt1, pc.f[j]);  // r_t - p0_j
+      const cdf3 Gphij = cdf3_scale(half, cdf3_sub(A, cdf_v(I0, pc.d[j])));
+      const cdf3 DGxphij = cdf3_scale(half, cdf_rcross(rf, cdf3_sub(Q1, cdf_v(Q0, pc.d[j]))));
+      const cdf3 K21 = cdf3_add(IL13, cdf_v(ISn11, df3_sub(rho1, pc.f[j])));
+      const cdf3 K41 = cdf_zcross(K31, rf);
+      const cdf3 GK = cdf3_add(Gphij, K21);
+      for (int i = 0; i < nht; i++) {
+        const df3 phi = df3_scale(half, df3_sub(rt1, pc.e[i]));
+        const cdf t = cdf_sub(cdf_mul(pc.ksq, cdf_rdot(phi, GK)), L2);
+        acc.L[i * 3 + j] = cdf_add(acc.L[i * 3 + j], cdf_scale(wd, t));
+        const df3 vx = df3_cross(df3_sub(pc.f[j], pc.e[i]), ISn3hn);  // (p0_j - p0_i) x ISn3hn
+        cdf3 KK = cdf3_add(DGxphij, K41);
+        KK.x.r = df_add(KK.x.r, vx.x);
+        KK.y.r = df_add(KK.y.r, vx.y);
+        KK.z.r = df_add(KK.z.r, vx.z);
+        const cdf kk = cdf_rdot(phi, KK);
+        acc.K[i * 3 + j] = cdf_sub(acc.K[i * 3 + j], cdf_scale(wd, kk));
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ df warp_sum_df(df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const df u = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, u);
+  }
+  return v;
 }
 
 // DF: the smooth inner rule in double-float (near_inner_df), else FP64.
@@ -831,15 +917,40 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     for (int k = 0; k < 9; k++) { L[k] = {0, 0}; K[k] = {0, 0}; }
     const d3 nS = ld3(S.n);
     const double Ai2 = 0.5 * S.Ai;
-    for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
+    if (DF) {
+      NearPairDF pc;
+      for (int i = 0; i < 3; i++) {
+        pc.e[i] = df3_make(i < nht ? ld3(T.hp0[i]) - Pt : d3{0, 0, 0});
+        pc.f[i] = df3_make(i < nhs ? ld3(S.hp0[i]) - Pt : d3{0, 0, 0});
+        pc.d[i] = df3_make(dj[i]);
+      }
+      pc.nS = df3_make(nS);
+      pc.Ai2 = df_make(Ai2);
+      pc.ksq = {df_make(ksq.r), df_make(ksq.i)};
+      pc.k2 = {df_make(k2.r), df_make(k2.i)};
+      pc.k2_3 = {df_make(BEM_ONETHIRD * k2.r), df_make(BEM_ONETHIRD * k2.i)};
+      NearAccDF acc;
+      const df z = {0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 9; k++) { acc.L[k] = {z, z}; acc.K[k] = {z, z}; }
+      for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
+        const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
+        near_outer_df(nodes_df, T, S, g, pc, rt, c_rule105[q][2], acc);
+      }
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+        L[k] = {df_to_double(warp_sum_df(acc.L[k].r)), df_to_double(warp_sum_df(acc.L[k].i))};
+        K[k] = {df_to_double(warp_sum_df(acc.K[k].r)), df_to_double(warp_sum_df(acc.K[k].i))};
+      }
+    }
+    for (int q = lane; !DF && q < BEMGPU_TRI_RULE105_N; q += 32) {
       const double w = c_rule105[q][2];
       const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
       const d3 rts = rt - Ps;
       // LKSmoothInnerIntegrand over s[0] (src/Impedance.cpp:93-105) as moments
       z1 I0 = {0, 0}, Q0 = {0, 0};
       z3 A = z3zero(), Q1 = z3zero();
-      if (DF) near_inner_df(nodes_df, rts, g, I0, A, Q0, Q1);
-      for (int u = 0; !DF && u < BEMGPU_TRI_RULE91_N; u++) {
+      for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
         const d3 l = {nodes[u][0], nodes[u][1], nodes[u][2]};
         const double ws = nodes[u][3];
         const d3 x = rts - l;
@@ -914,7 +1025,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
       }
     }
 #pragma unroll
-    for (int k = 0; k < 9; k++) {
+    for (int k = 0; !DF && k < 9; k++) {
       L[k].r = warp_sum(L[k].r); L[k].i = warp_sum(L[k].i);
       K[k].r = warp_sum(K[k].r); K[k].i = warp_sum(K[k].i);
     }
