@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(HERE, "libbemgpu.so")
 
 OK = 0
 ERR_ARG, ERR_OOM, ERR_CUDA, ERR_SINGULAR, ERR_NO_CONVERGE, ERR_TIMEOUT, ERR_MESH = -1, -2, -3, -4, -5, -6, -7
+ERR_CANCELLED = -8
+PENDING = 1
 K_NAMES = ["fill_far", "fill_near", "gather", "lu_panel", "lu_gemm", "trsm", "solve_gemm", "trace", "refine_gemm",
            "near_spmm", "slice"]
 PREC_FP64 = 0
@@ -22,7 +24,7 @@ PREC_MIXED_LA = 2
 
 ERR_NAMES = {ERR_ARG: "BEMGPU_ERR_ARG", ERR_OOM: "BEMGPU_ERR_OOM", ERR_CUDA: "BEMGPU_ERR_CUDA",
              ERR_SINGULAR: "BEMGPU_ERR_SINGULAR", ERR_NO_CONVERGE: "BEMGPU_ERR_NO_CONVERGE",
-             ERR_TIMEOUT: "BEMGPU_ERR_TIMEOUT", ERR_MESH: "BEMGPU_ERR_MESH"}
+             ERR_TIMEOUT: "BEMGPU_ERR_TIMEOUT", ERR_MESH: "BEMGPU_ERR_MESH", ERR_CANCELLED: "BEMGPU_ERR_CANCELLED"}
 
 # Every symbol include/bemgpu.h declares.
 EXPORTED = [
@@ -32,6 +34,8 @@ EXPORTED = [
     "bemgpu_tree_size", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
     "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64", "bemgpu_zgemm_exact",
+    "bemgpu_farm_create", "bemgpu_farm_destroy", "bemgpu_farm_lanes", "bemgpu_farm_lane_ctx", "bemgpu_farm_submit",
+    "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error",
 ]
 
 
@@ -98,6 +102,14 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_cgemm_acc64": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_zgemm_exact": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_heat_transfer": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(ctypes.c_double), P(SolveInfo)]),
+        "bemgpu_farm_create": (i32, [i32, i32, P(vp)]),
+        "bemgpu_farm_destroy": (i32, [vp]),
+        "bemgpu_farm_lanes": (i32, [vp]),
+        "bemgpu_farm_lane_ctx": (i32, [vp, i32, P(vp)]),
+        "bemgpu_farm_submit": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(i64)]),
+        "bemgpu_farm_poll": (i32, [vp, i64, ctypes.c_double, P(ctypes.c_double), P(SolveInfo)]),
+        "bemgpu_farm_cancel": (i32, [vp, i64]),
+        "bemgpu_farm_last_error": (ctypes.c_char_p, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

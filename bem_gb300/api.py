@@ -226,6 +226,17 @@ def dimensionless_omega(a: float, eV: float) -> float:
     return _lib.load().bemgpu_dimensionless_omega(float(a), float(eV))
 
 
+def _solve_req(a: float, eV: float, T1: float, T2: float, s: RWGTree, t: RWGTree) -> _lib.SolveReq:
+    """The material constants of one request at eV, as CalcHeatTransfer reads
+    them (src/HeatTransfer.cpp:15-24: setTemperature, then eps/mu)."""
+    s.diel.setTemperature(T1)
+    t.diel.setTemperature(T2)
+    e1, m1, e2, m2 = s.diel.eps(eV), s.diel.mu(eV), t.diel.eps(eV), t.diel.mu(eV)
+    c2 = ctypes.c_double * 2
+    return _lib.SolveReq(a, eV, T1, T2, c2(e1.real, e1.imag), c2(m1.real, m1.imag), c2(e2.real, e2.imag),
+                         c2(m2.real, m2.imag))
+
+
 def CalcHeatTransfer(a: float, eV: float, T1: float, T2: float, top: RWGTree, s: RWGTree, t: RWGTree,
                      options: Options | None = None, precision: int = _lib.PREC_FP64, info: dict | None = None,
                      strict: bool = True) -> float:
@@ -234,11 +245,7 @@ def CalcHeatTransfer(a: float, eV: float, T1: float, T2: float, top: RWGTree, s:
     With strict=False a mixed-precision solve whose refinement stalls returns
     its result anyway; info['err_est'] then states the estimated error."""
     options = options or Options()
-    s.diel.setTemperature(T1)
-    t.diel.setTemperature(T2)
-    e1, m1, e2, m2 = s.diel.eps(eV), s.diel.mu(eV), t.diel.eps(eV), t.diel.mu(eV)
-    req = _lib.SolveReq(a, eV, T1, T2, (ctypes.c_double * 2)(e1.real, e1.imag), (ctypes.c_double * 2)(m1.real, m1.imag),
-                        (ctypes.c_double * 2)(e2.real, e2.imag), (ctypes.c_double * 2)(m2.real, m2.imag))
+    req = _solve_req(a, eV, T1, T2, s, t)
     P = ctypes.c_double()
     si = _lib.SolveInfo()
     ctx = top.geom.ctx
@@ -268,3 +275,109 @@ class FrequencySweep:
         except OSError as e:
             import sys
             sys.stderr.write(f"{filename}: {e.strerror}\n")
+
+
+class Farm:
+    """In-process request farm: the counterpart of the reference's MPI task
+    farm (src/transfer-mpi.cpp:25-190), where a Master queues
+    (a, gap, f, T1, T2) jobs and Servants run CalcHeatTransfer.  Here
+    ``lanes`` contexts on one GPU, each driven by its own native thread, take
+    requests from a FIFO, so several solves overlap on the device.
+
+    ``submit`` takes CalcHeatTransfer's arguments and returns a ticket;
+    ``result`` waits for it and returns the spectral power with
+    CalcHeatTransfer's error behaviour.  The farm keeps the trees of every
+    uncollected request alive."""
+
+    def __init__(self, lanes: int = 2, device: int = 0):
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = L.bemgpu_farm_create(int(device), int(lanes), ctypes.byref(h))
+        if rc != _lib.OK:
+            raise _lib.BemGpuError(rc, f"cannot create a {lanes}-lane farm on CUDA device {device}")
+        self.handle = h
+        self.lanes = lanes
+        self.device = device
+        self._held = {}
+
+    def _err(self) -> str:
+        return _lib.load().bemgpu_farm_last_error(self.handle).decode()
+
+    def lane_contexts(self) -> list:
+        """Raw context handles of the lanes (for bemgpu_prof_* statistics)."""
+        out = []
+        for i in range(self.lanes):
+            c = ctypes.c_void_p()
+            _lib.load().bemgpu_farm_lane_ctx(self.handle, i, ctypes.byref(c))
+            out.append(c)
+        return out
+
+    def submit(self, a: float, eV: float, T1: float, T2: float, top: RWGTree, s: RWGTree, t: RWGTree,
+               options: Options | None = None, precision: int = _lib.PREC_FP64) -> int:
+        options = options or Options()
+        req = _solve_req(a, eV, T1, T2, s, t)
+        tk = ctypes.c_int64()
+        rc = _lib.load().bemgpu_farm_submit(self.handle, top.handle, s.handle, t.handle, ctypes.byref(req),
+                                           ctypes.byref(options._c()), int(precision), ctypes.byref(tk))
+        if rc != _lib.OK:
+            raise _lib.BemGpuError(rc, self._err())
+        self._held[tk.value] = (top, s, t)
+        return tk.value
+
+    def poll(self, ticket: int, timeout: float | None = 0.0, info: dict | None = None, strict: bool = True):
+        """The request's spectral power, or None while it runs.  ``timeout``
+        in seconds (None: wait until it finishes)."""
+        P = ctypes.c_double()
+        si = _lib.SolveInfo()
+        ms = -1.0 if timeout is None else 1e3 * float(timeout)
+        rc = _lib.load().bemgpu_farm_poll(self.handle, int(ticket), ms, ctypes.byref(P), ctypes.byref(si))
+        if rc == _lib.PENDING:
+            return None
+        self._held.pop(int(ticket), None)
+        if info is not None:
+            for k, _ in _lib.SolveInfo._fields_:
+                info[k] = getattr(si, k)
+        if rc != _lib.OK and not (rc == _lib.ERR_NO_CONVERGE and not strict):
+            raise _lib.BemGpuError(rc, self._err())
+        return P.value
+
+    def result(self, ticket: int, info: dict | None = None, strict: bool = True) -> float:
+        return self.poll(ticket, None, info, strict)
+
+    def cancel(self, ticket: int) -> bool:
+        """True if the request was still queued and is now dropped."""
+        rc = _lib.load().bemgpu_farm_cancel(self.handle, int(ticket))
+        if rc < 0:
+            raise _lib.BemGpuError(rc, self._err())
+        return rc == _lib.OK
+
+    def map(self, jobs, options: Options | None = None, precision: int = _lib.PREC_FP64, strict: bool = True,
+            infos: list | None = None) -> list:
+        """Solves every (a, eV, T1, T2, top, s, t) of ``jobs``; results in job order."""
+        tickets = [self.submit(*j, options=options, precision=precision) for j in jobs]
+        out = []
+        for tk in tickets:
+            info = {} if infos is not None else None
+            out.append(self.result(tk, info, strict))
+            if infos is not None:
+                infos.append(info)
+        return out
+
+    def close(self):
+        if self.handle:
+            _lib.load().bemgpu_farm_destroy(self.handle)
+            self.handle = None
+            self._held.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

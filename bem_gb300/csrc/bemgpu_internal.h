@@ -57,6 +57,11 @@ struct bemgpu_tree_s {
   TriRec *d_rec = nullptr;
 };
 
+struct NearList {
+  NearPair *d = nullptr;
+  int64_t n = 0;
+};
+
 struct bemgpu_geom_s {
   bemgpu_ctx_s *ctx = nullptr;
   int refs = 1;  // the caller's handle + one per tree; freed at zero
@@ -64,11 +69,12 @@ struct bemgpu_geom_s {
   std::vector<double> xyz;
   std::vector<int> tri;
   std::vector<std::vector<int>> tris_at_vertex;
-};
-
-struct NearList {
-  NearPair *d = nullptr;
-  int64_t n = 0;
+  // per (t, s) tree pair over this geometry: the near-pair list (device) and
+  // the far-pair counts per rule; shared by every context that solves the
+  // trees (request-farm lanes), guarded by cache_mu
+  std::mutex cache_mu;
+  std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, NearList> near_cache;
+  std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, std::vector<int64_t>> far_rule_cache;
 };
 
 struct bemgpu_ctx_s {
@@ -80,9 +86,6 @@ struct bemgpu_ctx_s {
   std::mutex mu;
   // workspace: one growable device buffer per purpose
   std::map<std::string, std::pair<void *, size_t>> ws;
-  // near-pair lists cached per (t, s) tree pair
-  std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, NearList> near_cache;
-  std::map<std::pair<const bemgpu_tree_s *, const bemgpu_tree_s *>, std::vector<int64_t>> far_rule_cache;
   cudaEvent_t ev[8];
   int64_t launches = 0;  // kernels launched by this context
   bool tc_ready = false;      // gemm_tc.cu kernels: shared-memory attribute set

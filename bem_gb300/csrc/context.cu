@@ -91,9 +91,12 @@ void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::v
 }
 
 const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
+  (void)ctx;
+  bemgpu_geom_s *g = t->geom;
+  std::lock_guard<std::mutex> lk(g->cache_mu);
   auto key = std::make_pair(t, s);
-  auto it = ctx->near_cache.find(key);
-  if (it != ctx->near_cache.end()) return &it->second;
+  auto it = g->near_cache.find(key);
+  if (it != g->near_cache.end()) return &it->second;
   std::vector<NearPair> pairs;
   bem_build_near_pairs(t, s, pairs);
   NearList nl;
@@ -105,7 +108,7 @@ const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const b
     }
     cudaMemcpy(nl.d, pairs.data(), sizeof(NearPair) * pairs.size(), cudaMemcpyHostToDevice);
   }
-  auto res = ctx->near_cache.emplace(key, nl);
+  auto res = g->near_cache.emplace(key, nl);
   return &res.first->second;
 }
 
@@ -136,9 +139,12 @@ ProfScope::~ProfScope() {
 
 const int64_t *bem_far_rule_counts(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s,
                                    const bemgpu_options_t *opt) {
+  (void)ctx;
+  bemgpu_geom_s *g = t->geom;
+  std::lock_guard<std::mutex> lk(g->cache_mu);
   auto key = std::make_pair(t, s);
-  auto it = ctx->far_rule_cache.find(key);
-  if (it != ctx->far_rule_cache.end()) return it->second.data();
+  auto it = g->far_rule_cache.find(key);
+  if (it != g->far_rule_cache.end()) return it->second.data();
   std::vector<int64_t> c(5, 0);
   for (const TriRec &T : t->host_rec)
     for (const TriRec &S : s->host_rec) {
@@ -154,7 +160,7 @@ const int64_t *bem_far_rule_counts(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, co
             : d * opt->farThresh21 > e2 ? 3 : 4;
       c[k]++;
     }
-  auto res = ctx->far_rule_cache.emplace(key, c);
+  auto res = g->far_rule_cache.emplace(key, c);
   return res.first->second.data();
 }
 
@@ -219,7 +225,6 @@ static void ctx_teardown(bemgpu_ctx_s *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto &kv : ctx->ws) cudaFree(kv.second.first);
-  for (auto &kv : ctx->near_cache) cudaFree(kv.second.d);
   for (auto &e : ctx->ev) cudaEventDestroy(e);
   for (auto &e : ctx->ev_pool) cudaEventDestroy(e);
   cudaStreamDestroy(ctx->stream);
@@ -286,6 +291,8 @@ int bemgpu_geom_create(bemgpu_ctx_t ctx, const double *xyz, int nv, const int *t
 // caller then drops the geometry's reference on the context, unlocked).
 static bool geom_release(bemgpu_geom_s *g) {
   if (--g->refs == 0) {
+    cudaSetDevice(g->ctx->device);
+    for (auto &kv : g->near_cache) cudaFree(kv.second.d);
     delete g;
     return true;
   }
@@ -408,17 +415,23 @@ int bemgpu_tree_destroy(bemgpu_tree_t t) {
   bool geom_freed;
   {
   std::lock_guard<std::mutex> lk(ctx->mu);
-  cudaStreamSynchronize(ctx->stream);
-  for (auto it = ctx->far_rule_cache.begin(); it != ctx->far_rule_cache.end();) {
-    if (it->first.first == t || it->first.second == t) it = ctx->far_rule_cache.erase(it);
-    else ++it;
-  }
-  for (auto it = ctx->near_cache.begin(); it != ctx->near_cache.end();) {
-    if (it->first.first == t || it->first.second == t) {
-      cudaFree(it->second.d);
-      it = ctx->near_cache.erase(it);
-    } else {
-      ++it;
+  // any context may have solved the tree: wait for the device, not one stream
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  bemgpu_geom_s *g = t->geom;
+  {
+    std::lock_guard<std::mutex> lc(g->cache_mu);
+    for (auto it = g->far_rule_cache.begin(); it != g->far_rule_cache.end();) {
+      if (it->first.first == t || it->first.second == t) it = g->far_rule_cache.erase(it);
+      else ++it;
+    }
+    for (auto it = g->near_cache.begin(); it != g->near_cache.end();) {
+      if (it->first.first == t || it->first.second == t) {
+        cudaFree(it->second.d);
+        it = g->near_cache.erase(it);
+      } else {
+        ++it;
+      }
     }
   }
   cudaFree(t->d_rec);

@@ -1,0 +1,230 @@
+// Request farm: the in-process counterpart of the reference's MPI task farm
+// (src/transfer-mpi.cpp:25-190).  There, a Master thread queues
+// (a, gap, f, T1, T2) jobs and hands each to an idle Servant process, which
+// runs CalcHeatTransfer and sends back one double.  Here the servants are
+// lanes: each lane is a context (its own CUDA stream and workspace) driven by
+// one host thread, so the solves of several requests overlap on one GPU (the
+// latency-bound LU panels and fill tails of one lane run beside the
+// tensor-core products of another).  Requests wait in a FIFO; results are
+// collected by ticket.  No kernels live here: this file is host C++.
+#include "bemgpu_internal.h"
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+struct FarmJob {
+  int64_t ticket = 0;
+  bemgpu_tree_t top = nullptr, s = nullptr, t = nullptr;
+  bemgpu_solve_req_t req{};
+  bemgpu_options_t opt{};
+  int precision = 0;
+};
+
+enum JobState { QUEUED, RUNNING, DONE };
+
+struct FarmResult {
+  JobState state = QUEUED;
+  int status = BEMGPU_OK;
+  double P = 0.0;
+  bemgpu_solve_info_t info{};
+  std::string error;
+};
+
+}  // namespace
+
+struct bemgpu_farm_s {
+  int device = 0;
+  std::vector<bemgpu_ctx_t> lanes;
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv_job, cv_done;
+  std::deque<FarmJob> queue;
+  std::unordered_map<int64_t, FarmResult> results;  // every ticket not yet collected
+  int64_t next_ticket = 1;
+  bool stop = false;
+  std::string last_error;
+};
+
+namespace {
+
+void lane_main(bemgpu_farm_s *f, int lane) {
+  bemgpu_ctx_t ctx = f->lanes[lane];
+  for (;;) {
+    FarmJob job;
+    {
+      std::unique_lock<std::mutex> lk(f->mu);
+      f->cv_job.wait(lk, [f] { return f->stop || !f->queue.empty(); });
+      if (f->queue.empty()) return;  // stopping, nothing left
+      job = f->queue.front();
+      f->queue.pop_front();
+      f->results[job.ticket].state = RUNNING;
+    }
+    double P = 0.0;
+    bemgpu_solve_info_t info{};
+    const int rc = bemgpu_heat_transfer(ctx, job.top, job.s, job.t, &job.req, &job.opt, job.precision, &P, &info);
+    {
+      std::lock_guard<std::mutex> lk(f->mu);
+      FarmResult &r = f->results[job.ticket];
+      r.state = DONE;
+      r.status = rc;
+      r.P = P;
+      r.info = info;
+      if (rc != BEMGPU_OK) r.error = bemgpu_ctx_last_error(ctx);
+    }
+    f->cv_done.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bemgpu_farm_create(int device, int lanes, bemgpu_farm_t *out) {
+  if (!out || lanes < 1 || lanes > 16) return BEMGPU_ERR_ARG;
+  *out = nullptr;
+  bemgpu_farm_s *f = new bemgpu_farm_s();
+  f->device = device;
+  for (int i = 0; i < lanes; i++) {
+    bemgpu_ctx_t c = nullptr;
+    const int rc = bemgpu_ctx_create(device, &c);
+    if (rc != BEMGPU_OK) {
+      for (bemgpu_ctx_t l : f->lanes) bemgpu_ctx_destroy(l);
+      delete f;
+      return rc;
+    }
+    f->lanes.push_back(c);
+  }
+  for (int i = 0; i < lanes; i++) f->threads.emplace_back(lane_main, f, i);
+  *out = f;
+  return BEMGPU_OK;
+}
+
+int bemgpu_farm_destroy(bemgpu_farm_t f) {
+  if (!f) return BEMGPU_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(f->mu);
+    // queued requests are dropped (as cancelled); running ones finish
+    for (const FarmJob &j : f->queue) {
+      FarmResult &r = f->results[j.ticket];
+      r.state = DONE;
+      r.status = BEMGPU_ERR_CANCELLED;
+    }
+    f->queue.clear();
+    f->stop = true;
+  }
+  f->cv_job.notify_all();
+  for (std::thread &t : f->threads) t.join();
+  for (bemgpu_ctx_t c : f->lanes) bemgpu_ctx_destroy(c);
+  delete f;
+  return BEMGPU_OK;
+}
+
+int bemgpu_farm_lanes(bemgpu_farm_t f) { return f ? (int)f->lanes.size() : BEMGPU_ERR_ARG; }
+
+int bemgpu_farm_lane_ctx(bemgpu_farm_t f, int lane, bemgpu_ctx_t *ctx) {
+  if (!f || !ctx || lane < 0 || lane >= (int)f->lanes.size()) return BEMGPU_ERR_ARG;
+  *ctx = f->lanes[lane];
+  return BEMGPU_OK;
+}
+
+int bemgpu_farm_submit(bemgpu_farm_t f, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
+                       const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision, int64_t *ticket) {
+  if (!f || !top || !s || !t || !req || !ticket) return BEMGPU_ERR_ARG;
+  if (top->geom != s->geom || top->geom != t->geom || top->nrwg != s->nrwg + t->nrwg) {
+    std::lock_guard<std::mutex> lk(f->mu);
+    f->last_error = "farm_submit: top, s, t must share one geometry and size(top) = size(s) + size(t)";
+    return BEMGPU_ERR_ARG;
+  }
+  if (top->geom->ctx->device != f->device) {
+    std::lock_guard<std::mutex> lk(f->mu);
+    f->last_error = "farm_submit: the trees live on another device than the farm";
+    return BEMGPU_ERR_ARG;
+  }
+  if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED && precision != BEMGPU_PREC_MIXED_LA) {
+    std::lock_guard<std::mutex> lk(f->mu);
+    f->last_error = "farm_submit: unknown precision";
+    return BEMGPU_ERR_ARG;
+  }
+  FarmJob j;
+  j.top = top;
+  j.s = s;
+  j.t = t;
+  j.req = *req;
+  if (opt) j.opt = *opt; else bemgpu_options_default(&j.opt);
+  j.precision = precision;
+  {
+    std::lock_guard<std::mutex> lk(f->mu);
+    if (f->stop) return BEMGPU_ERR_ARG;
+    j.ticket = f->next_ticket++;
+    f->results[j.ticket] = FarmResult();
+    f->queue.push_back(j);
+    *ticket = j.ticket;
+  }
+  f->cv_job.notify_one();
+  return BEMGPU_OK;
+}
+
+int bemgpu_farm_poll(bemgpu_farm_t f, int64_t ticket, double timeout_ms, double *P_out, bemgpu_solve_info_t *info) {
+  if (!f) return BEMGPU_ERR_ARG;
+  std::unique_lock<std::mutex> lk(f->mu);
+  auto it = f->results.find(ticket);
+  if (it == f->results.end()) {
+    f->last_error = "farm_poll: unknown or already collected ticket";
+    return BEMGPU_ERR_ARG;
+  }
+  auto done = [f, ticket] {
+    auto i = f->results.find(ticket);
+    return i == f->results.end() || i->second.state == DONE;
+  };
+  if (timeout_ms < 0) {
+    f->cv_done.wait(lk, done);
+  } else if (timeout_ms > 0) {
+    f->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), done);
+  }
+  it = f->results.find(ticket);
+  if (it == f->results.end()) {  // collected meanwhile by another thread
+    f->last_error = "farm_poll: ticket collected by another caller";
+    return BEMGPU_ERR_ARG;
+  }
+  if (it->second.state != DONE) return BEMGPU_PENDING;
+  const FarmResult r = it->second;
+  f->results.erase(it);
+  if (P_out) *P_out = r.P;
+  if (info) *info = r.info;
+  if (r.status != BEMGPU_OK) f->last_error = r.error.empty() ? "farm: request cancelled" : r.error;
+  return r.status;
+}
+
+int bemgpu_farm_cancel(bemgpu_farm_t f, int64_t ticket) {
+  if (!f) return BEMGPU_ERR_ARG;
+  bool found = false;
+  {
+    std::lock_guard<std::mutex> lk(f->mu);
+    if (f->results.find(ticket) == f->results.end()) {
+      f->last_error = "farm_cancel: unknown or already collected ticket";
+      return BEMGPU_ERR_ARG;
+    }
+    for (auto it = f->queue.begin(); it != f->queue.end(); ++it)
+      if (it->ticket == ticket) {
+        f->queue.erase(it);
+        FarmResult &r = f->results[ticket];
+        r.state = DONE;
+        r.status = BEMGPU_ERR_CANCELLED;
+        found = true;
+        break;
+      }
+  }
+  if (found) f->cv_done.notify_all();
+  return found ? BEMGPU_OK : BEMGPU_PENDING;
+}
+
+const char *bemgpu_farm_last_error(bemgpu_farm_t f) { return f ? f->last_error.c_str() : "null farm"; }
+
+}  // extern "C"

@@ -1171,7 +1171,11 @@ ZDev to_zdev(const bemgpu_green_t *g) { return {g->Zeps[0], g->Zeps[1], g->Zmu[0
 
 bool g_tables_loaded[64] = {false};
 
+std::mutex g_tables_mu;
+
 int load_tables(bemgpu_ctx_s *ctx) {
+  // once per device; contexts on several host threads (farm lanes) may race here
+  std::lock_guard<std::mutex> lk(g_tables_mu);
   if (g_tables_loaded[ctx->device]) return BEMGPU_OK;
   BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule6, bemgpu_tri_rule6, sizeof(bemgpu_tri_rule6)));
   BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule10, bemgpu_tri_rule10, sizeof(bemgpu_tri_rule10)));
@@ -1348,6 +1352,7 @@ constexpr size_t NOALLOC_NEAR_BYTES = 2u << 20;       // first 2 MiB: the near-p
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
 std::mutex g_noalloc_mu;
+std::mutex g_noalloc_run_mu;  // one call at a time uses the shared scratch
 void *g_noalloc_addr[64] = {nullptr};
 
 }  // namespace
@@ -1372,6 +1377,9 @@ extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree
   bemgpu_options_t o;
   if (opt) o = *opt; else bemgpu_options_default(&o);
   std::lock_guard<std::mutex> lk(ctx->mu);
+  // the scratch is one array per process: calls from several contexts take
+  // turns (each call ends with its stream synchronised)
+  std::lock_guard<std::mutex> lkrun(g_noalloc_run_mu);
   cudaSetDevice(ctx->device);
   // Set-up, once per device with that device current: the host-side name of
   // the array is not a device address; ask the runtime for the address.

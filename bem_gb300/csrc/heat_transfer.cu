@@ -97,6 +97,9 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   if (!ctx || !top || !s || !t || !req || !P_out) return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: null argument");
   if (top->geom != s->geom || top->geom != t->geom)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: trees must share one geometry");
+  if (top->geom->ctx->device != ctx->device)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: the trees live on device %d, the context on %d",
+                    top->geom->ctx->device, ctx->device);
   if (top->nrwg != s->nrwg + t->nrwg)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: size(top) != size(s) + size(t)");
   if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED && precision != BEMGPU_PREC_MIXED_LA)

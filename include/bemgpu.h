@@ -36,6 +36,8 @@ extern "C" {
 #define BEMGPU_ERR_NO_CONVERGE (-5)  /* iterative refinement did not reach its tolerance */
 #define BEMGPU_ERR_TIMEOUT (-6)      /* a bounded device wait ran out */
 #define BEMGPU_ERR_MESH (-7)         /* mesh/RWG table is not a valid closed RWG table */
+#define BEMGPU_ERR_CANCELLED (-8)    /* a farm request was cancelled before it started */
+#define BEMGPU_PENDING 1             /* a farm request has not finished (not an error) */
 
 /* ---- precision modes ---- */
 #define BEMGPU_PREC_FP64 0    /* plain path: every stage in FP64 / complex128 */
@@ -48,6 +50,7 @@ extern "C" {
 typedef struct bemgpu_ctx_s *bemgpu_ctx_t;
 typedef struct bemgpu_geom_s *bemgpu_geom_t;
 typedef struct bemgpu_tree_s *bemgpu_tree_t;
+typedef struct bemgpu_farm_s *bemgpu_farm_t;
 
 /* GreensFunction fields (src/GreensFunction.h:7-28), complex values as {re, im}. */
 typedef struct {
@@ -195,6 +198,37 @@ int bemgpu_zgemm_exact(bemgpu_ctx_t ctx, int m, int n, int k, const double *dA, 
 int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
                          const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
                          double *P_out, bemgpu_solve_info_t *info);
+
+/* ---- request farm ----
+ * Replaces the reference's MPI task farm (src/transfer-mpi.cpp:25-190: a Master
+ * queue of (a, gap, f, T1, T2) jobs, Servants that run CalcHeatTransfer and
+ * return one double) inside one process: `lanes` contexts on one device, each
+ * driven by its own host thread, take requests from a FIFO, so several solves
+ * overlap on the GPU.  Trees are used read-only and must outlive every request
+ * that names them; they may belong to any context on the same device.  */
+int bemgpu_farm_create(int device, int lanes, bemgpu_farm_t *out);
+/* Drops the queued requests (their tickets become BEMGPU_ERR_CANCELLED),
+ * waits for the running ones, and frees the lanes. */
+int bemgpu_farm_destroy(bemgpu_farm_t farm);
+int bemgpu_farm_lanes(bemgpu_farm_t farm);
+/* The context of one lane (for bemgpu_prof_* and bemgpu_ctx_launches). */
+int bemgpu_farm_lane_ctx(bemgpu_farm_t farm, int lane, bemgpu_ctx_t *ctx);
+/* Queues one CalcHeatTransfer request (the arguments of bemgpu_heat_transfer;
+ * *req and *opt are copied) and returns its ticket. */
+int bemgpu_farm_submit(bemgpu_farm_t farm, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
+                       const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
+                       int64_t *ticket);
+/* Waits up to timeout_ms (< 0: without limit, 0: not at all) for a request.
+ * Returns BEMGPU_PENDING if it has not finished, else its status, exactly as
+ * bemgpu_heat_transfer would have returned it, with *P_out and *info written;
+ * a finished ticket is collected once.  */
+int bemgpu_farm_poll(bemgpu_farm_t farm, int64_t ticket, double timeout_ms, double *P_out,
+                     bemgpu_solve_info_t *info);
+/* Removes a queued request: BEMGPU_OK (its poll returns BEMGPU_ERR_CANCELLED),
+ * BEMGPU_PENDING if it has already started or finished (poll it as usual). */
+int bemgpu_farm_cancel(bemgpu_farm_t farm, int64_t ticket);
+/* Message of the farm's last failed call or collected failed request. */
+const char *bemgpu_farm_last_error(bemgpu_farm_t farm);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,76 @@
+"""Request farm (bemgpu_farm_*): several lanes solving at once must give the
+same spectral powers as one CalcHeatTransfer call after another, bit for bit
+(every kernel of the solve is deterministic), keep the reference's error
+behaviour per request, and drop queued requests on cancel / destroy.
+The reference's counterpart is the MPI task farm, src/transfer-mpi.cpp:25-190."""
+import numpy as np
+import pytest
+
+from bem_gb300 import _lib, api, mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def _systems(level=1, gaps=(0.05, 0.2)):
+    v, t = mesh.icosphere(1.0, level, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    return [api.parseShapes(b2.translated(mesh.gap_translation(v, v, g)), b2, d, d) for g in gaps]
+
+
+@pytest.mark.parametrize("precision", [_lib.PREC_FP64, _lib.PREC_MIXED_LA])
+@pytest.mark.parametrize("lanes", [1, 3])
+def test_farm_matches_serial_solves(precision, lanes):
+    systems = _systems()
+    jobs = [(1e-6, f, 300.0, 0.0, *systems[i % 2]) for i, f in enumerate(np.linspace(0.085, 0.125, 7))]
+    serial = [api.CalcHeatTransfer(*j, precision=precision, strict=False) for j in jobs]
+    with api.Farm(lanes) as farm:
+        infos = []
+        got = farm.map(jobs, precision=precision, strict=False, infos=infos)
+    assert got == serial
+    assert all(i["ms_fill"] > 0 for i in infos)
+
+
+def test_farm_out_of_order_collection_and_cancel():
+    systems = _systems(level=2, gaps=(0.1,))
+    top, s, t = systems[0]
+    with api.Farm(2) as farm:
+        tickets = [farm.submit(1e-6, f, 300.0, 0.0, top, s, t, precision=_lib.PREC_MIXED_LA)
+                   for f in np.linspace(0.09, 0.12, 6)]
+        # the last request is queued behind five others on two lanes
+        cancelled = farm.cancel(tickets[-1])
+        Ps = [farm.result(tk, strict=False) for tk in reversed(tickets[:-1])]
+        assert all(np.isfinite(Ps)) and all(P > 0 for P in Ps)
+        if cancelled:
+            with pytest.raises(_lib.BemGpuError) as e:
+                farm.result(tickets[-1])
+            assert e.value.code == _lib.ERR_CANCELLED
+        else:
+            assert farm.result(tickets[-1], strict=False) > 0
+        # a collected ticket is gone
+        with pytest.raises(_lib.BemGpuError) as e:
+            farm.poll(tickets[0])
+        assert e.value.code == _lib.ERR_ARG
+
+
+def test_farm_rejects_bad_requests():
+    systems = _systems(level=1, gaps=(0.1,))
+    top, s, t = systems[0]
+    with api.Farm(1) as farm:
+        with pytest.raises(_lib.BemGpuError) as e:
+            farm.submit(1e-6, 0.1, 300.0, 0.0, top, t, s, precision=7)
+        assert e.value.code == _lib.ERR_ARG
+        with pytest.raises(_lib.BemGpuError):
+            farm.submit(1e-6, 0.1, 300.0, 0.0, s, s, t)  # size(top) != size(s) + size(t)
+        # the farm still serves after rejected requests
+        assert farm.result(farm.submit(1e-6, 0.1, 300.0, 0.0, top, s, t)) == \
+            api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, t)
+
+
+def test_farm_destroy_drops_queued_requests():
+    systems = _systems(level=2, gaps=(0.1,))
+    farm = api.Farm(1)
+    for f in np.linspace(0.09, 0.12, 4):
+        farm.submit(1e-6, f, 300.0, 0.0, *systems[0], precision=_lib.PREC_MIXED_LA)
+    farm.close()  # returns after the running request; the queued ones are dropped
+    assert farm.handle is None
