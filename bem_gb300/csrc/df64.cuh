@@ -205,4 +205,30 @@ __device__ __forceinline__ df df_exp_df(df x) {
   return df_scale2(e, __int_as_float((127 + (int)n) << 23));
 }
 
+__device__ __forceinline__ df df_abs(df a) { return a.hi < 0.f ? df_neg(a) : a; }
+
+// log x, x > 0 with e^-85 < x < e^85: y0 = logf(x) (FP32), then one Newton
+// step on e^y = x: t = x e^-y0 - 1 (small), log x = y0 + log(1 + t) with
+// log(1 + t) = t - t^2/2 (the t^3 term is below 2^-48 for |t| < 2^-20).
+__device__ __forceinline__ df df_log(df x) {
+  const float y0 = logf(x.hi);
+  const df e = df_exp_df({-y0, 0.f});
+  const df t = df_add_f(df_mul(x, e), -1.f);
+  const df u = df_add_f(t, -0.5f * t.hi * t.hi);
+  return df_add_f(u, y0);
+}
+
+// atan2(y, x), (x, y) != (0, 0): t0 = atan2f(y, x) (FP32), then the exact
+// correction t = t0 + atan(r), r = (y cos t0 - x sin t0) / (x cos t0 + y sin t0),
+// with atan(r) = r for |r| < 2^-20 (the r^3 / 3 term is below 2^-60).
+__device__ __forceinline__ df df_atan2(df y, df x) {
+  const float t0 = atan2f(y.hi, x.hi);
+  df s, c;
+  df_sincos_df({t0, 0.f}, s, c);
+  const df num = df_sub(df_mul(y, c), df_mul(x, s));
+  const df den = df_add(df_mul(x, c), df_mul(y, s));
+  if (den.hi == 0.f) return {t0, 0.f};
+  return df_add_f(df_mul(num, df_rcp(den)), t0);
+}
+
 }  // namespace

@@ -730,88 +730,205 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 constexpr int NEAR_WARPS = 4;
 
-// Smooth inner rule of a near pair at one outer node, double-float version:
-// the same moments as the FP64 loop in near_pairs_kernel (LKSmoothInnerIntegrand,
-// src/Impedance.cpp:93-105, with scalar_gradient_smooth, src/GreensFunction.cpp:54-69),
-// summed in df from df nodes (l, w) and widened to FP64.
-__device__ __noinline__ void near_inner_df(const float (*nd)[8], d3 rts, const GreenDev &g, cdf &I0o, cdf3 &Ao,
-                                             cdf &Q0o, cdf3 &Q1o) {
-  const df3 r = df3_make(rts);
+// Moments of the smooth inner rule at one outer node (complex df):
+// I0 = sum w g~, A = sum w g~ l, Q0 = sum w q~, Q1 = sum w q~ l.
+struct InnerMomDF {
+  cdf I0, Q0;
+  cdf3 A, Q1;
+};
+
+// Smooth inner rule of a near pair at NP outer nodes at once, double-float
+// version: the same moments as the FP64 loop in near_pairs_kernel
+// (LKSmoothInnerIntegrand, src/Impedance.cpp:93-105, with
+// scalar_gradient_smooth, src/GreensFunction.cpp:54-69), summed in df from df
+// nodes (l, w).  The NP points are independent dependency chains over the same
+// inner nodes, which the scheduler interleaves.
+template <int NP>
+__device__ __noinline__ void near_inner_df(const float (*nd)[8], const df3 *rp, const GreenDev &g, InnerMomDF *out) {
   const df ikr = df_make(g.ikr), iki = df_make(g.iki), k2r = df_make(g.k2r), k2i = df_make(g.k2i);
-  df I0r = {0.f, 0.f}, I0i = {0.f, 0.f}, Q0r = {0.f, 0.f}, Q0i = {0.f, 0.f};
-  df Ar[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Ai[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-  df Qr[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Qi[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  df3 r[NP];
+  df I0r[NP], I0i[NP], Q0r[NP], Q0i[NP], Ar[NP][3], Ai[NP][3], Qr[NP][3], Qi[NP][3];
+  const df z = {0.f, 0.f};
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    r[p] = rp[p];
+    I0r[p] = z; I0i[p] = z; Q0r[p] = z; Q0i[p] = z;
+#pragma unroll
+    for (int c = 0; c < 3; c++) { Ar[p][c] = z; Ai[p][c] = z; Qr[p][c] = z; Qi[p][c] = z; }
+  }
   for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
     const float4 n0 = *reinterpret_cast<const float4 *>(&nd[u][0]);
     const float4 n1 = *reinterpret_cast<const float4 *>(&nd[u][4]);
     const df l[3] = {{n0.x, n0.y}, {n0.z, n0.w}, {n1.x, n1.y}};
     const df ws = {n1.z, n1.w};
-    const df xx = df_sub(r.x, l[0]), xy = df_sub(r.y, l[1]), xz = df_sub(r.z, l[2]);
-    const df R2 = df_add(df_add(df_sqr(xx), df_sqr(xy)), df_sqr(xz));
-    const df R = df_sqrt(R2);
-    const df Ri = df_rcp(R);
-    df er, ei;
-    df_exp_ikR(g, ikr, iki, R, er, ei);
-    // g~ = (e - 1)/R - k2 R
-    const df gr = df_sub(df_mul(df_add_f(er, -1.f), Ri), df_mul(k2r, R));
-    const df gi = df_sub(df_mul(ei, Ri), df_mul(k2i, R));
-    // q~ = (e (1 - ikR) + R^2 k2 - 1) / R^3
-    const df zr = df_mul(ikr, R), zi = df_mul(iki, R);
-    const df mr = df_add_f(df_neg(zr), 1.f), mi = df_neg(zi);
-    df nr = df_sub(df_mul(er, mr), df_mul(ei, mi));
-    df ni = df_add(df_mul(er, mi), df_mul(ei, mr));
-    nr = df_add_f(df_add(nr, df_mul(R2, k2r)), -1.f);
-    ni = df_add(ni, df_mul(R2, k2i));
-    const df Ri3 = df_mul(df_sqr(Ri), Ri);
-    const df qr = df_mul(Ri3, nr), qi = df_mul(Ri3, ni);
-    const df gwr = df_mul(ws, gr), gwi = df_mul(ws, gi), qwr = df_mul(ws, qr), qwi = df_mul(ws, qi);
-    I0r = df_add(I0r, gwr);
-    I0i = df_add(I0i, gwi);
-    Q0r = df_add(Q0r, qwr);
-    Q0i = df_add(Q0i, qwi);
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      Ar[c] = df_add(Ar[c], df_mul(gwr, l[c]));
-      Ai[c] = df_add(Ai[c], df_mul(gwi, l[c]));
-      Qr[c] = df_add(Qr[c], df_mul(qwr, l[c]));
-      Qi[c] = df_add(Qi[c], df_mul(qwi, l[c]));
+    for (int p = 0; p < NP; p++) {
+      const df xx = df_sub(r[p].x, l[0]), xy = df_sub(r[p].y, l[1]), xz = df_sub(r[p].z, l[2]);
+      const df R2 = df_add(df_add(df_sqr(xx), df_sqr(xy)), df_sqr(xz));
+      const df R = df_sqrt(R2);
+      const df Ri = df_rcp(R);
+      df er, ei;
+      df_exp_ikR(g, ikr, iki, R, er, ei);
+      // g~ = (e - 1)/R - k2 R
+      const df gr = df_sub(df_mul(df_add_f(er, -1.f), Ri), df_mul(k2r, R));
+      const df gi = df_sub(df_mul(ei, Ri), df_mul(k2i, R));
+      // q~ = (e (1 - ikR) + R^2 k2 - 1) / R^3
+      const df zr = df_mul(ikr, R), zi = df_mul(iki, R);
+      const df mr = df_add_f(df_neg(zr), 1.f), mi = df_neg(zi);
+      df nr = df_sub(df_mul(er, mr), df_mul(ei, mi));
+      df ni = df_add(df_mul(er, mi), df_mul(ei, mr));
+      nr = df_add_f(df_add(nr, df_mul(R2, k2r)), -1.f);
+      ni = df_add(ni, df_mul(R2, k2i));
+      const df Ri3 = df_mul(df_sqr(Ri), Ri);
+      const df qr = df_mul(Ri3, nr), qi = df_mul(Ri3, ni);
+      const df gwr = df_mul(ws, gr), gwi = df_mul(ws, gi), qwr = df_mul(ws, qr), qwi = df_mul(ws, qi);
+      I0r[p] = df_add(I0r[p], gwr);
+      I0i[p] = df_add(I0i[p], gwi);
+      Q0r[p] = df_add(Q0r[p], qwr);
+      Q0i[p] = df_add(Q0i[p], qwi);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        Ar[p][c] = df_add(Ar[p][c], df_mul(gwr, l[c]));
+        Ai[p][c] = df_add(Ai[p][c], df_mul(gwi, l[c]));
+        Qr[p][c] = df_add(Qr[p][c], df_mul(qwr, l[c]));
+        Qi[p][c] = df_add(Qi[p][c], df_mul(qwi, l[c]));
+      }
     }
   }
-  I0o = {I0r, I0i};
-  Q0o = {Q0r, Q0i};
-  Ao = {{Ar[0], Ai[0]}, {Ar[1], Ai[1]}, {Ar[2], Ai[2]}};
-  Q1o = {{Qr[0], Qi[0]}, {Qr[1], Qi[1]}, {Qr[2], Qi[2]}};
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    out[p].I0 = {I0r[p], I0i[p]};
+    out[p].Q0 = {Q0r[p], Q0i[p]};
+    out[p].A = {{Ar[p][0], Ai[p][0]}, {Ar[p][1], Ai[p][1]}, {Ar[p][2], Ai[p][2]}};
+    out[p].Q1 = {{Qr[p][0], Qi[p][0]}, {Qr[p][1], Qi[p][1]}, {Qr[p][2], Qi[p][2]}};
+  }
+}
+
+// A triangle in double-float, vertices relative to a chosen origin O (the
+// test triangle's p0): what the closed-form integrals below read.
+struct TriFrameDF {
+  df3 p0, p1, p2, n, v01, v12, v20, m01, m12, m20;
+  df nv01i, nv12i, nv20i;
+};
+
+__device__ void tri_frame_df(const TriRec &T, d3 O, TriFrameDF &F) {
+  F.p0 = df3_make(ld3(T.p0) - O);
+  F.p1 = df3_make(ld3(T.p1) - O);
+  F.p2 = df3_make(ld3(T.p2) - O);
+  F.n = df3_make(ld3(T.n));
+  F.v01 = df3_make(ld3(T.v01));
+  F.v12 = df3_make(ld3(T.v12));
+  F.v20 = df3_make(ld3(T.v20));
+  F.m01 = df3_make(ld3(T.m01));
+  F.m12 = df3_make(ld3(T.m12));
+  F.m20 = df3_make(ld3(T.m20));
+  F.nv01i = df_make(T.nv01i);
+  F.nv12i = df_make(T.nv12i);
+  F.nv20i = df_make(T.nv20i);
+}
+
+__device__ __forceinline__ df log_ratio_df(df num, df den, float tol) {
+  if (fabsf(num.hi) < tol || fabsf(den.hi) < tol) return {0.f, 0.f};
+  return df_log(df_mul(num, df_rcp(den)));
+}
+
+// The closed-form potential integrals of a triangle F seen from the point r
+// (both relative to the same origin), in double-float: the analytic part of
+// EHNonSmoothIntegral (src/Source.cpp:16-86, with full = true: ISn3h, ISn1,
+// IS1, IL1, IL3) and LKEdgeIntegral (src/Impedance.cpp:13-73, full = false:
+// ISn3h, ISn1, IL1), step for step as eh_nonsmooth / lk_edge_integral do them
+// in FP64; h = (r - p0) . n.  tol is the edge-line cut-off of the logarithms.
+__device__ __noinline__ void tri_potentials_df(const TriFrameDF &F, df3 r, float tol, bool full, df &ISn3h,
+                                               df &ISn1, df &IS1, df3 &IL1, df3 &IL3, df &h) {
+  const df3 p0 = df3_sub(r, F.p0), p1 = df3_sub(r, F.p1), p2 = df3_sub(r, F.p2);
+  const df R02 = df3_dot(p0, p0), R12 = df3_dot(p1, p1), R22 = df3_dot(p2, p2);
+  const df R0 = df_sqrt(R02), R1 = df_sqrt(R12), R2 = df_sqrt(R22);
+  const df3 a0 = df3_scale(df_rcp(R0), p0), a1 = df3_scale(df_rcp(R1), p1), a2 = df3_scale(df_rcp(R2), p2);
+  const df x = df_add_f(df_add(df3_dot(a0, df3_add(a1, a2)), df3_dot(a1, a2)), 1.f);
+  const df y = df_abs(df3_dot(a0, df3_cross(a1, a2)));
+  h = df3_dot(p0, F.n);
+  const df at = df_atan2(y, x);
+  ISn3h = df_scale2(at, h.hi < 0.f ? -2.f : 2.f);
+  const df s010 = df_mul(F.nv01i, df3_dot(F.v01, p0)), s011 = df_mul(F.nv01i, df3_dot(F.v01, p1));
+  const df s121 = df_mul(F.nv12i, df3_dot(F.v12, p1)), s122 = df_mul(F.nv12i, df3_dot(F.v12, p2));
+  const df s202 = df_mul(F.nv20i, df3_dot(F.v20, p2)), s200 = df_mul(F.nv20i, df3_dot(F.v20, p0));
+  const df ILn1_01 = log_ratio_df(df_sub(R1, s011), df_sub(R0, s010), tol);
+  const df ILn1_12 = log_ratio_df(df_sub(R2, s122), df_sub(R1, s121), tol);
+  const df ILn1_20 = log_ratio_df(df_sub(R0, s200), df_sub(R2, s202), tol);
+  const df t01 = df3_dot(F.m01, p0), t12 = df3_dot(F.m12, p1), t20 = df3_dot(F.m20, p2);
+  const df tl = df_add(df_add(df_mul(t01, ILn1_01), df_mul(t12, ILn1_12)), df_mul(t20, ILn1_20));
+  ISn1 = df_neg(df_add(df_mul(h, ISn3h), tl));
+  const df R02_01 = df_sub(R02, df_sqr(s010));
+  const df R02_12 = df_sub(R12, df_sqr(s121));
+  const df R02_20 = df_sub(R22, df_sqr(s202));
+  const df half = {0.5f, 0.f};
+  const df IL1_01 = df_mul(half, df_sub(df_mul(R02_01, ILn1_01), df_sub(df_mul(R1, s011), df_mul(R0, s010))));
+  const df IL1_12 = df_mul(half, df_sub(df_mul(R02_12, ILn1_12), df_sub(df_mul(R2, s122), df_mul(R1, s121))));
+  const df IL1_20 = df_mul(half, df_sub(df_mul(R02_20, ILn1_20), df_sub(df_mul(R0, s200), df_mul(R2, s202))));
+  IL1 = df3_add(df3_add(df3_scale(IL1_01, F.m01), df3_scale(IL1_12, F.m12)), df3_scale(IL1_20, F.m20));
+  if (!full) return;
+  const df q3 = {0.75f, 0.f}, q1 = {0.25f, 0.f};
+  const df IL3_01 = df_sub(df_mul(q3, df_mul(R02_01, IL1_01)),
+                           df_mul(q1, df_sub(df_mul(df_mul(R12, R1), s011), df_mul(df_mul(R02, R0), s010))));
+  const df IL3_12 = df_sub(df_mul(q3, df_mul(R02_12, IL1_12)),
+                           df_mul(q1, df_sub(df_mul(df_mul(R22, R2), s122), df_mul(df_mul(R12, R1), s121))));
+  const df IL3_20 = df_sub(df_mul(q3, df_mul(R02_20, IL1_20)),
+                           df_mul(q1, df_sub(df_mul(df_mul(R02, R0), s200), df_mul(df_mul(R22, R2), s202))));
+  const df third = {0x1.555556p-2f, -0x1.555556p-27f};
+  const df tI = df_add(df_add(df_mul(t01, IL1_01), df_mul(t12, IL1_12)), df_mul(t20, IL1_20));
+  IS1 = df_mul(third, df_sub(df_mul(df_sqr(h), ISn1), tI));
+  IL3 = df3_add(df3_add(df3_scale(IL3_01, F.m01), df3_scale(IL3_12, F.m12)), df3_scale(IL3_20, F.m20));
 }
 
 // Per-pair double-float constants of the close-pair contraction, relative to
 // the test triangle's frame origin P_t: e_i = p0_i - P_t, f_j = p0_j - P_t,
-// d_j = p0_j - P_s.
+// d_j = p0_j - P_s.  One per warp, in shared memory (every lane reads the same
+// words).
 struct NearPairDF {
-  df3 e[3], f[3], d[3], nS;
+  TriFrameDF Sf, Tf;        // source and test triangles
+  df3 e[3], f[3], d[3];
+  df3 sPs, v01t, v02t;      // P_s - P_t and the test triangle's edge vectors
   df Ai2;
   cdf ksq, k2, k2_3;
+  float tol_eh, tol_plane, tol_edge;
 };
 // The nine L and K sums of a near pair (complex df).
 struct NearAccDF {
   cdf L[9], K[9];
 };
 
-// One outer node of a near pair in double-float: the smooth inner rule
-// (near_inner_df), the analytic singular terms (eh_nonsmooth, FP64) and the
-// close-pair contraction of src/Impedance.cpp:194-250 in df, added to acc.
-__device__ __noinline__ void near_outer_df(const float (*nd)[8], const TriRec &T, const TriRec &S, const GreenDev &g,
-                                           const NearPairDF &pc, d3 rt, double w, NearAccDF &acc) {
+__device__ void near_pair_df_setup(const TriRec &T, const TriRec &S, const GreenDev &g, NearPairDF &pc) {
   const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
-  cdf I0, Q0;
-  cdf3 A, Q1;
-  near_inner_df(nd, rt - Ps, g, I0, A, Q0, Q1);
-  double ISn3h_d, ISn1_d, IS1_d;
-  d3 IL1_d, IL3_d;
-  eh_nonsmooth(S, rt, ISn3h_d, ISn1_d, IS1_d, IL1_d, IL3_d);
-  const double h_d = dot(rt - Ps, ld3(S.n));
-  const df3 rt1 = df3_make(rt - Pt);
-  const df3 IL1 = df3_make(IL1_d), IL3 = df3_make(IL3_d);
-  const df ISn1 = df_make(ISn1_d), IS1 = df_make(IS1_d), wd = df_make(w);
+  tri_frame_df(S, Pt, pc.Sf);
+  tri_frame_df(T, Pt, pc.Tf);
+  for (int i = 0; i < 3; i++) {
+    pc.e[i] = df3_make(i < T.nh ? ld3(T.hp0[i]) - Pt : d3{0, 0, 0});
+    pc.f[i] = df3_make(i < S.nh ? ld3(S.hp0[i]) - Pt : d3{0, 0, 0});
+    pc.d[i] = df3_make(i < S.nh ? ld3(S.hp0[i]) - Ps : d3{0, 0, 0});
+  }
+  pc.sPs = df3_make(Ps - Pt);
+  pc.v01t = df3_make(ld3(T.v01));
+  pc.v02t = df3_make(ld3(T.v02));
+  pc.Ai2 = df_make(0.5 * S.Ai);
+  pc.ksq = {df_make(g.ksqr), df_make(g.ksqi)};
+  pc.k2 = {df_make(g.k2r), df_make(g.k2i)};
+  pc.k2_3 = {df_make(BEM_ONETHIRD * g.k2r), df_make(BEM_ONETHIRD * g.k2i)};
+  pc.tol_eh = (float)(1e-6 * S.elen0);
+  pc.tol_plane = (float)(1e-8 * S.elen0);
+  pc.tol_edge = (float)(1e-8 * T.elen0);
+}
+
+// One outer node of a near pair in double-float: given the node's smooth
+// inner moments (near_inner_df), the analytic singular terms
+// (tri_potentials_df) and the close-pair contraction of
+// src/Impedance.cpp:194-250, added to acc.  rt1 is the node relative to P_t.
+__device__ __noinline__ void near_outer_df(const InnerMomDF &m, const NearPairDF &pc, int nht, int nhs, df3 rt1,
+                                           df wd, NearAccDF &acc) {
+  const cdf I0 = m.I0, Q0 = m.Q0;
+  const cdf3 A = m.A, Q1 = m.Q1;
+  df ISn3h, ISn1, IS1, h;
+  df3 IL1, IL3;
+  tri_potentials_df(pc.Sf, rt1, pc.tol_eh, true, ISn3h, ISn1, IS1, IL1, IL3, h);
   // IL13 = Ai2 (k2/3 IL3 + IL1), ISn11 = Ai2 (ISn1 + k2 IS1), L2 = 2 ISn11 + I0
   cdf3 IL13 = cdf_v(pc.k2_3, IL3);
   IL13.x.r = df_add(IL13.x.r, IL1.x);
@@ -821,8 +938,7 @@ __device__ __noinline__ void near_outer_df(const float (*nd)[8], const TriRec &T
   const cdf ISn11 = cdf_scale(pc.Ai2, cdf{df_add(ISn1, df_mul(pc.k2.r, IS1)), df_mul(pc.k2.i, IS1)});
   const cdf L2 = cdf_add(cdf_add(ISn11, ISn11), I0);
   const df half = {0.5f, 0.f};
-  const int nht = T.nh, nhs = S.nh;
-  if (fabs(h_d) < 1e-8 * S.elen0) {
+  if (fabsf(h.hi) < pc.tol_plane) {
     for (int j = 0; j < nhs; j++) {
       const cdf3 Gphij = cdf3_scale(half, cdf3_sub(A, cdf_v(I0, pc.d[j])));
       const cdf3 K21 = cdf3_add(IL13, cdf_v(ISn11, df3_sub(rt1, pc.f[j])));
@@ -834,11 +950,11 @@ __device__ __noinline__ void near_outer_df(const float (*nd)[8], const TriRec &T
       }
     }
   } else {
-    const df h = df_make(h_d);
-    const df3 ISn3hn = df3_scale(df_mul(pc.Ai2, df_make(ISn3h_d)), pc.nS);
-    const df3 rho1 = df3_sub(rt1, df3_scale(h, pc.nS));
+    const df3 nS = pc.Sf.n;
+    const df3 ISn3hn = df3_scale(df_mul(pc.Ai2, ISn3h), nS);
+    const df3 rho1 = df3_sub(rt1, df3_scale(h, nS));
     const cdf Ai2k2 = cdf_scale(pc.Ai2, pc.k2);
-    const cdf3 K31 = cdf_v(Ai2k2, df3_sub(IL1, df3_scale(df_mul(h, ISn1), pc.nS)));
+    const cdf3 K31 = cdf_v(Ai2k2, df3_sub(IL1, df3_scale(df_mul(h, ISn1), nS)));
     for (int j = 0; j < nhs; j++) {
       const df3 rf = df3_sub(rt1, pc.f[j]);  // r_t - p0_j
       const cdf3 Gphij = cdf3_scale(half, cdf3_sub(A, cdf_v(I0, pc.d[j])));
@@ -862,6 +978,20 @@ __device__ __noinline__ void near_outer_df(const float (*nd)[8], const TriRec &T
   }
 }
 
+// The neighbour-edge K correction of src/Impedance.cpp:301-324 at one source
+// edge node v (relative to P_t) in double-float: LKEdgeIntegral over the test
+// triangle, then Ke[i] += w (IL1 + ISn1 (rho - p0_i)).
+__device__ __noinline__ void near_edge_df(const NearPairDF &pc, int nht, df3 v, df w, df3 *Ke) {
+  df ISn3h, ISn1, IS1, h;
+  df3 IL1, IL3;
+  tri_potentials_df(pc.Tf, v, pc.tol_edge, false, ISn3h, ISn1, IS1, IL1, IL3, h);
+  const df3 rho = df3_sub(v, df3_scale(h, pc.Tf.n));
+  for (int i = 0; i < nht; i++) {
+    const df3 c = df3_add(IL1, df3_scale(ISn1, df3_sub(rho, pc.e[i])));
+    Ke[i] = df3_add(Ke[i], df3_scale(w, c));
+  }
+}
+
 __device__ __forceinline__ df warp_sum_df(df v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -878,12 +1008,24 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
   __shared__ double s_nodes[NEAR_WARPS][DF ? 1 : BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
   __shared__ __align__(16) float s_nodes_df[NEAR_WARPS][DF ? BEMGPU_TRI_RULE91_N : 1][8];
+  // double-float path: the outer rule (xi1, xi2, w as df) and one pair record per warp
+  __shared__ float s_outer_df[DF ? BEMGPU_TRI_RULE105_N : 1][6];
+  __shared__ NearPairDF s_pc[DF ? NEAR_WARPS : 1];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   double(*nodes)[4] = s_nodes[wid];
   float(*nodes_df)[8] = s_nodes_df[wid];
   const z1 ksq = {g.ksqr, g.ksqi};
   const z1 k2 = {g.k2r, g.k2i};
+  if (DF) {
+    for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
+      for (int c = 0; c < 3; c++) {
+        const df v = df_make(c_rule105[u][c]);
+        s_outer_df[u][2 * c] = v.hi;
+        s_outer_df[u][2 * c + 1] = v.lo;
+      }
+    __syncthreads();
+  }
   for (int64_t p = (int64_t)blockIdx.x * NEAR_WARPS + wid; p < npairs; p += (int64_t)gridDim.x * NEAR_WARPS) {
     const NearPair np = list[p];
     const TriRec &T = Tr[np.t];
@@ -918,24 +1060,21 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     const d3 nS = ld3(S.n);
     const double Ai2 = 0.5 * S.Ai;
     if (DF) {
-      NearPairDF pc;
-      for (int i = 0; i < 3; i++) {
-        pc.e[i] = df3_make(i < nht ? ld3(T.hp0[i]) - Pt : d3{0, 0, 0});
-        pc.f[i] = df3_make(i < nhs ? ld3(S.hp0[i]) - Pt : d3{0, 0, 0});
-        pc.d[i] = df3_make(dj[i]);
-      }
-      pc.nS = df3_make(nS);
-      pc.Ai2 = df_make(Ai2);
-      pc.ksq = {df_make(ksq.r), df_make(ksq.i)};
-      pc.k2 = {df_make(k2.r), df_make(k2.i)};
-      pc.k2_3 = {df_make(BEM_ONETHIRD * k2.r), df_make(BEM_ONETHIRD * k2.i)};
+      NearPairDF &pc = s_pc[DF ? wid : 0];
+      if (lane == 0) near_pair_df_setup(T, S, g, pc);
+      __syncwarp();
       NearAccDF acc;
       const df z = {0.f, 0.f};
 #pragma unroll
       for (int k = 0; k < 9; k++) { acc.L[k] = {z, z}; acc.K[k] = {z, z}; }
       for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
-        const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
-        near_outer_df(nodes_df, T, S, g, pc, rt, c_rule105[q][2], acc);
+        const float *o = s_outer_df[DF ? q : 0];
+        const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
+        const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
+        const df3 rs = df3_sub(rt1, pc.sPs);
+        InnerMomDF mom;
+        near_inner_df<1>(nodes_df, &rs, g, &mom);
+        near_outer_df(mom, pc, nht, nhs, rt1, wq, acc);
       }
 #pragma unroll
       for (int k = 0; k < 9; k++) {
@@ -1038,7 +1177,29 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
 #pragma unroll
         for (int i = 0; i < 3; i++) Ke[e][i] = {0, 0, 0};
       const d3 nT = ld3(T.n);
-      for (int idx = lane; idx < 45; idx += 32) {
+      if (DF) {
+        const NearPairDF &pc = s_pc[DF ? wid : 0];
+        df3 Kd[3][3];
+        const df z = {0.f, 0.f};
+#pragma unroll
+        for (int e = 0; e < 3; e++)
+#pragma unroll
+          for (int i = 0; i < 3; i++) Kd[e][i] = {z, z, z};
+        for (int idx = lane; idx < 45; idx += 32) {
+          const int e = idx / 15, q = idx - e * 15;
+          const df3 v0 = e == 0 ? pc.Sf.p0 : (e == 1 ? pc.Sf.p1 : pc.Sf.p2);
+          const df3 v1 = e == 0 ? pc.Sf.v01 : (e == 1 ? pc.Sf.v12 : pc.Sf.v20);
+          const df3 v = df3_add(v0, df3_scale(df_make(c_line15[q][0]), v1));
+          near_edge_df(pc, nht, v, df_make(c_line15[q][1]), Kd[e]);
+        }
+#pragma unroll
+        for (int e = 0; e < 3; e++)
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+            Ke[e][i] = {df_to_double(warp_sum_df(Kd[e][i].x)), df_to_double(warp_sum_df(Kd[e][i].y)),
+                        df_to_double(warp_sum_df(Kd[e][i].z))};
+      }
+      for (int idx = lane; !DF && idx < 45; idx += 32) {
         const int e = idx / 15, q = idx - e * 15;
         const d3 v0 = e == 0 ? ld3(S.p0) : (e == 1 ? ld3(S.p1) : ld3(S.p2));
         const d3 v1 = e == 0 ? ld3(S.v01) : (e == 1 ? ld3(S.v12) : ld3(S.v20));
@@ -1059,7 +1220,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
         }
       }
 #pragma unroll
-      for (int e = 0; e < 3; e++)
+      for (int e = 0; !DF && e < 3; e++)
 #pragma unroll
         for (int i = 0; i < 3; i++) {
           Ke[e][i].x = warp_sum(Ke[e][i].x);
