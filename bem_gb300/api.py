@@ -12,6 +12,12 @@ Same names, argument meaning and error behaviour as the reference's surface
   parseShapes(...) -> (top, s, t)             src/HeatTransfer.cpp:61-109 (with the
                                               trees kept alive, which the reference's
                                               by-value out-parameters do not do)
+  Farm(lanes).submit / result / cancel        the MPI task farm, src/transfer-mpi.cpp:25-190
+                                              (several solves in flight on one GPU)
+
+Materials beyond FixedLorentz / SiC live in bem_gb300.dielectrics, the X3D
+reader in bem_gb300.x3d, the transfer / transfer-mpi front ends in
+bem_gb300.transfer.
 
 All compute runs in libbemgpu.so on the GPU; there is no CPU path.
 """

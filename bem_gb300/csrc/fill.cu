@@ -246,7 +246,7 @@ __device__ __forceinline__ void df_exp_ikR(const GreenDev &g, df ikr, df iki, df
     df_sincos_df(th, sn, cs);
   else
     df_sincos(df_to_double(th), sn, cs);
-  if (g.ikr == 0.0) {
+  if (ikr.hi == 0.f) {  // real k (df_make keeps zero exactly): no FP64 compare per node
     er = cs;
     ei = sn;
     return;
@@ -260,70 +260,6 @@ __device__ __forceinline__ void df_exp_ikR(const GreenDev &g, df ikr, df iki, df
   const df m = df_exp_df(a);
   er = df_mul(m, cs);
   ei = df_mul(m, sn);
-}
-
-__device__ __noinline__ void far_pair_df(const TriRec &T, const TriRec &S, const GreenDev &g,
-                                         const double (*rule)[3], const float (*rdf)[6], int nr, HalfPairBlock *H,
-                                         int ntr) {
-  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
-  const d3 v01t = ld3(T.v01), v02t = ld3(T.v02);
-  const df3 v01s = df3_make(ld3(S.v01)), v02s = df3_make(ld3(S.v02));
-  const d3 D0 = Pt - Ps;
-  const df ikr = df_make(g.ikr), iki = df_make(g.iki);
-  z1 U0 = {0, 0}, U1 = {0, 0}, V0 = {0, 0};
-  z3 U2 = z3zero(), U3 = z3zero(), V1 = z3zero(), V2 = z3zero(), V3 = z3zero();
-  for (int q = 0; q < nr; q++) {
-    const double a = rule[q][0], b = rule[q][1], w = rule[q][2];
-    const d3 rho = a * v01t + b * v02t;
-    const df3 rts = df3_make(D0 + rho);  // r_t - P_s
-    df I0r = {0.f, 0.f}, I0i = {0.f, 0.f}, Q0r = {0.f, 0.f}, Q0i = {0.f, 0.f};
-    df Ar[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Ai[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    df Qr[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, Qi[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    for (int u = 0; u < nr; u++) {
-      const df as = {rdf[u][0], rdf[u][1]}, bs = {rdf[u][2], rdf[u][3]}, ws = {rdf[u][4], rdf[u][5]};
-      const df l[3] = {df_add(df_mul(as, v01s.x), df_mul(bs, v02s.x)), df_add(df_mul(as, v01s.y), df_mul(bs, v02s.y)),
-                       df_add(df_mul(as, v01s.z), df_mul(bs, v02s.z))};
-      const df xx = df_sub(rts.x, l[0]), xy = df_sub(rts.y, l[1]), xz = df_sub(rts.z, l[2]);
-      const df R2 = df_add(df_add(df_sqr(xx), df_sqr(xy)), df_sqr(xz));
-      const df R = df_sqrt(R2);
-      const df Ri = df_rcp(R);
-      df er, ei;
-      df_exp_ikR(g, ikr, iki, R, er, ei);
-      // scalar_gradient, src/GreensFunction.cpp:41-52: g = e / R, q = g (1 - ikR) / R^2
-      const df gr = df_mul(er, Ri), gi = df_mul(ei, Ri);
-      const df zr = df_mul(ikr, R), zi = df_mul(iki, R);
-      const df mr = df_add_f(df_neg(zr), 1.f), mi = df_neg(zi);  // 1 - ikR
-      const df Ri2 = df_sqr(Ri);
-      const df qr0 = df_sub(df_mul(gr, mr), df_mul(gi, mi)), qi0 = df_add(df_mul(gr, mi), df_mul(gi, mr));
-      const df qr = df_mul(qr0, Ri2), qi = df_mul(qi0, Ri2);
-      const df gwr = df_mul(ws, gr), gwi = df_mul(ws, gi), qwr = df_mul(ws, qr), qwi = df_mul(ws, qi);
-      I0r = df_add(I0r, gwr);
-      I0i = df_add(I0i, gwi);
-      Q0r = df_add(Q0r, qwr);
-      Q0i = df_add(Q0i, qwi);
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        Ar[c] = df_add(Ar[c], df_mul(gwr, l[c]));
-        Ai[c] = df_add(Ai[c], df_mul(gwi, l[c]));
-        Qr[c] = df_add(Qr[c], df_mul(qwr, l[c]));
-        Qi[c] = df_add(Qi[c], df_mul(qwi, l[c]));
-      }
-    }
-    const z1 I0 = {df_to_double(I0r), df_to_double(I0i)}, Q0 = {df_to_double(Q0r), df_to_double(Q0i)};
-    const z3 A = {{df_to_double(Ar[0]), df_to_double(Ai[0])}, {df_to_double(Ar[1]), df_to_double(Ai[1])},
-                  {df_to_double(Ar[2]), df_to_double(Ai[2])}};
-    const z3 Q1 = {{df_to_double(Qr[0]), df_to_double(Qi[0])}, {df_to_double(Qr[1]), df_to_double(Qi[1])},
-                   {df_to_double(Qr[2]), df_to_double(Qi[2])}};
-    zacc(U0, zscale(w, I0));
-    zacc(U1, zscale(w, rdot(rho, A)));
-    U2 = z3add(U2, zs_v(zscale(w, I0), rho));
-    U3 = z3add(U3, z3scale(w, A));
-    zacc(V0, zscale(w, Q0));
-    V1 = z3add(V1, z3scale(w, zcross(Q1, rho)));
-    V2 = z3add(V2, z3scale(w, Q1));
-    V3 = z3add(V3, zs_v(zscale(w, Q0), rho));
-  }
-  far_contract(T, S, g, U0, U1, U2, U3, V0, V1, V2, V3, H, ntr);
 }
 
 // ---------------- far pairs entirely in double-float ----------------
