@@ -18,7 +18,20 @@
 
 namespace {
 
-constexpr int NB = 64;  // panel width
+constexpr int NB = 64;  // panel width of the FP64 LU and of the blocked solves
+constexpr int NB_MAX = 128;  // widest LU panel (complex64: LuCfg<float>)
+// LU panel width per type: complex64 uses 128-wide panels so that the trailing
+// updates are K = 128 tensor-core products (half the passes over the trailing
+// matrix of 64-wide panels); complex128 keeps 64 (its diagonal block must fit
+// the triangular-solve kernel's shared memory).
+template <typename T>
+struct LuCfg {
+  static constexpr int NBL = 64;
+};
+template <>
+struct LuCfg<float> {
+  static constexpr int NBL = 128;
+};
 
 template <typename T>
 struct V2;
@@ -397,17 +410,18 @@ __global__ void __launch_bounds__(COOP_THREADS)
 }
 
 // B[0:w, :] <- L11^{-1} B (unit lower) or U11^{-1} B (upper) with the w x w
-// diagonal block in shared memory; one warp per right-hand-side column, lane
-// holds rows lane and lane+32.
-template <typename T, bool UPPER>
+// diagonal block (w <= 32 R) in shared memory; one warp per right-hand-side
+// column, lane holds rows lane + 32 r, r < R.
+template <typename T, bool UPPER, int R>
 __global__ void __launch_bounds__(256) trsm_block_kernel(const T *Ad, int64_t lda, int w, T *B, int64_t ldb,
                                                          int ncols) {
   typedef typename V2<T>::type T2;
+  constexpr int LDS = 32 * R;
   extern __shared__ __align__(16) unsigned char trsm_smem[];
-  T2 *Ls = reinterpret_cast<T2 *>(trsm_smem);  // NB * NB
+  T2 *Ls = reinterpret_cast<T2 *>(trsm_smem);  // LDS * LDS
   for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
     const int r = idx % w, c = idx / w;
-    Ls[r + NB * c] = reinterpret_cast<const T2 *>(Ad)[r + lda * (int64_t)c];
+    Ls[r + LDS * c] = reinterpret_cast<const T2 *>(Ad)[r + lda * (int64_t)c];
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -415,51 +429,55 @@ __global__ void __launch_bounds__(256) trsm_block_kernel(const T *Ad, int64_t ld
   const int nwarps = blockDim.x >> 5;
   for (int col = blockIdx.x * nwarps + warp; col < ncols; col += gridDim.x * nwarps) {
     T2 *b = reinterpret_cast<T2 *>(B) + ldb * (int64_t)col;
-    cx<T> x0 = {0, 0}, x1 = {0, 0};
-    if (lane < w) x0 = {b[lane].x, b[lane].y};
-    if (lane + 32 < w) x1 = {b[lane + 32].x, b[lane + 32].y};
+    cx<T> x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      x[r] = {0, 0};
+      if (lane + 32 * r < w) x[r] = {b[lane + 32 * r].x, b[lane + 32 * r].y};
+    }
     if (!UPPER) {
       for (int i = 0; i < w; i++) {
-        const cx<T> xi = {__shfl_sync(0xffffffffu, i < 32 ? x0.r : x1.r, i & 31),
-                          __shfl_sync(0xffffffffu, i < 32 ? x0.i : x1.i, i & 31)};
-        if (lane > i && lane < w) {
-          const T2 l = Ls[lane + NB * i];
-          x0.r -= l.x * xi.r - l.y * xi.i;
-          x0.i -= l.x * xi.i + l.y * xi.r;
-        }
-        if (lane + 32 > i && lane + 32 < w) {
-          const T2 l = Ls[lane + 32 + NB * i];
-          x1.r -= l.x * xi.r - l.y * xi.i;
-          x1.i -= l.x * xi.i + l.y * xi.r;
+        cx<T> own = {0, 0};
+#pragma unroll
+        for (int r = 0; r < R; r++)
+          if ((i >> 5) == r) own = x[r];
+        const cx<T> xi = {__shfl_sync(0xffffffffu, own.r, i & 31), __shfl_sync(0xffffffffu, own.i, i & 31)};
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const int row = lane + 32 * r;
+          if (row > i && row < w) {
+            const T2 l = Ls[row + LDS * i];
+            x[r].r -= l.x * xi.r - l.y * xi.i;
+            x[r].i -= l.x * xi.i + l.y * xi.r;
+          }
         }
       }
     } else {
       for (int i = w - 1; i >= 0; i--) {
         // x_i /= U_ii on the owning lane, then broadcast
-        if (i < 32 && lane == i) {
-          const T2 d = Ls[i + NB * i];
-          x0 = cmul(x0, crecip(cx<T>{d.x, d.y}));
-        }
-        if (i >= 32 && lane == i - 32) {
-          const T2 d = Ls[i + NB * i];
-          x1 = cmul(x1, crecip(cx<T>{d.x, d.y}));
-        }
-        const cx<T> xi = {__shfl_sync(0xffffffffu, i < 32 ? x0.r : x1.r, i & 31),
-                          __shfl_sync(0xffffffffu, i < 32 ? x0.i : x1.i, i & 31)};
-        if (lane < i) {
-          const T2 u = Ls[lane + NB * i];
-          x0.r -= u.x * xi.r - u.y * xi.i;
-          x0.i -= u.x * xi.i + u.y * xi.r;
-        }
-        if (lane + 32 < i) {
-          const T2 u = Ls[lane + 32 + NB * i];
-          x1.r -= u.x * xi.r - u.y * xi.i;
-          x1.i -= u.x * xi.i + u.y * xi.r;
+        const T2 d = Ls[i + LDS * i];
+        cx<T> own = {0, 0};
+#pragma unroll
+        for (int r = 0; r < R; r++)
+          if ((i >> 5) == r) {
+            if (lane == (i & 31)) x[r] = cmul(x[r], crecip(cx<T>{d.x, d.y}));
+            own = x[r];
+          }
+        const cx<T> xi = {__shfl_sync(0xffffffffu, own.r, i & 31), __shfl_sync(0xffffffffu, own.i, i & 31)};
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const int row = lane + 32 * r;
+          if (row < i) {
+            const T2 u = Ls[row + LDS * i];
+            x[r].r -= u.x * xi.r - u.y * xi.i;
+            x[r].i -= u.x * xi.i + u.y * xi.r;
+          }
         }
       }
     }
-    if (lane < w) b[lane] = V2<T>::make(x0.r, x0.i);
-    if (lane + 32 < w) b[lane + 32] = V2<T>::make(x1.r, x1.i);
+#pragma unroll
+    for (int r = 0; r < R; r++)
+      if (lane + 32 * r < w) b[lane + 32 * r] = V2<T>::make(x[r].r, x[r].i);
   }
 }
 
@@ -595,17 +613,20 @@ struct GemmCfg<float> {
   static constexpr int BM = 128, BN = 64, TM = 8, TN = 4, BK = 8;
 };
 
-template <typename T>
-constexpr int trsm_smem_bytes() { return NB * NB * (int)sizeof(typename V2<T>::type); }
+template <typename T, int R = NB / 32>
+constexpr int trsm_smem_bytes() { return 32 * R * 32 * R * (int)sizeof(typename V2<T>::type); }
 
 template <typename T>
 int set_trsm_attrs(bemgpu_ctx_s *ctx) {
   static bool done[64] = {false};
   if (done[ctx->device]) return BEMGPU_OK;
-  BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_block_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         trsm_smem_bytes<T>()));
-  BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_block_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         trsm_smem_bytes<T>()));
+  constexpr int RL = LuCfg<T>::NBL / 32;
+  BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_block_kernel<T, false, NB / 32>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, trsm_smem_bytes<T>()));
+  BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_block_kernel<T, true, NB / 32>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, trsm_smem_bytes<T>()));
+  BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(trsm_block_kernel<T, false, RL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         trsm_smem_bytes<T, RL>()));
   done[ctx->device] = true;
   return BEMGPU_OK;
 }
@@ -716,11 +737,11 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
   }
   T *cval = (T *)bem_workspace(ctx, "coop_cval", sizeof(T) * 2 * 1024);
   int *crow = (int *)bem_workspace(ctx, "coop_crow", sizeof(int) * 2 * 1024);
-  T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * 1024 * (size_t)NB);
-  T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)NB);
+  T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * 1024 * (size_t)NB_MAX);
+  T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)NB_MAX);
   unsigned *counter = (unsigned *)bem_workspace(ctx, "coop_counter", sizeof(unsigned));
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
-  if (!cval || !crow || !cdata || !drow || !counter || !err || G > 1024 || w > NB) {
+  if (!cval || !crow || !cdata || !drow || !counter || !err || G > 1024 || w > NB_MAX) {
     rc = bem_fail(ctx, BEMGPU_ERR_OOM, "getrf: panel workspace");
     return true;
   }
@@ -753,8 +774,9 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
   BEM_CUDA_TRY(ctx, cudaMemsetAsync(d_info, 0, sizeof(int), stream));
   const T mone[2] = {T(-1), T(0)}, one[2] = {T(1), T(0)};
   const double cb = 2.0 * sizeof(T);  // bytes per complex element
-  for (int k0 = 0; k0 < n; k0 += NB) {
-    const int w = std::min(NB, n - k0);
+  constexpr int NBL = LuCfg<T>::NBL;
+  for (int k0 = 0; k0 < n; k0 += NBL) {
+    const int w = std::min(NBL, n - k0);
     const int rows = n - k0;
     const int blocks = std::max(1, std::min(ctx->num_sms * 2, (rows + PANEL_THREADS - 1) / PANEL_THREADS));
     int prc = BEMGPU_OK;
@@ -776,7 +798,9 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
       const int nr = n - k0 - w;
       T *A11 = A + 2 * (k0 + lda * (int64_t)k0);
       T *A12 = A + 2 * (k0 + lda * (int64_t)(k0 + w));
-      const int tb = std::min((nr + 7) / 8, ctx->num_sms * 4);
+      // one CTA per SM at most: each CTA stages the w x w diagonal block in
+      // shared memory once and walks its share of the columns
+      const int tb = std::min((nr + 7) / 8, NBL > 64 ? ctx->num_sms : ctx->num_sms * 4);
       {
         ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * nr);
         laswp_kernel<T><<<(nr + 127) / 128, 128, 0, stream>>>(A, lda, k0 + w, n, k0, k0 + w, d_ipiv);
@@ -784,7 +808,8 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
       }
       {
         ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nr, 2.0 * cb * w * nr);
-        trsm_block_kernel<T, false><<<tb, 256, trsm_smem_bytes<T>(), stream>>>(A11, lda, w, A12, lda, nr);
+        trsm_block_kernel<T, false, NBL / 32>
+            <<<tb, 256, trsm_smem_bytes<T, NBL / 32>(), stream>>>(A11, lda, w, A12, lda, nr);
         ctx->launches++;
       }
       T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
@@ -816,7 +841,7 @@ int getrs_impl(bemgpu_ctx_s *ctx, const T *A, int64_t lda, int n, const int *d_i
     T *Bk = B + 2 * (int64_t)k0;
     {
       ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nrhs, 2.0 * cb * w * nrhs);
-      trsm_block_kernel<T, false><<<tb, 256, trsm_smem_bytes<T>(), stream>>>(L11, lda, w, Bk, ldb, nrhs);
+      trsm_block_kernel<T, false, NB / 32><<<tb, 256, trsm_smem_bytes<T>(), stream>>>(L11, lda, w, Bk, ldb, nrhs);
       ctx->launches++;
     }
     if (k0 + w < n) {
@@ -835,7 +860,7 @@ int getrs_impl(bemgpu_ctx_s *ctx, const T *A, int64_t lda, int n, const int *d_i
     T *Bk = B + 2 * (int64_t)k0;
     {
       ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nrhs, 2.0 * cb * w * nrhs);
-      trsm_block_kernel<T, true><<<tb, 256, trsm_smem_bytes<T>(), stream>>>(U11, lda, w, Bk, ldb, nrhs);
+      trsm_block_kernel<T, true, NB / 32><<<tb, 256, trsm_smem_bytes<T>(), stream>>>(U11, lda, w, Bk, ldb, nrhs);
       ctx->launches++;
     }
     if (k0 > 0) {
