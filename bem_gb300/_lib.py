@@ -35,7 +35,8 @@ EXPORTED = [
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
     "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64", "bemgpu_zgemm_exact",
     "bemgpu_farm_create", "bemgpu_farm_destroy", "bemgpu_farm_lanes", "bemgpu_farm_lane_ctx", "bemgpu_farm_submit",
-    "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error",
+    "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error", "bemgpu_farm_set_budget",
+    "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint",
 ]
 
 
@@ -60,7 +61,8 @@ class SolveInfo(ctypes.Structure):
                 ("ms_trace", ctypes.c_double), ("ms_refine", ctypes.c_double),
                 ("S_re", ctypes.c_double), ("S_im", ctypes.c_double), ("err_est", ctypes.c_double),
                 ("refine_iters", ctypes.c_int),
-                ("pairs_near", ctypes.c_int64), ("pairs_far_fp64", ctypes.c_int64), ("pairs_far_fp32", ctypes.c_int64)]
+                ("pairs_near", ctypes.c_int64), ("pairs_far_fp64", ctypes.c_int64), ("pairs_far_fp32", ctypes.c_int64),
+                ("ms_queued", ctypes.c_double), ("ms_latency", ctypes.c_double)]
 
 
 _lib = None
@@ -110,6 +112,11 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_farm_poll": (i32, [vp, i64, ctypes.c_double, P(ctypes.c_double), P(SolveInfo)]),
         "bemgpu_farm_cancel": (i32, [vp, i64]),
         "bemgpu_farm_last_error": (ctypes.c_char_p, [vp]),
+        "bemgpu_farm_set_budget": (i32, [vp, i64]),
+        "bemgpu_farm_budget": (i64, [vp]),
+        "bemgpu_ctx_workspace_bytes": (i64, [vp]),
+        "bemgpu_ctx_trim": (i32, [vp]),
+        "bemgpu_solve_footprint": (i64, [i32, i32, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

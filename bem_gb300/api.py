@@ -283,6 +283,16 @@ class FrequencySweep:
             sys.stderr.write(f"{filename}: {e.strerror}\n")
 
 
+def solve_footprint(s: RWGTree, t: RWGTree, precision: int = _lib.PREC_FP64) -> int:
+    """Device bytes one CalcHeatTransfer solve of these bodies needs at most."""
+    return int(_lib.load().bemgpu_solve_footprint(s.rwgs, t.rwgs, int(precision)))
+
+
+def _check_farm(rc: int, farm):
+    if rc != _lib.OK:
+        raise _lib.BemGpuError(rc, _lib.load().bemgpu_farm_last_error(farm.handle).decode())
+
+
 class Farm:
     """In-process request farm: the counterpart of the reference's MPI task
     farm (src/transfer-mpi.cpp:25-190), where a Master queues
@@ -308,6 +318,15 @@ class Farm:
 
     def _err(self) -> str:
         return _lib.load().bemgpu_farm_last_error(self.handle).decode()
+
+    @property
+    def budget(self) -> int:
+        """Device bytes the lanes may hold together (admission by footprint)."""
+        return int(_lib.load().bemgpu_farm_budget(self.handle))
+
+    @budget.setter
+    def budget(self, nbytes: int):
+        _check_farm(_lib.load().bemgpu_farm_set_budget(self.handle, int(nbytes)), self)
 
     def lane_contexts(self) -> list:
         """Raw context handles of the lanes (for bemgpu_prof_* statistics)."""

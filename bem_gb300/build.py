@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbemgpu.so")
 
 SOURCES = ["context.cu", "fill.cu", "dense.cu", "gemm_tc.cu", "gemm_exact.cu", "mixed.cu", "heat_transfer.cu", "farm.cu"]
-HEADERS = ["bemgpu_internal.h", "quadrature_tables.h", "tc_common.cuh", os.path.join("..", "..", "include", "bemgpu.h")]
+HEADERS = ["bemgpu_internal.h", "quadrature_tables.h", "tc_common.cuh", "df64.cuh", "df_constants.h", os.path.join("..", "..", "include", "bemgpu.h")]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

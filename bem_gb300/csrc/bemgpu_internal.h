@@ -117,6 +117,15 @@ struct ProfScope {
   ~ProfScope();
 };
 
+// Device bytes of an exact-product operand (bem_exact_prep) and of the bf16x3
+// slice planes of a complex64 tensor-core product (bem_cgemm_tc).
+size_t bem_exact_operand_bytes(bool is_a, int rows, int k, int slices);
+void bem_cgemm_tc_bytes(int m, int n, int k, size_t &a_bytes, size_t &b_bytes);
+// Frees one named workspace buffer (after synchronising the context stream).
+void bem_workspace_release(bemgpu_ctx_s *ctx, const std::string &name);
+// Bytes of workspace the context holds.
+size_t bem_workspace_bytes(const bemgpu_ctx_s *ctx);
+
 // Sets ctx->last_error and returns code.
 int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...);
 // Returns a device buffer of at least `bytes` for `name` (grown on demand).

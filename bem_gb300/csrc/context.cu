@@ -67,6 +67,20 @@ void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes) {
   return p;
 }
 
+void bem_workspace_release(bemgpu_ctx_s *ctx, const std::string &name) {
+  auto it = ctx->ws.find(name);
+  if (it == ctx->ws.end()) return;
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(it->second.first);
+  ctx->ws.erase(it);
+}
+
+size_t bem_workspace_bytes(const bemgpu_ctx_s *ctx) {
+  size_t b = 0;
+  for (auto &kv : ctx->ws) b += kv.second.second;
+  return b;
+}
+
 void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::vector<NearPair> &pairs) {
   pairs.clear();
   const bemgpu_geom_s *g = t->geom;
@@ -255,6 +269,23 @@ int bemgpu_ctx_stream(bemgpu_ctx_t ctx, void **stream) {
 }
 
 int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx) { return ctx ? ctx->launches : BEMGPU_ERR_ARG; }
+
+int64_t bemgpu_ctx_workspace_bytes(bemgpu_ctx_t ctx) {
+  if (!ctx) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return (int64_t)bem_workspace_bytes(ctx);
+}
+
+int bemgpu_ctx_trim(bemgpu_ctx_t ctx) {
+  if (!ctx) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->ws) cudaFree(kv.second.first);
+  ctx->ws.clear();
+  ctx->tc_err_ready = false;  // the error flag lived in the workspace
+  return BEMGPU_OK;
+}
 
 const char *bemgpu_ctx_last_error(bemgpu_ctx_t ctx) {
   return ctx ? ctx->last_error.c_str() : "null context";

@@ -7,8 +7,17 @@
 // latency-bound LU panels and fill tails of one lane run beside the
 // tensor-core products of another).  Requests wait in a FIFO; results are
 // collected by ticket.  No kernels live here: this file is host C++.
+//
+// Admission by HBM footprint: a lane starts a request only when the
+// request's footprint (bemgpu_solve_footprint) plus what the other lanes hold
+// or have reserved fits the farm's budget (by default 90 % of the device
+// memory free when the farm was created).  A lane that must wait first gives
+// back its own workspace if it holds more than the request needs, then the
+// workspaces of idle lanes; requests wait in ticket order, and a request
+// larger than the whole budget fails with BEMGPU_ERR_OOM at once.
 #include "bemgpu_internal.h"
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -28,6 +37,9 @@ struct FarmJob {
 };
 
 enum JobState { QUEUED, RUNNING, DONE };
+enum LaneState { IDLE, WAITING, BUSY, TRIMMING };
+
+typedef std::chrono::steady_clock Clock;
 
 struct FarmResult {
   JobState state = QUEUED;
@@ -35,7 +47,12 @@ struct FarmResult {
   double P = 0.0;
   bemgpu_solve_info_t info{};
   std::string error;
+  Clock::time_point t_submit, t_start;
 };
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double, std::milli>(b - a).count();
+}
 
 }  // namespace
 
@@ -50,33 +67,118 @@ struct bemgpu_farm_s {
   int64_t next_ticket = 1;
   bool stop = false;
   std::string last_error;
+  // admission
+  size_t budget = 0;
+  std::vector<LaneState> state;
+  std::vector<size_t> held, reserved;  // workspace held; reserved while running
+  std::deque<int64_t> waiters;         // tickets waiting for memory, in order
+  std::condition_variable cv_mem;
 };
 
 namespace {
+
+// Gives back lane l's workspace; called with f->mu held, which it releases
+// while the context synchronises and frees.
+void trim_lane(bemgpu_farm_s *f, int l, std::unique_lock<std::mutex> &lk) {
+  const LaneState was = f->state[l];
+  f->state[l] = TRIMMING;
+  lk.unlock();
+  bemgpu_ctx_trim(f->lanes[l]);
+  lk.lock();
+  f->held[l] = f->reserved[l] = 0;
+  f->state[l] = was;
+  f->cv_mem.notify_all();
+  f->cv_job.notify_all();
+}
+
+// Waits until lane `me` may run a request needing `need` bytes.  Called with
+// f->mu held and the lane in state WAITING.  Returns false if it can never fit.
+bool admit(bemgpu_farm_s *f, int me, int64_t ticket, size_t need, std::unique_lock<std::mutex> &lk) {
+  if (need > f->budget) return false;
+  f->waiters.push_back(ticket);
+  for (;;) {
+    if (f->waiters.front() == ticket) {
+      size_t others = 0;
+      bool running = false;
+      for (int l = 0; l < (int)f->lanes.size(); l++)
+        if (l != me) {
+          others += std::max(f->held[l], f->reserved[l]);
+          running |= f->state[l] == BUSY || f->state[l] == TRIMMING;
+        }
+      if (others + std::max(f->held[me], need) <= f->budget) break;
+      if (f->held[me] > need) {
+        trim_lane(f, me, lk);
+        continue;
+      }
+      int victim = -1;
+      for (int l = 0; l < (int)f->lanes.size(); l++)
+        if (l != me && (f->state[l] == IDLE || f->state[l] == WAITING) && f->held[l] > 0) victim = l;
+      if (victim >= 0) {
+        trim_lane(f, victim, lk);
+        continue;
+      }
+      if (!running) break;  // nothing else holds memory: run (and fail with OOM if it does not fit)
+    }
+    f->cv_mem.wait(lk);
+  }
+  f->waiters.pop_front();
+  f->reserved[me] = std::max(f->held[me], need);
+  f->cv_mem.notify_all();
+  return true;
+}
 
 void lane_main(bemgpu_farm_s *f, int lane) {
   bemgpu_ctx_t ctx = f->lanes[lane];
   for (;;) {
     FarmJob job;
+    bool ok;
     {
       std::unique_lock<std::mutex> lk(f->mu);
-      f->cv_job.wait(lk, [f] { return f->stop || !f->queue.empty(); });
+      f->cv_job.wait(lk, [f, lane] { return (f->stop || !f->queue.empty()) && f->state[lane] != TRIMMING; });
       if (f->queue.empty()) return;  // stopping, nothing left
       job = f->queue.front();
       f->queue.pop_front();
-      f->results[job.ticket].state = RUNNING;
+      f->state[lane] = WAITING;
+      const int64_t need = bemgpu_solve_footprint(job.s->nrwg, job.t->nrwg, job.precision);
+      ok = admit(f, lane, job.ticket, (size_t)need, lk);
+      f->state[lane] = ok ? BUSY : IDLE;
+      FarmResult &r = f->results[job.ticket];
+      r.state = RUNNING;
+      r.t_start = Clock::now();
+      if (!ok) {
+        r.state = DONE;
+        r.status = BEMGPU_ERR_OOM;
+        char buf[160];
+        snprintf(buf, sizeof buf, "farm: the request needs %.2f GB, more than the farm's budget of %.2f GB",
+                 need / 1e9, f->budget / 1e9);
+        r.error = buf;
+      }
+    }
+    if (!ok) {
+      f->cv_done.notify_all();
+      continue;
     }
     double P = 0.0;
     bemgpu_solve_info_t info{};
     const int rc = bemgpu_heat_transfer(ctx, job.top, job.s, job.t, &job.req, &job.opt, job.precision, &P, &info);
+    const size_t held = (size_t)std::max<int64_t>(0, bemgpu_ctx_workspace_bytes(ctx));
     {
-      std::lock_guard<std::mutex> lk(f->mu);
+      std::unique_lock<std::mutex> lk(f->mu);
       FarmResult &r = f->results[job.ticket];
       r.state = DONE;
       r.status = rc;
       r.P = P;
       r.info = info;
+      const Clock::time_point now = Clock::now();
+      r.info.ms_queued = ms_between(r.t_submit, r.t_start);
+      r.info.ms_latency = ms_between(r.t_submit, now);
       if (rc != BEMGPU_OK) r.error = bemgpu_ctx_last_error(ctx);
+      f->held[lane] = held;
+      f->reserved[lane] = 0;
+      f->state[lane] = IDLE;
+      // a request waiting for memory gets this lane's workspace
+      if (!f->waiters.empty() && held > 0) trim_lane(f, lane, lk);
+      f->cv_mem.notify_all();
     }
     f->cv_done.notify_all();
   }
@@ -101,6 +203,13 @@ int bemgpu_farm_create(int device, int lanes, bemgpu_farm_t *out) {
     }
     f->lanes.push_back(c);
   }
+  size_t fr = 0, tot = 0;
+  cudaSetDevice(device);
+  cudaMemGetInfo(&fr, &tot);
+  f->budget = (size_t)(0.9 * (double)fr);
+  f->state.assign(lanes, IDLE);
+  f->held.assign(lanes, 0);
+  f->reserved.assign(lanes, 0);
   for (int i = 0; i < lanes; i++) f->threads.emplace_back(lane_main, f, i);
   *out = f;
   return BEMGPU_OK;
@@ -127,6 +236,22 @@ int bemgpu_farm_destroy(bemgpu_farm_t f) {
 }
 
 int bemgpu_farm_lanes(bemgpu_farm_t f) { return f ? (int)f->lanes.size() : BEMGPU_ERR_ARG; }
+
+int bemgpu_farm_set_budget(bemgpu_farm_t f, int64_t bytes) {
+  if (!f || bytes <= 0) return BEMGPU_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(f->mu);
+    f->budget = (size_t)bytes;
+  }
+  f->cv_mem.notify_all();
+  return BEMGPU_OK;
+}
+
+int64_t bemgpu_farm_budget(bemgpu_farm_t f) {
+  if (!f) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(f->mu);
+  return (int64_t)f->budget;
+}
 
 int bemgpu_farm_lane_ctx(bemgpu_farm_t f, int lane, bemgpu_ctx_t *ctx) {
   if (!f || !ctx || lane < 0 || lane >= (int)f->lanes.size()) return BEMGPU_ERR_ARG;
@@ -164,6 +289,7 @@ int bemgpu_farm_submit(bemgpu_farm_t f, bemgpu_tree_t top, bemgpu_tree_t s, bemg
     if (f->stop) return BEMGPU_ERR_ARG;
     j.ticket = f->next_ticket++;
     f->results[j.ticket] = FarmResult();
+    f->results[j.ticket].t_submit = Clock::now();
     f->queue.push_back(j);
     *ticket = j.ticket;
   }

@@ -388,6 +388,13 @@ bool ex_maps(CUtensorMap *maps, const __nv_bfloat16 *S, int slices, int64_t rows
 
 bool bem_exact_available() { return encode_fn() != nullptr; }
 
+size_t bem_exact_operand_bytes(bool is_a, int rows, int k, int slices) {
+  const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
+                          : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
+  const int64_t kp = ((2 * (int64_t)k + 127) / 128) * 128;
+  return sizeof(__nv_bfloat16) * (size_t)slices * rp * kp + 64;
+}
+
 int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
                    double sign, int slices, ExactOperand &op, cudaStream_t st) {
   if (slices < 3 || slices > 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);

@@ -467,6 +467,14 @@ int bem_tc_error(bemgpu_ctx_s *ctx, bool reset) {
 // C (+)= sign * A B on the tensor cores.  out: TC_OUT_F32 (complex64 C),
 // TC_OUT_F64 (complex128 C, FP32 accumulation), TC_OUT_F64_COMP (complex128
 // C, per-K-step FP32 sums accumulated as two-float sums).  Column-major, ldc.
+void bem_cgemm_tc_bytes(int m, int n, int k, size_t &a_bytes, size_t &b_bytes) {
+  const int64_t Mp = ((2 * (int64_t)m + TC_BM - 1) / TC_BM) * TC_BM;
+  const int64_t Np = (((int64_t)n + TC_BN - 1) / TC_BN) * TC_BN;
+  const int64_t Kp = ((2 * (int64_t)k + TC_BK - 1) / TC_BK) * TC_BK;
+  a_bytes = sizeof(__nv_bfloat16) * TC_SLICES * (size_t)(Mp * Kp);
+  b_bytes = sizeof(__nv_bfloat16) * TC_SLICES * (size_t)(Np * Kp);
+}
+
 int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, const float *A, int64_t lda,
                  const float *B, int64_t ldb, void *C, int64_t ldc, int out, int accumulate, cudaStream_t st,
                  int tri) {

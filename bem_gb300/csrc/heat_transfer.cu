@@ -91,6 +91,46 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 }  // namespace
 
+namespace {
+
+// Device bytes of the solve-phase buffers (everything allocated after the
+// fill and gather), mirroring the allocation sites in mixed.cu, dense.cu,
+// gemm_tc.cu and gemm_exact.cu (mixed path) or below (FP64 path).
+size_t solve_phase_bytes(int Ns, int Nt, int precision) {
+  const size_t N = (size_t)Ns + Nt, n = 2 * N, ns2 = 2 * (size_t)Ns, nt2 = 2 * (size_t)Nt;
+  const size_t nn = n * n, nm = n * nt2, st2 = ns2 * nt2;
+  const size_t scratch = 8u << 20;  // LU panel candidates and rows (coop_*), flags, trace partials
+  if (precision == BEMGPU_PREC_FP64)
+    return 16 * nm + 2 * 16 * st2 + 4 * n + scratch;
+  size_t b = 3 * 8 * nn + 2 * 8 * nm + 16 * (ns2 * ns2 + nt2 * nt2) + 3 * 16 * nm + 3 * 16 * st2;
+  b += 4 * n + 16 * (((ns2 + 31) / 32) * ((nt2 + 31) / 32)) + 1024;
+  // exact operands: -W, H1, H2 (5 slices), the iterate Y, the trace's X and X^H
+  b += bem_exact_operand_bytes(true, (int)n, (int)n, 5) + bem_exact_operand_bytes(true, (int)ns2, (int)ns2, 5) +
+       bem_exact_operand_bytes(true, (int)nt2, (int)nt2, 5) + bem_exact_operand_bytes(false, (int)nt2, (int)n, 5) +
+       bem_exact_operand_bytes(false, (int)nt2, (int)ns2, 5) + bem_exact_operand_bytes(false, (int)ns2, (int)nt2, 5);
+  // bf16x3 slice planes: the largest product is the application of L^-1 / U^-1
+  // to the n x nt2 right-hand sides; the triangular inverses' halves are smaller
+  size_t a1, b1, a2, b2;
+  bem_cgemm_tc_bytes((int)n, (int)nt2, (int)n, a1, b1);
+  bem_cgemm_tc_bytes((int)(n / 2 + 64), (int)(n / 2 + 64), (int)(n / 2 + 64), a2, b2);
+  b += std::max(a1, a2) + std::max(b1, b2);
+  b += 8 * (n / 2 + 64) * (n / 2 + 64);  // triangular-inverse scratch
+  b += scratch;
+  return b;
+}
+
+size_t fill_phase_bytes(int Ns, int Nt) {
+  const size_t N = (size_t)Ns + Nt, n = 2 * N, ns2 = 2 * (size_t)Ns, nt2 = 2 * (size_t)Nt;
+  return sizeof(HalfPairBlock) * (N * N + (size_t)Ns * Ns + (size_t)Nt * Nt) + 16 * (n * n + ns2 * ns2 + nt2 * nt2);
+}
+
+}  // namespace
+
+extern "C" int64_t bemgpu_solve_footprint(int nrwg_s, int nrwg_t, int precision) {
+  if (nrwg_s < 1 || nrwg_t < 1) return BEMGPU_ERR_ARG;
+  return (int64_t)(fill_phase_bytes(nrwg_s, nrwg_t) + solve_phase_bytes(nrwg_s, nrwg_t, precision));
+}
+
 extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
                                     const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
                                     double *P_out, bemgpu_solve_info_t *info) {
@@ -138,6 +178,20 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   if (!rc) rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st);
   if (rc) return rc;
   cudaEventRecord(ev[7], st);
+  {
+    // The half-pair blocks are dead once W, G1, G2 are gathered.  When the
+    // solve phase would not fit beside them, give them back first (large
+    // solves); otherwise keep them for the next request of this size.
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    const size_t held = bem_workspace_bytes(ctx), need = solve_phase_bytes(Ns, Nt, precision);
+    const size_t hb = sizeof(HalfPairBlock) * ((size_t)N * N + (size_t)Ns * Ns + (size_t)Nt * Nt);
+    if (held + fr < hb + 16 * ((size_t)n * n + (size_t)ns2 * ns2 + (size_t)nt2 * nt2) + need + (256u << 20)) {
+      bem_workspace_release(ctx, "Hext");
+      bem_workspace_release(ctx, "Hint1");
+      bem_workspace_release(ctx, "Hint2");
+    }
+  }
   if (precision != BEMGPU_PREC_FP64) {
     bemgpu_solve_info_t mi;
     memset(&mi, 0, sizeof mi);

@@ -79,6 +79,7 @@ typedef struct {
   double err_est;           /* estimated relative error of Re S (0 on the FP64 path) */
   int refine_iters;
   int64_t pairs_near, pairs_far_fp64, pairs_far_fp32;
+  double ms_queued, ms_latency; /* farm requests: submit -> start and submit -> done, host clock */
 } bemgpu_solve_info_t;
 
 /* ---- context ---- */
@@ -93,6 +94,14 @@ const char *bemgpu_version(void);
 int bemgpu_ctx_stream(bemgpu_ctx_t ctx, void **stream);
 /* Number of kernels the context launched since it was created. */
 int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx);
+/* Bytes of device workspace the context holds (it grows to the largest solve
+ * seen and is kept for the next one), and giving all of it back. */
+int64_t bemgpu_ctx_workspace_bytes(bemgpu_ctx_t ctx);
+int bemgpu_ctx_trim(bemgpu_ctx_t ctx);
+/* Device bytes one CalcHeatTransfer solve needs at most (fill scratch plus
+ * solve buffers) for bodies of nrwg_s and nrwg_t RWGs: the admission figure of
+ * the request farm.  No reference counterpart. */
+int64_t bemgpu_solve_footprint(int nrwg_s, int nrwg_t, int precision);
 /* Engines of the complex64 products: gemm = LU and correction solves,
  * acc64 = refinement residual and trace (FP64 output); 0 = the library's
  * choice (tensor cores where the shape allows), 1 = tensor cores where the
@@ -211,6 +220,10 @@ int bemgpu_farm_create(int device, int lanes, bemgpu_farm_t *out);
  * waits for the running ones, and frees the lanes. */
 int bemgpu_farm_destroy(bemgpu_farm_t farm);
 int bemgpu_farm_lanes(bemgpu_farm_t farm);
+/* Device bytes the lanes may hold together (admission by footprint); the
+ * default is 90 % of the memory free when the farm was created. */
+int bemgpu_farm_set_budget(bemgpu_farm_t farm, int64_t bytes);
+int64_t bemgpu_farm_budget(bemgpu_farm_t farm);
 /* The context of one lane (for bemgpu_prof_* and bemgpu_ctx_launches). */
 int bemgpu_farm_lane_ctx(bemgpu_farm_t farm, int lane, bemgpu_ctx_t *ctx);
 /* Queues one CalcHeatTransfer request (the arguments of bemgpu_heat_transfer;

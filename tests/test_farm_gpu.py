@@ -74,3 +74,74 @@ def test_farm_destroy_drops_queued_requests():
         farm.submit(1e-6, f, 300.0, 0.0, *systems[0], precision=_lib.PREC_MIXED_LA)
     farm.close()  # returns after the running request; the queued ones are dropped
     assert farm.handle is None
+
+
+def _system_level(level, gap):
+    v, t = mesh.icosphere(1.0, level, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    return api.parseShapes(b2.translated(mesh.gap_translation(v, v, gap)), b2, d, d)
+
+
+def test_uneven_sizes_same_alone_and_in_the_mix():
+    """Requests of different N (icospheres L1 and L2, two gaps) interleaved on
+    three lanes give exactly the spectral power each gives alone."""
+    systems = [_system_level(1, 0.05), _system_level(2, 0.1), _system_level(1, 0.3), _system_level(2, 0.02)]
+    jobs = [(1e-6, f, 300.0, 0.0, *systems[i % 4]) for i, f in enumerate(np.linspace(0.085, 0.125, 8))]
+    alone = [api.CalcHeatTransfer(*j, precision=_lib.PREC_MIXED_LA, strict=False) for j in jobs]
+    with api.Farm(3) as farm:
+        infos = []
+        mixed = farm.map(jobs, precision=_lib.PREC_MIXED_LA, strict=False, infos=infos)
+    assert mixed == alone
+    assert all(i["ms_latency"] >= i["ms_queued"] >= 0 for i in infos)
+
+
+def test_footprint_bounds_the_workspace():
+    """bemgpu_solve_footprint is the admission figure: it must cover what a
+    solve allocates, without overstating it by much."""
+    L = _lib.load()
+    for level, prec in ((1, _lib.PREC_FP64), (2, _lib.PREC_FP64), (2, _lib.PREC_MIXED_LA)):
+        ctx = api.Context(0)
+        top2, s2, t2 = api.parseShapes(*_bodies(level, 0.1), api.FixedLorentz(*api.SIC_CONFIG),
+                                       api.FixedLorentz(*api.SIC_CONFIG), ctx)
+        api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top2, s2, t2, precision=prec, strict=False)
+        held = L.bemgpu_ctx_workspace_bytes(ctx.handle)
+        fp = api.solve_footprint(s2, t2, prec)
+        assert held <= fp <= 1.5 * held + (64 << 20), (level, prec, held, fp)
+        assert L.bemgpu_ctx_trim(ctx.handle) == 0 and L.bemgpu_ctx_workspace_bytes(ctx.handle) == 0
+        # a trimmed context solves again and gives the same answer
+        P1 = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top2, s2, t2, precision=prec, strict=False)
+        L.bemgpu_ctx_trim(ctx.handle)
+        P2 = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top2, s2, t2, precision=prec, strict=False)
+        assert P1 == P2
+        del top2, s2, t2
+        ctx.close()
+
+
+def _bodies(level, gap):
+    v, t = mesh.icosphere(1.0, level, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    return b2.translated(mesh.gap_translation(v, v, gap)), b2
+
+
+def test_admission_by_footprint():
+    """A budget that holds one solve at a time serialises the lanes (same
+    results); a request larger than the budget fails with BEMGPU_ERR_OOM."""
+    small = _system_level(1, 0.1)
+    big = _system_level(2, 0.1)
+    fp_big = api.solve_footprint(big[1], big[2], _lib.PREC_MIXED_LA)
+    fp_small = api.solve_footprint(small[1], small[2], _lib.PREC_MIXED_LA)
+    jobs = [(1e-6, f, 300.0, 0.0, *(big if i % 2 else small)) for i, f in enumerate(np.linspace(0.09, 0.12, 6))]
+    alone = [api.CalcHeatTransfer(*j, precision=_lib.PREC_MIXED_LA, strict=False) for j in jobs]
+    with api.Farm(3) as farm:
+        farm.budget = fp_big + fp_small // 2   # room for one large solve and half a small one
+        assert farm.budget == fp_big + fp_small // 2
+        got = farm.map(jobs, precision=_lib.PREC_MIXED_LA, strict=False)
+        assert got == alone
+        farm.budget = fp_big // 2
+        tk = farm.submit(*jobs[1], precision=_lib.PREC_MIXED_LA)
+        with pytest.raises(_lib.BemGpuError) as e:
+            farm.result(tk)
+        assert e.value.code == _lib.ERR_OOM
+        farm.budget = 4 * fp_big
+        assert farm.result(farm.submit(*jobs[1], precision=_lib.PREC_MIXED_LA), strict=False) == alone[1]
