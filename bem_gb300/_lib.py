@@ -37,6 +37,7 @@ EXPORTED = [
     "bemgpu_farm_create", "bemgpu_farm_destroy", "bemgpu_farm_lanes", "bemgpu_farm_lane_ctx", "bemgpu_farm_submit",
     "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error", "bemgpu_farm_set_budget",
     "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint",
+    "bemgpu_ctx_set_solver",
 ]
 
 
@@ -62,7 +63,7 @@ class SolveInfo(ctypes.Structure):
                 ("S_re", ctypes.c_double), ("S_im", ctypes.c_double), ("err_est", ctypes.c_double),
                 ("refine_iters", ctypes.c_int),
                 ("pairs_near", ctypes.c_int64), ("pairs_far_fp64", ctypes.c_int64), ("pairs_far_fp32", ctypes.c_int64),
-                ("ms_queued", ctypes.c_double), ("ms_latency", ctypes.c_double)]
+                ("ms_queued", ctypes.c_double), ("ms_latency", ctypes.c_double), ("solver", ctypes.c_int)]
 
 
 _lib = None
@@ -117,6 +118,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_ctx_workspace_bytes": (i64, [vp]),
         "bemgpu_ctx_trim": (i32, [vp]),
         "bemgpu_solve_footprint": (i64, [i32, i32, i32]),
+        "bemgpu_ctx_set_solver": (i32, [vp, i32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

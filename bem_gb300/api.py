@@ -56,6 +56,12 @@ class Context:
         self.handle = h
         self.device = device
 
+    def set_solver(self, mode: int):
+        """Mixed-path factorization: 0 complex64 LU escalating to the FP64-class
+        tensor-core LU when refinement does not converge, 1 complex64 only, 2
+        FP64-class only."""
+        _check(_lib.load().bemgpu_ctx_set_solver(self.handle, int(mode)), self)
+
     def close(self):
         if self.handle:
             _lib.load().bemgpu_ctx_destroy(self.handle)

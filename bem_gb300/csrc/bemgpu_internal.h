@@ -94,6 +94,7 @@ struct bemgpu_ctx_s {
   bool coop_panel = true;  // LU panels in one cooperative launch (else one launch per column)
   int gemm_engine = 0;   // complex64 LU/solve GEMMs: 0 tensor cores where possible, 2 FMA pipes only
   int acc_engine = 0;    // residual/trace GEMMs with FP64 output: same choices
+  int solver = 0;        // mixed path: 0 complex64 with FP64-class escalation, 1 complex64, 2 FP64-class
   // live kernel statistics
   bool prof = false;
   struct ProfRec {
@@ -184,6 +185,12 @@ int bem_zgetrf(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, in
 // B (n x nrhs) <- A^{-1} B using the LU factors and pivots of bem_zgetrf.
 int bem_zgetrs(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int *d_ipiv, double *B,
                int64_t ldb, int nrhs, cudaStream_t stream);
+// FP64-class LU and solve on the tensor cores: FP64 panels and diagonal
+// blocks, every trailing / off-diagonal update a 5-slice exact product.
+int bem_zgetrf_exact(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, int *d_info,
+                     cudaStream_t stream);
+int bem_zgetrs_exact(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int *d_ipiv, double *B,
+                     int64_t ldb, int nrhs, cudaStream_t stream);
 // complex64 versions (mixed path).
 int bem_cgetrf(bemgpu_ctx_s *ctx, float *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream);
 int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int *d_ipiv, float *B, int64_t ldb,
@@ -247,5 +254,5 @@ int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const 
 
 // ---- mixed-precision solve (mixed.cu) ----
 // W (FP64, n x n, ld n), G1 (ns2 x ns2), G2 ((n-ns2) x (n-ns2)) as filled; writes S = 1/4 Tr(B2^H B1).
-int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const double *G1, const double *G2,
+int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
                     cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info);

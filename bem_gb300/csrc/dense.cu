@@ -765,7 +765,8 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
 }
 
 template <typename T>
-int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
+int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream,
+               bool exact = false) {
   if (int rc0 = set_trsm_attrs<T>(ctx)) return rc0;
   PivCand *cand = (PivCand *)bem_workspace(ctx, "lu_cand", sizeof(PivCand) * 1024);
   unsigned int *counter = (unsigned int *)bem_workspace(ctx, "lu_counter", sizeof(unsigned int));
@@ -814,7 +815,17 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
       }
       T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
       T *A22 = A + 2 * (k0 + w + lda * (int64_t)(k0 + w));
-      int rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
+      int rc;
+      if (exact && sizeof(T) == 8) {
+        // FP64-class trailing update on the tensor cores: A22 -= A21 A12 as a
+        // 5-slice exact product (complex128 in and out)
+        ExactOperand oa, ob;
+        rc = bem_exact_prep(ctx, "lu_L", true, (const double *)A21, lda, nr, w, -1.0, 5, oa, stream);
+        if (!rc) rc = bem_exact_prep(ctx, "lu_U", false, (const double *)A12, lda, nr, w, 1.0, 5, ob, stream);
+        if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_LU_GEMM, oa, ob, (double *)A22, lda, 1, stream);
+      } else {
+        rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
+      }
       if (rc) return rc;
     }
     BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -882,6 +893,62 @@ int bem_zgetrs(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int
                int nrhs, cudaStream_t stream) {
   return getrs_impl<double>(ctx, A, lda, n, d_ipiv, B, ldb, nrhs, stream);
 }
+int bem_zgetrf_exact(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
+  return getrf_impl<double>(ctx, A, lda, n, d_ipiv, d_info, stream, true);
+}
+
+// B <- A^{-1} B with the factors of bem_zgetrf_exact: row interchanges, then
+// blocked forward / back substitution; each 64 x 64 diagonal block is solved
+// in FP64 (trsm_block_kernel) and the off-diagonal block updates are 5-slice
+// exact tensor-core products, so the solve keeps FP64-class accuracy.
+int bem_zgetrs_exact(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int *d_ipiv, double *B, int64_t ldb,
+                     int nrhs, cudaStream_t stream) {
+  if (int rc0 = set_trsm_attrs<double>(ctx)) return rc0;
+  {
+    ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 64.0 * n * (double)nrhs);
+    laswp_kernel<double><<<(nrhs + 127) / 128, 128, 0, stream>>>(B, ldb, 0, nrhs, 0, n, d_ipiv);
+    ctx->launches++;
+  }
+  const int tb = std::min((nrhs + 7) / 8, ctx->num_sms * 4);
+  int rc = BEMGPU_OK;
+  for (int k0 = 0; k0 < n && !rc; k0 += NB) {  // forward: L Y = P B (unit lower)
+    const int w = std::min(NB, n - k0);
+    double *Bk = B + 2 * (int64_t)k0;
+    {
+      ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nrhs, 32.0 * w * nrhs);
+      trsm_block_kernel<double, false, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), stream>>>(
+          A + 2 * (k0 + lda * (int64_t)k0), lda, w, Bk, ldb, nrhs);
+      ctx->launches++;
+    }
+    if (k0 + w < n) {
+      ExactOperand oa, ob;
+      rc = bem_exact_prep(ctx, "rs_L", true, A + 2 * (k0 + w + lda * (int64_t)k0), lda, n - k0 - w, w, -1.0, 5, oa,
+                          stream);
+      if (!rc) rc = bem_exact_prep(ctx, "rs_B", false, Bk, ldb, nrhs, w, 1.0, 5, ob, stream);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_SOLVE_GEMM, oa, ob, B + 2 * (int64_t)(k0 + w), ldb, 1, stream);
+    }
+  }
+  const int nblk = (n + NB - 1) / NB;
+  for (int bi = nblk - 1; bi >= 0 && !rc; bi--) {  // backward: U X = Y
+    const int k0 = bi * NB, w = std::min(NB, n - k0);
+    double *Bk = B + 2 * (int64_t)k0;
+    {
+      ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nrhs, 32.0 * w * nrhs);
+      trsm_block_kernel<double, true, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), stream>>>(
+          A + 2 * (k0 + lda * (int64_t)k0), lda, w, Bk, ldb, nrhs);
+      ctx->launches++;
+    }
+    if (k0 > 0) {
+      ExactOperand oa, ob;
+      rc = bem_exact_prep(ctx, "rs_L", true, A + 2 * (lda * (int64_t)k0), lda, k0, w, -1.0, 5, oa, stream);
+      if (!rc) rc = bem_exact_prep(ctx, "rs_B", false, Bk, ldb, nrhs, w, 1.0, 5, ob, stream);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_SOLVE_GEMM, oa, ob, B, ldb, 1, stream);
+    }
+  }
+  if (!rc) BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return rc;
+}
+
 int bem_cgetrf(bemgpu_ctx_s *ctx, float *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
   return getrf_impl<float>(ctx, A, lda, n, d_ipiv, d_info, stream);
 }

@@ -622,6 +622,14 @@ extern "C" int bemgpu_cgemm_acc64(bemgpu_ctx_t ctx, int m, int n, int k, const f
   return BEMGPU_OK;
 }
 
+extern "C" int bemgpu_ctx_set_solver(bemgpu_ctx_t ctx, int mode) {
+  if (!ctx || mode < 0 || mode > 2)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "set_solver: modes are 0 (complex64, escalating), 1 (complex64), 2 (FP64-class)");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->solver = mode;
+  return BEMGPU_OK;
+}
+
 extern "C" int bemgpu_ctx_set_engines(bemgpu_ctx_t ctx, int gemm, int acc64) {
   if (!ctx || gemm < 0 || gemm > 2 || acc64 < 0 || acc64 > 2)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "set_engines: engines are 0 (choice), 1 (tensor cores), 2 (FMA pipes)");

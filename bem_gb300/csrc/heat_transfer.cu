@@ -185,8 +185,11 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     const size_t held = bem_workspace_bytes(ctx), need = solve_phase_bytes(Ns, Nt, precision);
-    const size_t hb = sizeof(HalfPairBlock) * ((size_t)N * N + (size_t)Ns * Ns + (size_t)Nt * Nt);
-    if (held + fr < hb + 16 * ((size_t)n * n + (size_t)ns2 * ns2 + (size_t)nt2 * nt2) + need + (256u << 20)) {
+    const size_t fill = fill_phase_bytes(Ns, Nt);
+    // solve-phase bytes not yet held (what the context holds beyond the fill
+    // buffers is solve-phase workspace of an earlier request)
+    const size_t missing = need - std::min(need, held > fill ? held - fill : (size_t)0);
+    if ((double)fr < 1.05 * (double)missing + (double)(1u << 30)) {
       bem_workspace_release(ctx, "Hext");
       bem_workspace_release(ctx, "Hint1");
       bem_workspace_release(ctx, "Hint2");

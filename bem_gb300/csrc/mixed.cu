@@ -139,6 +139,38 @@ __global__ void residual_finish_kernel(const double *__restrict__ R64, float *__
   reinterpret_cast<float2 *>(R32)[idx] = make_float2((float)v.x, (float)v.y);
 }
 
+// D = E_t + R64 in FP64 (the residual the FP64-class solve corrects with).
+__global__ void residual_fp64_kernel(const double *__restrict__ R64, double *__restrict__ D, int64_t ld, int n,
+                                     int row0) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (r >= n) return;
+  const int64_t idx = r + ld * (int64_t)c;
+  double2 v = reinterpret_cast<const double2 *>(R64)[idx];
+  if (r == row0 + c) v.x += 1.0;
+  reinterpret_cast<double2 *>(D)[idx] = v;
+}
+
+// Y += D (FP64).
+__global__ void add_fp64_kernel(double *__restrict__ Y, const double *__restrict__ D, int64_t ld, int n) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (r >= n) return;
+  const int64_t idx = r + ld * (int64_t)c;
+  double2 y = reinterpret_cast<double2 *>(Y)[idx];
+  const double2 d = reinterpret_cast<const double2 *>(D)[idx];
+  y.x += d.x;
+  y.y += d.y;
+  reinterpret_cast<double2 *>(Y)[idx] = y;
+}
+
+__global__ void identity_cols_c128_kernel(double *Y, int64_t ld, int n, int row0) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (r >= n) return;
+  reinterpret_cast<double2 *>(Y)[r + ld * (int64_t)c] = make_double2(r == row0 + c ? 1.0 : 0.0, 0.0);
+}
+
 __global__ void identity_cols_c64_kernel(float *Y, int64_t ld, int n, int row0, int ncols) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
@@ -225,7 +257,64 @@ int spectral_trace(bemgpu_ctx_s *ctx, MixedBufs &b, int n, int ns2, int nt2, cud
 
 }  // namespace
 
-int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const double *G1, const double *G2,
+namespace {
+
+// The FP64-class solve: W (already sliced into b.opW) is factored in place by
+// the tensor-core LU of FP64 accuracy (bem_zgetrf_exact), Y0 = W^-1 E_t by its
+// blocked solve, then the same refinement and trace as the complex64 path with
+// FP64 corrections.  Used when the complex64 factorization is not accurate
+// enough for the refinement to converge (ill-conditioned W), or on request.
+int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cudaStream_t st, double S[2],
+                 int &iters, double &err) {
+  const int nt2 = n - ns2;
+  const dim3 gm((n + 255) / 256, nt2);
+  int rc = bem_zgetrf_exact(ctx, W, n, n, b.ipiv, b.info, st);
+  if (rc) return rc;
+  int hinfo = 0;
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, b.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if (hinfo != 0) return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "FP64-class LU: zero pivot at column %d", hinfo);
+  identity_cols_c128_kernel<<<gm, 256, 0, st>>>(b.Y, n, n, ns2);
+  ctx->launches++;
+  rc = bem_zgetrs_exact(ctx, W, n, n, b.ipiv, b.Y, n, nt2, st);
+  if (rc) return rc;
+  double Sprev[2] = {0, 0};
+  rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, false);
+  if (rc) return rc;
+  err = 1.0;
+  double err_prev = 1.0;
+  for (iters = 1; iters <= 3; iters++) {
+    ExactOperand opY;
+    if (iters == 1) {
+      rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, MIXED_SLICES, opY, st);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
+    } else {
+      rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opY, st);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 1, st);
+    }
+    if (rc) return rc;
+    residual_fp64_kernel<<<gm, 256, 0, st>>>(b.R64, b.dY, n, n, ns2);
+    ctx->launches++;
+    rc = bem_zgetrs_exact(ctx, W, n, n, b.ipiv, b.dY, n, nt2, st);
+    if (rc) return rc;
+    add_fp64_kernel<<<gm, 256, 0, st>>>(b.Y, b.dY, n, n);
+    ctx->launches++;
+    Sprev[0] = S[0];
+    Sprev[1] = S[1];
+    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, true);
+    if (rc) return rc;
+    if (bem_tc_error(ctx, true))
+      return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "FP64-class solve: a tensor-core pipeline wait ran out");
+    err_prev = err;
+    err = fabs(S[0] - Sprev[0]) / fmax(fabs(S[0]), 1e-300);
+    if (err < 3e-7 || err > 0.5 * err_prev) break;
+  }
+  return BEMGPU_OK;
+}
+
+}  // namespace
+
+int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
                     cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info) {
   if (!bem_exact_available())
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "mixed solve: tensor-map encoding (driver entry point) unavailable");
@@ -270,6 +359,24 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   if (!rc) rc = bem_exact_prep(ctx, "H2", true, b.H2, nt2, nt2, nt2, 1.0, MIXED_SLICES, b.opH2, st);
   if (rc) return rc;
   cudaEventRecord(ev[1], st);
+  if (ctx->solver == 2) {
+    double S[2] = {0, 0}, err = 1.0;
+    int iters = 0;
+    rc = fp64lu_solve(ctx, W, n, ns2, b, st, S, iters, err);
+    if (rc) return rc;
+    cudaEventRecord(ev[5], st);
+    BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    S_out[0] = S[0];
+    S_out[1] = S[1];
+    if (info) {
+      info->ms_lu = ev_ms(ev[1], ev[5]);
+      info->err_est = err;
+      info->refine_iters = iters;
+      info->solver = 2;
+    }
+    if (err > 1e-6) return bem_fail(ctx, BEMGPU_ERR_NO_CONVERGE, "FP64-class solve: refinement stalled at %.2e", err);
+    return BEMGPU_OK;
+  }
   rc = bem_cgetrf(ctx, b.W32, n, n, b.ipiv, b.info, st);
   if (!rc) rc = bem_ctri_inverses(ctx, b.W32, n, n, b.Linv, b.Uinv, st);
   if (rc) return rc;
@@ -284,12 +391,13 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
   int hinfo = 0;
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, b.info, sizeof(int), cudaMemcpyDeviceToHost, st));
   BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-  if (hinfo != 0) return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "mixed solve: zero pivot at column %d", hinfo);
+  if (hinfo != 0 && ctx->solver != 0)
+    return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "mixed solve: zero pivot at column %d", hinfo);
   cudaEventRecord(ev[4], st);
   double Sprev[2] = {0, 0}, S[2] = {0, 0};
   int iters = 0;
-  double err = 1.0, err_prev = 1.0;
-  const int max_iters = 4;
+  double err = hinfo ? 1e300 : 1.0, err_prev = 1.0;
+  const int max_iters = hinfo ? 0 : 4;
   while (iters < max_iters) {
     // R = E_t - W Y: R64 holds -W Y; the first step forms it from Y, later
     // steps add -W dY of the last correction (3-slice product)
@@ -321,6 +429,15 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
     // converged, or stalled at the accuracy floor of the residual
     if (err < 3e-7 || err > 0.5 * err_prev) break;
   }
+  int solver = 1;
+  if (ctx->solver == 0 && !(err <= 1e-6)) {
+    // the complex64 factors are not accurate enough for this W (refinement
+    // diverged or stalled above the tolerance, or a zero pivot): factor W in
+    // FP64-class arithmetic on the tensor cores and refine with that
+    rc = fp64lu_solve(ctx, W, n, ns2, b, st, S, iters, err);
+    if (rc) return rc;
+    solver = 2;
+  }
   cudaEventRecord(ev[5], st);
   BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
   S_out[0] = S[0];
@@ -332,6 +449,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, const double *W, int n, int ns2, const do
     info->ms_refine = ev_ms(ev[4], ev[5]);
     info->err_est = err;
     info->refine_iters = iters;
+    info->solver = solver;
   }
   if (err > 1e-6) return bem_fail(ctx, BEMGPU_ERR_NO_CONVERGE, "mixed solve: refinement stalled at %.2e", err);
   return BEMGPU_OK;

@@ -80,6 +80,7 @@ typedef struct {
   int refine_iters;
   int64_t pairs_near, pairs_far_fp64, pairs_far_fp32;
   double ms_queued, ms_latency; /* farm requests: submit -> start and submit -> done, host clock */
+  int solver;                   /* mixed path: 1 complex64 LU, 2 FP64-class tensor-core LU */
 } bemgpu_solve_info_t;
 
 /* ---- context ---- */
@@ -107,6 +108,10 @@ int64_t bemgpu_solve_footprint(int nrwg_s, int nrwg_t, int precision);
  * choice (tensor cores where the shape allows), 1 = tensor cores where the
  * shape allows, 2 = FMA pipes only.  No reference counterpart (tuning). */
 int bemgpu_ctx_set_engines(bemgpu_ctx_t ctx, int gemm, int acc64);
+/* Factorization of the mixed path: 0 = complex64 LU, escalating to the
+ * FP64-class tensor-core LU when its refinement does not converge (default);
+ * 1 = complex64 only; 2 = FP64-class only.  No reference counterpart. */
+int bemgpu_ctx_set_solver(bemgpu_ctx_t ctx, int mode);
 
 /* ---- live kernel statistics (measurement hooks; no counterpart in the reference) ---- */
 /* Kernel classes timed with CUDA events on the context stream while enabled. */

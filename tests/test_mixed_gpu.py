@@ -87,3 +87,27 @@ def test_mixed_same_result_twice():
     a = api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, t, precision=_lib.PREC_MIXED_LA)
     b = api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, t, precision=_lib.PREC_MIXED_LA)
     assert a == b
+
+
+def test_fp64_class_tensor_core_lu_matches_fp64_path():
+    """The FP64-class factorization (LU and blocked solves whose updates are
+    5-slice exact tensor-core products) gives the FP64 path's spectral power to
+    the plain path's own bar, and the escalating default stays on complex64
+    for a well-conditioned system."""
+    v, t = mesh.icosphere(1.0, 2, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    b1 = b2.translated(mesh.gap_translation(v, v, 0.05))
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    ctx = api.Context(0)
+    top, s, tt = api.parseShapes(b1, b2, d, d, ctx)
+    for eV in (0.09, 0.117):
+        P64 = api.CalcHeatTransfer(1e-6, eV, 300.0, 0.0, top, s, tt, precision=_lib.PREC_FP64)
+        ctx.set_solver(2)
+        info = {}
+        P2 = api.CalcHeatTransfer(1e-6, eV, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+        assert info["solver"] == 2 and info["err_est"] < 1e-6
+        assert abs(P2 / P64 - 1) < 1e-8, (eV, P2, P64)
+        ctx.set_solver(0)
+        info = {}
+        P0 = api.CalcHeatTransfer(1e-6, eV, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+        assert info["solver"] == 1 and abs(P0 / P64 - 1) < 1e-6
