@@ -704,7 +704,7 @@ int gemm_any<float>(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, 
   return bem_cgemm(ctx, kind, opA, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream);
 }
 
-constexpr int COOP_MAX_SMEM = 200 * 1024;
+constexpr int COOP_MAX_SMEM = 226 * 1024;  // below the 227 KB per-CTA limit, with room for the static part
 
 // Factors the panel [k0, k0 + w) with one cooperative launch; returns false
 // (nothing launched) when the panel does not fit the cooperative kernel.
@@ -765,8 +765,7 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
 }
 
 template <typename T>
-int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream,
-               bool exact = false) {
+int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
   if (int rc0 = set_trsm_attrs<T>(ctx)) return rc0;
   PivCand *cand = (PivCand *)bem_workspace(ctx, "lu_cand", sizeof(PivCand) * 1024);
   unsigned int *counter = (unsigned int *)bem_workspace(ctx, "lu_counter", sizeof(unsigned int));
@@ -815,17 +814,7 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
       }
       T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
       T *A22 = A + 2 * (k0 + w + lda * (int64_t)(k0 + w));
-      int rc;
-      if (exact && sizeof(T) == 8) {
-        // FP64-class trailing update on the tensor cores: A22 -= A21 A12 as a
-        // 5-slice exact product (complex128 in and out)
-        ExactOperand oa, ob;
-        rc = bem_exact_prep(ctx, "lu_L", true, (const double *)A21, lda, nr, w, -1.0, 5, oa, stream);
-        if (!rc) rc = bem_exact_prep(ctx, "lu_U", false, (const double *)A12, lda, nr, w, 1.0, 5, ob, stream);
-        if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_LU_GEMM, oa, ob, (double *)A22, lda, 1, stream);
-      } else {
-        rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
-      }
+      int rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
       if (rc) return rc;
     }
     BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -893,57 +882,189 @@ int bem_zgetrs(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int
                int nrhs, cudaStream_t stream) {
   return getrs_impl<double>(ctx, A, lda, n, d_ipiv, B, ldb, nrhs, stream);
 }
-int bem_zgetrf_exact(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
-  return getrf_impl<double>(ctx, A, lda, n, d_ipiv, d_info, stream, true);
+namespace {
+
+constexpr int NBO = 512;  // super-block of the FP64-class LU and solve
+
+__global__ void identity_block_kernel(double *X, int64_t ld, int w) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (r >= w) return;
+  reinterpret_cast<double2 *>(X)[r + ld * (int64_t)c] = make_double2(r == c ? 1.0 : 0.0, 0.0);
 }
 
-// B <- A^{-1} B with the factors of bem_zgetrf_exact: row interchanges, then
-// blocked forward / back substitution; each 64 x 64 diagonal block is solved
-// in FP64 (trsm_block_kernel) and the off-diagonal block updates are 5-slice
-// exact tensor-core products, so the solve keeps FP64-class accuracy.
+// X (w x ncols, ld ldx) <- T^{-1} X for the w x w triangle T at (A, lda):
+// unit lower (UPPER false) or upper; 64-row diagonal blocks in FP64
+// (trsm_block_kernel), off-diagonal updates as 5-slice exact products.
+int tri_solve_exact(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int w, bool upper, double *X, int64_t ldx,
+                    int ncols, cudaStream_t st) {
+  const int tb = std::min((ncols + 7) / 8, ctx->num_sms * 4);
+  const int nblk = (w + NB - 1) / NB;
+  int rc = BEMGPU_OK;
+  for (int q = 0; q < nblk && !rc; q++) {
+    const int bi = upper ? nblk - 1 - q : q;
+    const int j0 = bi * NB, jw = std::min(NB, w - j0);
+    double *Xj = X + 2 * (int64_t)j0;
+    {
+      ProfScope ps(ctx, BEMGPU_K_TRSM, st, 4.0 * jw * jw * ncols, 32.0 * jw * ncols);
+      if (upper)
+        trsm_block_kernel<double, true, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), st>>>(
+            A + 2 * (j0 + lda * (int64_t)j0), lda, jw, Xj, ldx, ncols);
+      else
+        trsm_block_kernel<double, false, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), st>>>(
+            A + 2 * (j0 + lda * (int64_t)j0), lda, jw, Xj, ldx, ncols);
+      ctx->launches++;
+    }
+    const int m = upper ? j0 : w - j0 - jw;  // rows still to update
+    if (m > 0) {
+      ExactOperand oa, ob;
+      const double *Ablk = upper ? A + 2 * (lda * (int64_t)j0) : A + 2 * (j0 + jw + lda * (int64_t)j0);
+      rc = bem_exact_prep(ctx, "ts_A", true, Ablk, lda, m, jw, -1.0, 5, oa, st);
+      if (!rc) rc = bem_exact_prep(ctx, "ts_B", false, Xj, ldx, ncols, jw, 1.0, 5, ob, st);
+      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRSM, oa, ob, upper ? X : Xj + 2 * (int64_t)jw, ldx, 1, st);
+    }
+  }
+  return rc;
+}
+
+// Dst (m x ncols) (+)= sign * Ablk (m x k) * Bblk (k x ncols) as a 5-slice exact
+// product; Bblk may be Dst itself when accumulate is 0 (it is sliced first).
+int exact_mul(bemgpu_ctx_s *ctx, int kind, const double *Ablk, int64_t lda, int m, int k, double sign,
+              const double *Bblk, int64_t ldb, int ncols, double *Dst, int64_t ldd, int accumulate, cudaStream_t st) {
+  ExactOperand oa, ob;
+  int rc = bem_exact_prep(ctx, "xm_A", true, Ablk, lda, m, k, sign, 5, oa, st);
+  if (!rc) rc = bem_exact_prep(ctx, "xm_B", false, Bblk, ldb, ncols, k, 1.0, 5, ob, st);
+  if (!rc) rc = bem_exact_gemm(ctx, kind, oa, ob, Dst, ldd, accumulate, st);
+  return rc;
+}
+
+}  // namespace
+
+// FP64-class LU on the tensor cores, blocked twice: 512-column super-panels
+// are factored by 64-column cooperative panels whose updates stay inside the
+// super-panel; then the super-panel's pivots are applied to the other
+// columns, U12 = L11^{-1} A12 with the inverse of the 512 x 512 unit-lower
+// diagonal block, and A22 -= A21 U12 as one K = 512 exact product.  The
+// inverses of the diagonal super-blocks (L and U) are kept for
+// bem_zgetrs_exact ("lu_Lb", "lu_Ub": n x 512, block K at rows [K0, K0+512)).
+int bem_zgetrf_exact(bemgpu_ctx_s *ctx, double *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
+  if (int rc0 = set_trsm_attrs<double>(ctx)) return rc0;
+  double *Lb = (double *)bem_workspace(ctx, "lu_Lb", 16 * (size_t)n * NBO);
+  double *Ub = (double *)bem_workspace(ctx, "lu_Ub", 16 * (size_t)n * NBO);
+  if (!Lb || !Ub) return bem_fail(ctx, BEMGPU_ERR_OOM, "getrf_exact: workspace");
+  BEM_CUDA_TRY(ctx, cudaMemsetAsync(d_info, 0, sizeof(int), stream));
+  const double cb = 16.0;
+  int rc = BEMGPU_OK;
+  for (int K0 = 0; K0 < n && !rc; K0 += NBO) {
+    const int WO = std::min(NBO, n - K0);
+    for (int k0 = K0; k0 < K0 + WO && !rc; k0 += NB) {
+      const int w = std::min(NB, K0 + WO - k0);
+      int prc = BEMGPU_OK;
+      const bool coop = ctx->coop_panel && panel_coop<double>(ctx, A, lda, n, k0, w, d_ipiv, d_info, stream, prc);
+      if (prc) return prc;
+      if (!coop) {  // one launch per column when the panel does not fit the cooperative kernel
+        PivCand *cand = (PivCand *)bem_workspace(ctx, "lu_cand", sizeof(PivCand) * 1024);
+        unsigned int *counter = (unsigned int *)bem_workspace(ctx, "lu_counter", sizeof(unsigned int));
+        if (!cand || !counter) return bem_fail(ctx, BEMGPU_ERR_OOM, "getrf_exact: workspace");
+        BEM_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream));
+        const int rows = n - k0;
+        const int blocks = std::max(1, std::min(ctx->num_sms * 2, (rows + PANEL_THREADS - 1) / PANEL_THREADS));
+        for (int jj = 0; jj <= w; jj++) {
+          ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 8.0 * (rows - jj) * (w - jj), 32.0 * (rows - jj) * (w - jj));
+          panel_step_kernel<double><<<blocks, PANEL_THREADS, 0, stream>>>(A, lda, n, k0, w, jj, d_ipiv, d_info, cand,
+                                                                           counter);
+          ctx->launches++;
+        }
+      }
+      {
+        ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * WO);
+        if (k0 > K0) {
+          laswp_kernel<double><<<(k0 - K0 + 127) / 128, 128, 0, stream>>>(A, lda, K0, k0, k0, k0 + w, d_ipiv);
+          ctx->launches++;
+        }
+        if (k0 + w < K0 + WO) {
+          laswp_kernel<double><<<(K0 + WO - k0 - w + 127) / 128, 128, 0, stream>>>(A, lda, k0 + w, K0 + WO, k0, k0 + w,
+                                                                                 d_ipiv);
+          ctx->launches++;
+        }
+      }
+      const int nc = K0 + WO - k0 - w;  // super-panel columns right of this panel
+      if (nc > 0) {
+        const int tb = std::min((nc + 7) / 8, ctx->num_sms * 4);
+        {
+          ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nc, 2.0 * cb * w * nc);
+          trsm_block_kernel<double, false, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), stream>>>(
+              A + 2 * (k0 + lda * (int64_t)k0), lda, w, A + 2 * (k0 + lda * (int64_t)(k0 + w)), lda, nc);
+          ctx->launches++;
+        }
+        if (k0 + w < n)
+          rc = exact_mul(ctx, BEMGPU_K_LU_GEMM, A + 2 * (k0 + w + lda * (int64_t)k0), lda, n - k0 - w, w, -1.0,
+                         A + 2 * (k0 + lda * (int64_t)(k0 + w)), lda, nc, A + 2 * (k0 + w + lda * (int64_t)(k0 + w)),
+                         lda, 1, stream);
+      }
+    }
+    if (rc) break;
+    {
+      ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * WO * (n - WO));
+      if (K0 > 0) {
+        laswp_kernel<double><<<(K0 + 127) / 128, 128, 0, stream>>>(A, lda, 0, K0, K0, K0 + WO, d_ipiv);
+        ctx->launches++;
+      }
+      if (K0 + WO < n) {
+        laswp_kernel<double><<<(n - K0 - WO + 127) / 128, 128, 0, stream>>>(A, lda, K0 + WO, n, K0, K0 + WO, d_ipiv);
+        ctx->launches++;
+      }
+    }
+    // inverses of the diagonal super-block's triangles
+    const double *AKK = A + 2 * (K0 + lda * (int64_t)K0);
+    double *LbK = Lb + 2 * (int64_t)K0, *UbK = Ub + 2 * (int64_t)K0;
+    identity_block_kernel<<<dim3((WO + 255) / 256, WO), 256, 0, stream>>>(LbK, n, WO);
+    identity_block_kernel<<<dim3((WO + 255) / 256, WO), 256, 0, stream>>>(UbK, n, WO);
+    ctx->launches += 2;
+    rc = tri_solve_exact(ctx, AKK, lda, WO, false, LbK, n, WO, stream);
+    if (!rc) rc = tri_solve_exact(ctx, AKK, lda, WO, true, UbK, n, WO, stream);
+    if (rc || K0 + WO >= n) continue;
+    const int nr = n - K0 - WO;
+    double *A12 = A + 2 * (K0 + lda * (int64_t)(K0 + WO));
+    rc = exact_mul(ctx, BEMGPU_K_TRSM, LbK, n, WO, WO, 1.0, A12, lda, nr, A12, lda, 0, stream);
+    if (!rc)
+      rc = exact_mul(ctx, BEMGPU_K_LU_GEMM, A + 2 * (K0 + WO + lda * (int64_t)K0), lda, nr, WO, -1.0, A12, lda, nr,
+                     A + 2 * (K0 + WO + lda * (int64_t)(K0 + WO)), lda, 1, stream);
+  }
+  if (!rc) BEM_CUDA_TRY(ctx, cudaGetLastError());
+  return rc;
+}
+
+// B <- A^{-1} B with the factors and diagonal-block inverses of
+// bem_zgetrf_exact: row interchanges, then per 512-row super-block one exact
+// product with the block's inverse and one K = 512 exact update of the rest.
 int bem_zgetrs_exact(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, const int *d_ipiv, double *B, int64_t ldb,
                      int nrhs, cudaStream_t stream) {
-  if (int rc0 = set_trsm_attrs<double>(ctx)) return rc0;
+  const double *Lb = (const double *)bem_workspace(ctx, "lu_Lb", 16 * (size_t)n * NBO);
+  const double *Ub = (const double *)bem_workspace(ctx, "lu_Ub", 16 * (size_t)n * NBO);
+  if (!Lb || !Ub) return bem_fail(ctx, BEMGPU_ERR_OOM, "getrs_exact: workspace");
   {
     ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 64.0 * n * (double)nrhs);
     laswp_kernel<double><<<(nrhs + 127) / 128, 128, 0, stream>>>(B, ldb, 0, nrhs, 0, n, d_ipiv);
     ctx->launches++;
   }
-  const int tb = std::min((nrhs + 7) / 8, ctx->num_sms * 4);
   int rc = BEMGPU_OK;
-  for (int k0 = 0; k0 < n && !rc; k0 += NB) {  // forward: L Y = P B (unit lower)
-    const int w = std::min(NB, n - k0);
-    double *Bk = B + 2 * (int64_t)k0;
-    {
-      ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nrhs, 32.0 * w * nrhs);
-      trsm_block_kernel<double, false, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), stream>>>(
-          A + 2 * (k0 + lda * (int64_t)k0), lda, w, Bk, ldb, nrhs);
-      ctx->launches++;
-    }
-    if (k0 + w < n) {
-      ExactOperand oa, ob;
-      rc = bem_exact_prep(ctx, "rs_L", true, A + 2 * (k0 + w + lda * (int64_t)k0), lda, n - k0 - w, w, -1.0, 5, oa,
-                          stream);
-      if (!rc) rc = bem_exact_prep(ctx, "rs_B", false, Bk, ldb, nrhs, w, 1.0, 5, ob, stream);
-      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_SOLVE_GEMM, oa, ob, B + 2 * (int64_t)(k0 + w), ldb, 1, stream);
-    }
+  for (int K0 = 0; K0 < n && !rc; K0 += NBO) {  // forward: L Y = P B
+    const int WO = std::min(NBO, n - K0);
+    double *BK = B + 2 * (int64_t)K0;
+    rc = exact_mul(ctx, BEMGPU_K_SOLVE_GEMM, Lb + 2 * (int64_t)K0, n, WO, WO, 1.0, BK, ldb, nrhs, BK, ldb, 0, stream);
+    if (!rc && K0 + WO < n)
+      rc = exact_mul(ctx, BEMGPU_K_SOLVE_GEMM, A + 2 * (K0 + WO + lda * (int64_t)K0), lda, n - K0 - WO, WO, -1.0, BK,
+                     ldb, nrhs, B + 2 * (int64_t)(K0 + WO), ldb, 1, stream);
   }
-  const int nblk = (n + NB - 1) / NB;
+  const int nblk = (n + NBO - 1) / NBO;
   for (int bi = nblk - 1; bi >= 0 && !rc; bi--) {  // backward: U X = Y
-    const int k0 = bi * NB, w = std::min(NB, n - k0);
-    double *Bk = B + 2 * (int64_t)k0;
-    {
-      ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nrhs, 32.0 * w * nrhs);
-      trsm_block_kernel<double, true, NB / 32><<<tb, 256, trsm_smem_bytes<double>(), stream>>>(
-          A + 2 * (k0 + lda * (int64_t)k0), lda, w, Bk, ldb, nrhs);
-      ctx->launches++;
-    }
-    if (k0 > 0) {
-      ExactOperand oa, ob;
-      rc = bem_exact_prep(ctx, "rs_L", true, A + 2 * (lda * (int64_t)k0), lda, k0, w, -1.0, 5, oa, stream);
-      if (!rc) rc = bem_exact_prep(ctx, "rs_B", false, Bk, ldb, nrhs, w, 1.0, 5, ob, stream);
-      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_SOLVE_GEMM, oa, ob, B, ldb, 1, stream);
-    }
+    const int K0 = bi * NBO, WO = std::min(NBO, n - K0);
+    double *BK = B + 2 * (int64_t)K0;
+    rc = exact_mul(ctx, BEMGPU_K_SOLVE_GEMM, Ub + 2 * (int64_t)K0, n, WO, WO, 1.0, BK, ldb, nrhs, BK, ldb, 0, stream);
+    if (!rc && K0 > 0)
+      rc = exact_mul(ctx, BEMGPU_K_SOLVE_GEMM, A + 2 * (lda * (int64_t)K0), lda, K0, WO, -1.0, BK, ldb, nrhs, B, ldb, 1,
+                     stream);
   }
   if (!rc) BEM_CUDA_TRY(ctx, cudaGetLastError());
   return rc;
