@@ -9,10 +9,10 @@ Lorentz model, gaps {20, 50, 100, 200, 500, 1000} nm x 64 frequencies in
 Synthetic meshes from bem_gb300.mesh (seeded), no dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed] [--workload ico3|cube4|ico2] [--lanes L]
+                  [--precision fp64|mixed] [--workload ico3|ico2|cube4|tip] [--lanes L]
 
 Requests go through the request farm (bem_gb300.api.Farm): L lanes (default
-3), each a context with its own stream and host thread, keep L solves in
+4), each a context with its own stream and host thread, keep L solves in
 flight, as the reference's MPI task farm keeps one per servant.  The timed
 region is bracketed by device synchronisations and CUDA events, so it is the
 GPU's wall time for K solves.
@@ -45,6 +45,11 @@ WORKLOADS = {
     "ico3": dict(kind="ico", level=3, gaps=[0.02, 0.05, 0.1, 0.2, 0.5, 1.0], freqs=np.linspace(0.08, 0.13, 64)),
     "ico2": dict(kind="ico", level=2, gaps=[0.02, 0.05, 0.1, 0.2, 0.5, 1.0], freqs=np.linspace(0.08, 0.13, 64)),
     "cube4": dict(kind="cube", nsub=4, gaps=[0.1], freqs=np.linspace(0.08, 0.13, 20)),
+    # a tip over a plate: per request a cone (0.5 um base radius, 1 um high,
+    # hemispherical apex 50-200 nm) of 300-1500 RWG edges drawn from a seed, a
+    # 4 x 4 x 0.5 um plate of 1920 edges, gap log-uniform 10-1000 nm, frequency
+    # uniform 0.08-0.13 eV: requests of uneven N (4400-6800 unknowns)
+    "tip": dict(kind="tip", requests=64, seed=7),
 }
 
 
@@ -52,8 +57,26 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def tip_requests(wl):
+    """(tip body, plate body, eV) per request of the tip workload."""
+    from bem_gb300 import mesh
+    rng = np.random.default_rng(wl["seed"])
+    pv, pt = mesh.box(4.0, 4.0, 0.5, 16, 16, 2)
+    out = []
+    for _ in range(wl["requests"]):
+        gap = float(np.exp(rng.uniform(np.log(0.01), np.log(1.0))))
+        na = int(rng.integers(12, 21))
+        nside = int(rng.integers(4, 20))
+        tv, tt = mesh.cone_tip(0.5, 1.0, float(rng.uniform(0.05, 0.2)), n_around=na, n_side=nside, n_cap=3, n_base=3)
+        plate = mesh.Body.from_mesh(pv + np.array([0.0, 0.0, -gap - 0.25]), pt)
+        out.append((mesh.Body.from_mesh(tv, tt), plate, float(rng.uniform(0.08, 0.13))))
+    return out
+
+
 def make_bodies(wl):
     from bem_gb300 import mesh
+    if wl["kind"] == "tip":
+        return [(b1, b2) for (b1, b2, _) in tip_requests(wl)]
     if wl["kind"] == "ico":
         v, t = mesh.icosphere(1.0, wl["level"], jitter=0.02, seed=12345)
     else:
@@ -67,6 +90,8 @@ def make_bodies(wl):
 
 
 def step_grid(wl):
+    if wl["kind"] == "tip":
+        return [(i, r[2]) for i, r in enumerate(tip_requests(wl))]
     return [(gi, float(f)) for gi in range(len(wl["gaps"])) for f in wl["freqs"]]
 
 
@@ -184,6 +209,31 @@ def run_ours(args, rank, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
+    # Serving: Poisson arrivals at 80 % of the measured throughput, each
+    # request one (gap, frequency) solve; latency = submit -> result ready
+    # (the farm's host clock), reported as p50 / p99.
+    serving = None
+    if args.serve_requests > 0:
+        rate = 0.8 * args.steps * world / (ms / 1e3)
+        rng = np.random.default_rng(2024)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, args.serve_requests))
+        t0s = time.perf_counter()
+        tks = []
+        for k, ta in enumerate(arrivals):
+            dt = ta - (time.perf_counter() - t0s)
+            if dt > 0:
+                time.sleep(dt)
+            tks.append(farm.submit(*job(args.warmup + args.steps + k), precision=prec))
+        lat = []
+        for tk in tks:
+            info = {}
+            farm.result(tk, info=info, strict=False)
+            lat.append(info["ms_latency"])
+        span = time.perf_counter() - t0s
+        serving = {"arrivals": "poisson", "rate_per_s": rate, "requests": len(tks),
+                   "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                   "mean_ms": float(np.mean(lat)), "solves_per_s": len(tks) / span, "lanes": args.lanes}
+
     # e2e through the public API from host buffers: each step uploads its
     # geometry and trees from host arrays inside the timed region, submits the
     # request to the farm and reads the spectral power back.
@@ -260,6 +310,7 @@ def run_ours(args, rank, world):
         "e2e": {"value": args.steps / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": 8 + 16 + 4},
         "clocks": clk.summary(),
+        "serving": serving,
         "P_sample": Ps[:2],
     }
     return out
@@ -304,7 +355,7 @@ def roofline(stats, precision, pk, pk_kind):
         peak = pk.get("bf16_tflops_sustained", 1700.0)
         return dict(base, bound="tensor", achieved=ach, peak=peak, unit="TFLOP/s", frac=ach / peak,
                     peak_source=f"{pk_kind} bf16 sustained",
-                    executed_bf16_tflops=ach * products,
+                    executed_bf16_tflops=ach * products, executed_frac=ach * products / peak,
                     note=f"algorithmic complex flops (8 m n k); the kernel issues {products} bf16 slice products "
                          f"per complex MAC, so the tensor pipe runs {products}x the algorithmic rate")
     ach = by / (ms / 1e3) / 1e9
@@ -317,9 +368,15 @@ def roofline(stats, precision, pk, pk_kind):
 
 def workload_config(args, n_unknowns, world):
     wl = WORKLOADS[args.workload]
-    name = (f"{args.workload}: two r=1um icospheres L3 (1280 tris, 1920 RWGs each), N={n_unknowns}, SiC, "
-            f"gaps {wl['gaps']} um x {len(wl['freqs'])} f in 0.08-0.13 eV" if args.workload == "ico3"
-            else args.workload)
+    if args.workload == "ico3":
+        name = (f"{args.workload}: two r=1um icospheres L3 (1280 tris, 1920 RWGs each), N={n_unknowns}, SiC, "
+                f"gaps {wl['gaps']} um x {len(wl['freqs'])} f in 0.08-0.13 eV")
+    elif args.workload == "tip":
+        name = (f"tip: {wl['requests']} requests, cone tip (300-1500 RWGs, apex 50-200 nm) over a 4x4x0.5 um "
+                f"plate (1920 RWGs), gap log-uniform 10-1000 nm, f uniform 0.08-0.13 eV, seed {wl['seed']}; "
+                f"N varies per request")
+    else:
+        name = args.workload
     return {"workload": name, "precision": args.precision, "N": n_unknowns, "parallelism": f"replicas x{world}",
             "lanes": getattr(args, "lanes", 1),
             "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_unknowns ** 2 * 16 / 1e6)}
@@ -390,7 +447,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "mixed-fp32fill"])
     ap.add_argument("--workload", default="ico3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--lanes", type=int, default=3, help="farm lanes: solves in flight at once on the GPU")
+    ap.add_argument("--lanes", type=int, default=4, help="farm lanes: solves in flight at once on the GPU")
+    ap.add_argument("--serve-requests", type=int, default=16,
+                    help="requests of the Poisson-arrival serving measurement (0: skip)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     if world > 1 and args.impl == "ours":
