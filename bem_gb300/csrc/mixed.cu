@@ -33,6 +33,10 @@ namespace {
 constexpr int MIXED_SLICES = 5;  // block fixed-point slices of the refinement and trace products
 constexpr int DELTA_SLICES = 3;  // slices of a correction (~1e-4 of the iterate): its products carry
                                  // 2^-24 of their own size, far below 2^-41 of the whole
+constexpr int TRACE_SLICES = 4;  // slices of X in the full trace products H1 X, H2 X^H (10 products):
+                                 // ~2^-33 of |H||X| per entry; the trace of a product of two
+                                 // absorption (semi-definite) operators does not cancel, so S keeps
+                                 // ~1e-9 (measured 4e-10 against 5 slices at N = 7680)
 
 __global__ void c128_to_c64_kernel(const double *__restrict__ S, int64_t lds, float *__restrict__ D, int64_t ldd, int m,
                                    int n) {
@@ -228,7 +232,7 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 int spectral_trace(bemgpu_ctx_s *ctx, MixedBufs &b, int n, int ns2, int nt2, cudaStream_t st, double S[2],
                    bool incremental) {
   const double *X = incremental ? b.dY : b.Y;  // rows [0, ns2), leading dimension n
-  const int sl = incremental ? DELTA_SLICES : MIXED_SLICES;
+  const int sl = incremental ? DELTA_SLICES : TRACE_SLICES;
   const int acc = incremental ? 1 : 0;
   ExactOperand opX, opXH;
   int rc = bem_exact_prep(ctx, "X", false, X, n, nt2, ns2, 1.0, sl, opX, st);
