@@ -170,13 +170,13 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
                    cudaStream_t stream, int64_t *n_near, int64_t *n_far);
 // Z (complex128, column-major, ld) = gather of one H with g's Zeps/Zmu.
 int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, const bemgpu_green_t *g,
-                 double *Z, int64_t ld, cudaStream_t stream);
+                 double *Z, int64_t ld, cudaStream_t stream, bool df = false);
 // W = gather(Hext, gext) (+ gather(Hint1, g1) on the s block, + gather(Hint2, g2) on the t block),
 // G1 = gather(Hint1, g1), G2 = gather(Hint2, g2).
 int bem_gather_w(bemgpu_ctx_s *ctx, const HalfPairBlock *Hext, const HalfPairBlock *H1,
                  const HalfPairBlock *H2, int ns, int nt, const bemgpu_green_t *gext,
                  const bemgpu_green_t *g1, const bemgpu_green_t *g2, double *W, int64_t ldw, double *G1,
-                 int64_t ld1, double *G2, int64_t ld2, cudaStream_t stream);
+                 int64_t ld1, double *G2, int64_t ld2, cudaStream_t stream, bool df = false);
 
 // ---- dense complex linear algebra (dense.cu) ----
 // In-place LU with partial pivoting of the n x n complex128 column-major A.

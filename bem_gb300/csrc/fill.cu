@@ -33,6 +33,8 @@ struct GreenDev {
   double ikr, iki;      // ik
   double k2r, k2i;      // k2 = -ksquared/2
   double ksqr, ksqi;    // ksquared
+  // the same as double-float pairs (hi, lo), split on the host
+  float ikr_f[2], iki_f[2], k2r_f[2], k2i_f[2], ksqr_f[2], ksqi_f[2];
 };
 
 struct FarOpts {
@@ -135,6 +137,15 @@ __device__ __forceinline__ void store_block(HalfPairBlock *H, int ntr, int i, in
   double2 *p = reinterpret_cast<double2 *>(&H[(size_t)j * ntr + i].v[(a * 2 + b) * 4]);
   p[0] = make_double2(cL.r, cL.i);
   p[1] = make_double2(cK.r, cK.i);
+}
+
+// Double-float fill: the block holds each value as a float pair (hi, lo) in
+// its 8-byte slot; the gather widens hi + lo (exact in FP64).
+__device__ __forceinline__ void store_block_df(HalfPairBlock *H, int ntr, int i, int a, int j, int b, df Lr, df Li,
+                                               df Kr, df Ki) {
+  float4 *p = reinterpret_cast<float4 *>(&H[(size_t)j * ntr + i].v[(a * 2 + b) * 4]);
+  p[0] = make_float4(Lr.hi, Lr.lo, Li.hi, Li.lo);
+  p[1] = make_float4(Kr.hi, Kr.lo, Ki.hi, Ki.lo);
 }
 
 // Scatter coefficient of src/Impedance.cpp:372-375.
@@ -269,6 +280,7 @@ __device__ __forceinline__ void df_exp_ikR(const GreenDev &g, df ikr, df iki, df
 // then runs both rules, the outer moments and the closed-form contraction in
 // df, and only widens the nine (c L, c K) products to FP64 for the store.
 struct TriDF {
+  float p0[3][2];              // df frame origin (first half-RWG's free vertex)
   float v01[3][2], v02[3][2];  // df edge vectors of the first half-RWG's frame
   float e[3][3][2];            // df hp0[i] - p0
   float hs[3][2];              // df helen[i] / sqrt(4 pi)
@@ -281,7 +293,8 @@ __global__ void tri_df_kernel(const TriRec *__restrict__ R, int n, TriDF *__rest
   TriDF o;
   const double sc = sqrt(BEM_ONEOVER4PI);
   for (int c = 0; c < 3; c++) {
-    const df a = df_make(T.v01[c]), b = df_make(T.v02[c]);
+    const df a = df_make(T.v01[c]), b = df_make(T.v02[c]), p = df_make(T.p0[c]);
+    o.p0[c][0] = p.hi; o.p0[c][1] = p.lo;
     o.v01[c][0] = a.hi; o.v01[c][1] = a.lo;
     o.v02[c][0] = b.hi; o.v02[c][1] = b.lo;
   }
@@ -344,9 +357,9 @@ __device__ __forceinline__ cdf3 cdf3_zero() {
 __device__ __noinline__ void far_pair_df2(const TriRec &T, const TriRec &S, const TriDF &TD, const TriDF &SD,
                                           const GreenDev &g, const float (*rdf)[6], int nr, HalfPairBlock *H,
                                           int ntr) {
-  const df3 D0 = df3_make(ld3(T.p0) - ld3(S.p0));  // P_t - P_s
+  const df3 D0 = df3_sub(ld_df3(TD.p0), ld_df3(SD.p0));  // P_t - P_s
   const df3 v01t = ld_df3(TD.v01), v02t = ld_df3(TD.v02), v01s = ld_df3(SD.v01), v02s = ld_df3(SD.v02);
-  const df ikr = df_make(g.ikr), iki = df_make(g.iki);
+  const df ikr = {g.ikr_f[0], g.ikr_f[1]}, iki = {g.iki_f[0], g.iki_f[1]};
   const df z0 = {0.f, 0.f};
   cdf U0 = {z0, z0}, U1 = {z0, z0}, V0 = {z0, z0};
   cdf3 U2 = cdf3_zero(), U3 = cdf3_zero(), V1 = cdf3_zero(), V2 = cdf3_zero(), V3 = cdf3_zero();
@@ -399,7 +412,7 @@ __device__ __noinline__ void far_pair_df2(const TriRec &T, const TriRec &S, cons
     V3 = cdf3_add(V3, cdf_v(wQ0, rho));
   }
   // the closed form of far_pair(), in df
-  const cdf ksq = {df_make(g.ksqr), df_make(g.ksqi)};
+  const cdf ksq = {{g.ksqr_f[0], g.ksqr_f[1]}, {g.ksqi_f[0], g.ksqi_f[1]}};
   const df quarter = {0.25f, 0.f};
   for (int i = 0; i < T.nh; i++) {
     const df3 ei = ld_df3(TD.e[i]);
@@ -415,8 +428,7 @@ __device__ __noinline__ void far_pair_df2(const TriRec &T, const TriRec &S, cons
       df c = df_mul({TD.hs[i][0], TD.hs[i][1]}, {SD.hs[j][0], SD.hs[j][1]});
       if (T.hneg[i] != S.hneg[j]) c = df_neg(c);
       const cdf cL = cdf_scale(c, L), cK = cdf_scale(c, K);
-      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], z1{df_to_double(cL.r), df_to_double(cL.i)},
-                  z1{df_to_double(cK.r), df_to_double(cK.i)});
+      store_block_df(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], cL.r, cL.i, cK.r, cK.i);
     }
   }
 }
@@ -681,7 +693,8 @@ struct InnerMomDF {
 // inner nodes, which the scheduler interleaves.
 template <int NP>
 __device__ __noinline__ void near_inner_df(const float (*nd)[8], const df3 *rp, const GreenDev &g, InnerMomDF *out) {
-  const df ikr = df_make(g.ikr), iki = df_make(g.iki), k2r = df_make(g.k2r), k2i = df_make(g.k2i);
+  const df ikr = {g.ikr_f[0], g.ikr_f[1]}, iki = {g.iki_f[0], g.iki_f[1]};
+  const df k2r = {g.k2r_f[0], g.k2r_f[1]}, k2i = {g.k2i_f[0], g.k2i_f[1]};
   df3 r[NP];
   df I0r[NP], I0i[NP], Q0r[NP], Q0i[NP], Ar[NP][3], Ai[NP][3], Qr[NP][3], Qi[NP][3];
   const df z = {0.f, 0.f};
@@ -846,8 +859,8 @@ __device__ void near_pair_df_setup(const TriRec &T, const TriRec &S, const Green
   pc.v01t = df3_make(ld3(T.v01));
   pc.v02t = df3_make(ld3(T.v02));
   pc.Ai2 = df_make(0.5 * S.Ai);
-  pc.ksq = {df_make(g.ksqr), df_make(g.ksqi)};
-  pc.k2 = {df_make(g.k2r), df_make(g.k2i)};
+  pc.ksq = {{g.ksqr_f[0], g.ksqr_f[1]}, {g.ksqi_f[0], g.ksqi_f[1]}};
+  pc.k2 = {{g.k2r_f[0], g.k2r_f[1]}, {g.k2i_f[0], g.k2i_f[1]}};
   pc.k2_3 = {df_make(BEM_ONETHIRD * g.k2r), df_make(BEM_ONETHIRD * g.k2i)};
   pc.tol_eh = (float)(1e-6 * S.elen0);
   pc.tol_plane = (float)(1e-8 * S.elen0);
@@ -1182,7 +1195,12 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
       for (int k = 0; k < 9; k++)
         if (k == i * 3 + j) { Lv = L[k]; Kv = K[k]; }
       const double c = scatter_coef(T, i, S, j);
-      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, Lv), zscale(c, Kv));
+      const z1 cL = zscale(c, Lv), cK = zscale(c, Kv);
+      if (DF)
+        store_block_df(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], df_make(cL.r), df_make(cL.i),
+                       df_make(cK.r), df_make(cK.i));
+      else
+        store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], cL, cK);
     }
     __syncwarp();
   }
@@ -1193,10 +1211,27 @@ struct ZDev {
   double zer, zei, zmr, zmi;  // Zeps, Zmu
 };
 
+template <bool DFH>
 __device__ __forceinline__ void block_sum(const HalfPairBlock &b, z1 &sL, z1 &sK) {
-  const double2 *p = reinterpret_cast<const double2 *>(b.v);
   sL = {0, 0};
   sK = {0, 0};
+  if (DFH) {
+    // the four half-pair terms summed in double-float, widened once
+    const float4 *p = reinterpret_cast<const float4 *>(b.v);
+    df Lr = {0.f, 0.f}, Li = Lr, Kr = Lr, Ki = Lr;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float4 l = p[2 * k], kk = p[2 * k + 1];
+      Lr = df_add(Lr, {l.x, l.y});
+      Li = df_add(Li, {l.z, l.w});
+      Kr = df_add(Kr, {kk.x, kk.y});
+      Ki = df_add(Ki, {kk.z, kk.w});
+    }
+    sL = {df_to_double(Lr), df_to_double(Li)};
+    sK = {df_to_double(Kr), df_to_double(Ki)};
+    return;
+  }
+  const double2 *p = reinterpret_cast<const double2 *>(b.v);
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const double2 l = p[2 * k], kk = p[2 * k + 1];
@@ -1216,16 +1251,18 @@ __device__ __forceinline__ void write_2x2(double *Z, int64_t ld, int i, int j, z
   c1[1] = make_double2(d.r, d.i);
 }
 
+template <bool DFH>
 __global__ void gather_z_kernel(const HalfPairBlock *__restrict__ H, int ntr, int nsr, ZDev z, double *Z, int64_t ld) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (i >= ntr) return;
   z1 sL, sK;
-  block_sum(H[(size_t)j * ntr + i], sL, sK);
+  block_sum<DFH>(H[(size_t)j * ntr + i], sL, sK);
   write_2x2(Z, ld, i, j, {z.zer, z.zei}, {z.zmr, z.zmi}, sL, sK);
 }
 
 // W = Z_ext + blockdiag(G1, G2) and the G blocks themselves (src/HeatTransfer.cpp:26-35).
+template <bool DFH>
 __global__ void gather_w_kernel(const HalfPairBlock *__restrict__ He, const HalfPairBlock *__restrict__ H1,
                                 const HalfPairBlock *__restrict__ H2, int ns, int nt, ZDev ze, ZDev z1d, ZDev z2d,
                                 double *W, int64_t ldw, double *G1, int64_t ld1, double *G2, int64_t ld2) {
@@ -1234,14 +1271,14 @@ __global__ void gather_w_kernel(const HalfPairBlock *__restrict__ He, const Half
   const int j = blockIdx.y;
   if (i >= n) return;
   z1 sL, sK;
-  block_sum(He[(size_t)j * n + i], sL, sK);
+  block_sum<DFH>(He[(size_t)j * n + i], sL, sK);
   z1 a = zmul({ze.zer, ze.zei}, sL), d = zmul({ze.zmr, ze.zmi}, sL), k = sK;
   const bool in1 = i < ns && j < ns, in2 = i >= ns && j >= ns;
   if (in1 || in2) {
     z1 gL, gK;
     const ZDev &zz = in1 ? z1d : z2d;
     const int li = in1 ? i : i - ns, lj = in1 ? j : j - ns, nn = in1 ? ns : nt;
-    block_sum((in1 ? H1 : H2)[(size_t)lj * nn + li], gL, gK);
+    block_sum<DFH>((in1 ? H1 : H2)[(size_t)lj * nn + li], gL, gK);
     write_2x2(in1 ? G1 : G2, in1 ? ld1 : ld2, li, lj, {zz.zer, zz.zei}, {zz.zmr, zz.zmi}, gL, gK);
     const z1 ga = zmul({zz.zer, zz.zei}, gL), gd = zmul({zz.zmr, zz.zmi}, gL);
     a = zadd(a, ga);
@@ -1256,11 +1293,19 @@ __global__ void gather_w_kernel(const HalfPairBlock *__restrict__ He, const Half
   c1[1] = make_double2(d.r, d.i);
 }
 
+void split_df(double x, float out[2]) {
+  out[0] = (float)x;
+  out[1] = (float)(x - (double)out[0]);
+}
+
 GreenDev to_dev(const bemgpu_green_t *g) {
   GreenDev d;
   d.ikr = g->ik[0]; d.iki = g->ik[1];
   d.k2r = g->k2[0]; d.k2i = g->k2[1];
   d.ksqr = g->ksquared[0]; d.ksqi = g->ksquared[1];
+  split_df(d.ikr, d.ikr_f); split_df(d.iki, d.iki_f);
+  split_df(d.k2r, d.k2r_f); split_df(d.k2i, d.k2i_f);
+  split_df(d.ksqr, d.ksqr_f); split_df(d.ksqi, d.ksqi_f);
   return d;
 }
 
@@ -1368,11 +1413,14 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
 }
 
 int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, const bemgpu_green_t *g, double *Z,
-                 int64_t ld, cudaStream_t stream) {
+                 int64_t ld, cudaStream_t stream, bool df) {
   dim3 blk(128);
   dim3 grd((ntr + 127) / 128, nsr);
   ProfScope ps(ctx, BEMGPU_K_GATHER, stream, (double)ntr * nsr * (6 * 8 + 2 * 6), (double)ntr * nsr * (128 + 64));
-  gather_z_kernel<<<grd, blk, 0, stream>>>(H, ntr, nsr, to_zdev(g), Z, ld);
+  if (df)
+    gather_z_kernel<true><<<grd, blk, 0, stream>>>(H, ntr, nsr, to_zdev(g), Z, ld);
+  else
+    gather_z_kernel<false><<<grd, blk, 0, stream>>>(H, ntr, nsr, to_zdev(g), Z, ld);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   return BEMGPU_OK;
@@ -1380,13 +1428,18 @@ int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, co
 
 int bem_gather_w(bemgpu_ctx_s *ctx, const HalfPairBlock *Hext, const HalfPairBlock *H1, const HalfPairBlock *H2,
                  int ns, int nt, const bemgpu_green_t *gext, const bemgpu_green_t *g1, const bemgpu_green_t *g2,
-                 double *W, int64_t ldw, double *G1, int64_t ld1, double *G2, int64_t ld2, cudaStream_t stream) {
+                 double *W, int64_t ldw, double *G1, int64_t ld1, double *G2, int64_t ld2, cudaStream_t stream,
+                 bool df) {
   dim3 blk(128);
   dim3 grd((ns + nt + 127) / 128, ns + nt);
   const double nn = (double)(ns + nt) * (ns + nt), nd = (double)ns * ns + (double)nt * nt;
   ProfScope ps(ctx, BEMGPU_K_GATHER, stream, nn * 60 + nd * 80, nn * 192 + nd * 192);
-  gather_w_kernel<<<grd, blk, 0, stream>>>(Hext, H1, H2, ns, nt, to_zdev(gext), to_zdev(g1), to_zdev(g2), W, ldw, G1,
-                                           ld1, G2, ld2);
+  if (df)
+    gather_w_kernel<true><<<grd, blk, 0, stream>>>(Hext, H1, H2, ns, nt, to_zdev(gext), to_zdev(g1), to_zdev(g2), W,
+                                                   ldw, G1, ld1, G2, ld2);
+  else
+    gather_w_kernel<false><<<grd, blk, 0, stream>>>(Hext, H1, H2, ns, nt, to_zdev(gext), to_zdev(g1), to_zdev(g2), W,
+                                                    ldw, G1, ld1, G2, ld2);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   return BEMGPU_OK;
@@ -1409,7 +1462,7 @@ extern "C" int bemgpu_zts(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, co
   if (!H) return bem_fail(ctx, BEMGPU_ERR_OOM, "zts: workspace allocation failed");
   int rc = bem_fill_pairs(ctx, t, s, g, &o, precision, H, st, nullptr, nullptr);
   if (rc) return rc;
-  return bem_gather_z(ctx, H, t->nrwg, s->nrwg, g, (double *)dZ, ldz, st);
+  return bem_gather_z(ctx, H, t->nrwg, s->nrwg, g, (double *)dZ, ldz, st, precision == BEMGPU_PREC_MIXED_LA);
 }
 
 extern "C" int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
@@ -1516,7 +1569,7 @@ extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree
   }
   dim3 gblk(128);
   dim3 ggrd((t->nrwg + 127) / 128, s->nrwg);
-  gather_z_kernel<<<ggrd, gblk, 0, st>>>(H, t->nrwg, s->nrwg, to_zdev(g), (double *)dZ, ldz);
+  gather_z_kernel<false><<<ggrd, gblk, 0, st>>>(H, t->nrwg, s->nrwg, to_zdev(g), (double *)dZ, ldz);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   // The near-pair list was copied from host memory owned by this call.

@@ -175,7 +175,9 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   int rc = bem_fill_pairs(ctx, top, top, &gext, &o, fill_prec, He, st, &near1, &far1);
   if (!rc) rc = bem_fill_pairs(ctx, s, s, &g1, &o, fill_prec, H1, st, &near2, &far2);
   if (!rc) rc = bem_fill_pairs(ctx, t, t, &g2, &o, fill_prec, H2, st, &near3, &far3);
-  if (!rc) rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st);
+  if (!rc)
+    rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st,
+                      fill_prec == BEMGPU_PREC_MIXED_LA);
   if (rc) return rc;
   cudaEventRecord(ev[7], st);
   {
