@@ -622,6 +622,43 @@ extern "C" int bemgpu_cgemm_acc64(bemgpu_ctx_t ctx, int m, int n, int k, const f
   return BEMGPU_OK;
 }
 
+namespace {
+
+// Polls a word that nothing sets, at most `spins` times and about a second of
+// clock, then records a timeout in the context's error flag: the same exit
+// every bounded wait of the library takes (TMA / MMA pipelines, grid barriers).
+__global__ void wait_selftest_kernel(const unsigned *flag, long long spins, long long max_cycles, int *err) {
+  if (threadIdx.x != 0) return;
+  const long long t0 = clock64();
+  for (long long it = 0; it < spins; it++) {
+    if (*(volatile const unsigned *)flag != 0u) return;
+    if (clock64() - t0 > max_cycles) break;
+  }
+  atomicExch(err, 1);
+}
+
+}  // namespace
+
+extern "C" int bemgpu_ctx_wait_selftest(bemgpu_ctx_t ctx, int64_t spins) {
+  if (!ctx || spins < 1 || spins > 100000000) return bem_fail(ctx, BEMGPU_ERR_ARG, "wait_selftest: spins in [1, 1e8]");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  unsigned *flag = (unsigned *)bem_workspace(ctx, "selftest_flag", sizeof(unsigned));
+  int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
+  if (!flag || !err) return bem_fail(ctx, BEMGPU_ERR_OOM, "wait_selftest: workspace");
+  if (!ctx->tc_err_ready) {
+    BEM_CUDA_TRY(ctx, cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+    ctx->tc_err_ready = true;
+  }
+  BEM_CUDA_TRY(ctx, cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
+  wait_selftest_kernel<<<1, 32, 0, ctx->stream>>>(flag, (long long)spins, 2000000000ll, err);
+  ctx->launches++;
+  BEM_CUDA_TRY(ctx, cudaGetLastError());
+  if (bem_tc_error(ctx, true))
+    return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "wait_selftest: the bounded wait ran out after %lld polls", (long long)spins);
+  return BEMGPU_OK;
+}
+
 extern "C" int bemgpu_ctx_set_solver(bemgpu_ctx_t ctx, int mode) {
   if (!ctx || mode < 0 || mode > 2)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "set_solver: modes are 0 (complex64, escalating), 1 (complex64), 2 (FP64-class)");

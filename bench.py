@@ -349,7 +349,10 @@ def roofline(stats, precision, pk, pk_kind):
         ach = fl / (ms / 1e3) / 1e12
         return dict(base, bound="fp32 pipe (double-float)", achieved=ach, peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s",
                     frac=ach / FP64_NOMINAL_TFLOPS,
-                    peak_source="FP64-class work in double-float; compared with the nominal FP64 rate it replaces")
+                    peak_source="FP64-class work in double-float; compared with the nominal FP64 rate it replaces",
+                    note="algorithmic FP64-class flops of the fill (frozen count) per CUDA-event second; the FP32 "
+                         "pipes run the double-float arithmetic at ~55 % of their issue rate (ncu, near-pair "
+                         "kernel), so frac > 1 means faster than the FP64 pipe could be, not above a roofline")
     if bound == "tensor":
         ach = fl / (ms / 1e3) / 1e12
         peak = pk.get("bf16_tflops_sustained", 1700.0)

@@ -112,6 +112,11 @@ int bemgpu_ctx_set_engines(bemgpu_ctx_t ctx, int gemm, int acc64);
  * FP64-class tensor-core LU when its refinement does not converge (default);
  * 1 = complex64 only; 2 = FP64-class only.  No reference counterpart. */
 int bemgpu_ctx_set_solver(bemgpu_ctx_t ctx, int mode);
+/* Failure-path self-test: one kernel polls a flag that nothing sets, gives up
+ * after `spins` polls (or about a second), and records a timeout exactly as the
+ * library's bounded waits do; returns BEMGPU_ERR_TIMEOUT and leaves the context
+ * usable.  No reference counterpart. */
+int bemgpu_ctx_wait_selftest(bemgpu_ctx_t ctx, int64_t spins);
 
 /* ---- live kernel statistics (measurement hooks; no counterpart in the reference) ---- */
 /* Kernel classes timed with CUDA events on the context stream while enabled. */

@@ -74,3 +74,25 @@ def test_size_mismatch_is_rejected():
     with pytest.raises(Exception) as e:
         api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, s, s, tt)
     assert "ARG" in str(e.value)
+
+
+def test_bounded_wait_timeout_leaves_the_context_usable():
+    """Failure detection without a GPU fault: a wait on a flag that nothing
+    sets gives up after its budget and reports BEMGPU_ERR_TIMEOUT through the
+    same error flag the tensor-core pipelines and grid barriers use; the next
+    solve on the same context runs normally."""
+    from bem_gb300 import _lib
+    ctx = api.Context(0)
+    L = _lib.load()
+    assert L.bemgpu_ctx_wait_selftest(ctx.handle, 1000) == _lib.ERR_TIMEOUT
+    assert "ran out" in L.bemgpu_ctx_last_error(ctx.handle).decode()
+    v, t = mesh.cube(1.0, 2)
+    b2 = mesh.Body.from_mesh(v, t)
+    b1 = b2.translated(mesh.gap_translation(v, v, 0.1))
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    top, s, tt = api.parseShapes(b1, b2, d, d, ctx)
+    ref = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, *api.parseShapes(b1, b2, d, d))
+    for prec in (_lib.PREC_FP64, _lib.PREC_MIXED_LA):
+        P = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, tt, precision=prec)
+        assert abs(P / ref - 1) < (1e-12 if prec == _lib.PREC_FP64 else 1e-6)
+    assert L.bemgpu_ctx_wait_selftest(ctx.handle, 10) == _lib.ERR_TIMEOUT
