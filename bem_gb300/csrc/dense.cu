@@ -226,7 +226,8 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
 template <typename T>
 __global__ void __launch_bounds__(COOP_THREADS)
     panel_coop_kernel(T *A, int64_t lda, int n, int k0, int w, int chunk, int *ipiv, int *info, T *cval,
-                      int *crow, T *cdata_raw, T *drow_raw, unsigned *counter, int *err) {
+                      int *crow, T *cdata_raw, T *drow_raw, unsigned *counter, int *err,
+                      unsigned long long *best) {
   typedef typename V2<T>::type T2;
   extern __shared__ __align__(16) unsigned char coop_smem[];
   T2 *P = reinterpret_cast<T2 *>(coop_smem);  // chunk x w, P[i * w + c]
@@ -282,8 +283,17 @@ __global__ void __launch_bounds__(COOP_THREADS)
           bv = red_v[q];
           bi = red_i[q];
         }
-      cval[par * G + g] = bv;
-      crow[par * G + g] = bi;
+      if constexpr (sizeof(T) == 4) {
+        // complex64: the candidate goes into one packed key per column (slot
+        // j % 3), magnitude bits over the complemented row, so the largest key
+        // is the largest |re| + |im| and, among equal ones, the first row
+        if (bi != 0x7fffffff)
+          atomicMax(best + j % 3, ((unsigned long long)__float_as_uint((float)bv) << 32) |
+                                      (unsigned long long)(0xffffffffu - (unsigned)bi));
+      } else {
+        cval[par * G + g] = bv;
+        crow[par * G + g] = bi;
+      }
       s_row = bi;
     }
     __syncthreads();
@@ -310,9 +320,28 @@ __global__ void __launch_bounds__(COOP_THREADS)
     __syncthreads();
     if (s_abort) return;
     // (3) the pivot: every CTA reduces the same candidates in the same way
+    if constexpr (sizeof(T) == 4) {
+      if (tid == 0) {
+        const unsigned long long key = __ldcg(best + j % 3);
+        // slot (j - 1) % 3 was read by every CTA before it arrived here; it is
+        // next used at column j + 2, after the barrier this CTA passes later
+        if (g == 0 && j >= 1) atomicExch(best + (j - 1) % 3, 0ull);
+        const bool zero = (key >> 32) == 0ull;
+        const int row = zero ? dr : (int)(0xffffffffu - (unsigned)(key & 0xffffffffull));
+        s_zero = zero;
+        s_row = row;
+        s_win = zero ? -1 : (row - k0) / chunk;
+        if (g == 0) {
+          ipiv[dr] = row;
+          if (zero && *info == 0) *info = dr + 1;
+        }
+      }
+      __syncthreads();
+    }
     bv = T(-1);
     bi = 0x7fffffff;
     int bw = 0;
+    if constexpr (sizeof(T) == 8) {
     for (int q = tid; q < G; q += COOP_THREADS) {
       const T v = __ldcg(cval + par * G + q);
       const int r = __ldcg(crow + par * G + q);
@@ -360,6 +389,7 @@ __global__ void __launch_bounds__(COOP_THREADS)
       }
     }
     __syncthreads();
+    }
     const int p = s_row;
     const bool zero = s_zero;
     for (int c = tid; c < w; c += COOP_THREADS) {
@@ -740,8 +770,9 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
   T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * 1024 * (size_t)NB_MAX);
   T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)NB_MAX);
   unsigned *counter = (unsigned *)bem_workspace(ctx, "coop_counter", sizeof(unsigned));
+  unsigned long long *best = (unsigned long long *)bem_workspace(ctx, "coop_best", 4 * sizeof(unsigned long long));
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
-  if (!cval || !crow || !cdata || !drow || !counter || !err || G > 1024 || w > NB_MAX) {
+  if (!cval || !crow || !cdata || !drow || !counter || !best || !err || G > 1024 || w > NB_MAX) {
     rc = bem_fail(ctx, BEMGPU_ERR_OOM, "getrf: panel workspace");
     return true;
   }
@@ -750,8 +781,10 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
     ctx->tc_err_ready = true;
   }
   cudaMemsetAsync(counter, 0, sizeof(unsigned), stream);
+  cudaMemsetAsync(best, 0, 4 * sizeof(unsigned long long), stream);
   int n_ = n, k0_ = k0, w_ = w, chunk_ = chunk;
-  void *args[] = {&A, &lda, &n_, &k0_, &w_, &chunk_, &d_ipiv, &d_info, &cval, &crow, &cdata, &drow, &counter, &err};
+  void *args[] = {&A,    &lda,  &n_,    &k0_,  &w_,      &chunk_, &d_ipiv, &d_info,
+                  &cval, &crow, &cdata, &drow, &counter, &err,    &best};
   const double cb = 2.0 * sizeof(T);
   ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 4.0 * (double)rows * w * w, cb * 2.0 * rows * w);
   const cudaError_t e = cudaLaunchCooperativeKernel((const void *)panel_coop_kernel<T>, dim3(G), dim3(COOP_THREADS),
