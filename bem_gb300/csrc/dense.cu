@@ -277,67 +277,88 @@ __global__ void __launch_bounds__(COOP_THREADS)
       red_i[wid] = bi;
     }
     __syncthreads();
-    if (tid == 0) {
-      for (int q = 1; q < COOP_THREADS / 32; q++)
-        if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) {
-          bv = red_v[q];
-          bi = red_i[q];
+    // warp 0 publishes the CTA's candidate (value, row, row data) and the
+    // diagonal row, then its lane 0 takes the grid barrier; the other warps
+    // wait at the CTA barrier that follows
+    if (wid == 0) {
+      if (lane == 0) {
+        for (int q = 1; q < COOP_THREADS / 32; q++)
+          if (red_v[q] > bv || (red_v[q] == bv && red_i[q] < bi)) {
+            bv = red_v[q];
+            bi = red_i[q];
+          }
+        if constexpr (sizeof(T) == 4) {
+          // complex64: the candidate goes into one packed key per column (slot
+          // j % 3), magnitude bits over the complemented row, so the largest
+          // key is the largest |re| + |im| and, among equal ones, the first row
+          if (bi != 0x7fffffff)
+            atomicMax(best + j % 3, ((unsigned long long)__float_as_uint((float)bv) << 32) |
+                                        (unsigned long long)(0xffffffffu - (unsigned)bi));
+        } else {
+          cval[par * G + g] = bv;
+          crow[par * G + g] = bi;
         }
-      if constexpr (sizeof(T) == 4) {
-        // complex64: the candidate goes into one packed key per column (slot
-        // j % 3), magnitude bits over the complemented row, so the largest key
-        // is the largest |re| + |im| and, among equal ones, the first row
-        if (bi != 0x7fffffff)
-          atomicMax(best + j % 3, ((unsigned long long)__float_as_uint((float)bv) << 32) |
-                                      (unsigned long long)(0xffffffffu - (unsigned)bi));
-      } else {
-        cval[par * G + g] = bv;
-        crow[par * G + g] = bi;
       }
-      s_row = bi;
-    }
-    __syncthreads();
-    if (s_row != 0x7fffffff)
-      for (int c = tid; c < w; c += COOP_THREADS) cdata[(int64_t)(par * G + g) * w + c] = P[(s_row - rbeg) * w + c];
-    if (dr >= rbeg && dr < rend)
-      for (int c = tid; c < w; c += COOP_THREADS) drow[par * w + c] = P[(dr - rbeg) * w + c];
-    __syncthreads();
-    // (2) grid barrier
-    if (tid == 0) {
-      // the CTA's publishing writes (ordered before by the bar.sync above) are
-      // released with the arrival; the acquire load orders the reads below
-      arrive_release_u32(counter);
-      const unsigned target = (unsigned)G * (unsigned)(j + 1);
-      unsigned it = 0;
-      while (ld_acquire_u32(counter) < target) {
-        if (++it > COOP_SPIN_LIMIT) {
-          atomicExch(err, 1);
-          s_abort = true;
-          break;
+      bi = __shfl_sync(0xffffffffu, bi, 0);
+      if (bi != 0x7fffffff)
+        for (int c = lane; c < w; c += 32) cdata[(int64_t)(par * G + g) * w + c] = P[(bi - rbeg) * w + c];
+      if (dr >= rbeg && dr < rend)
+        for (int c = lane; c < w; c += 32) drow[par * w + c] = P[(dr - rbeg) * w + c];
+      __syncwarp();
+      // (2) grid barrier
+      if (lane == 0) {
+        // the warp's publishing writes (ordered before by the warp barrier and
+        // the fence) are released with the arrival; the acquire load orders
+        // the reads after the CTA barrier below
+        __threadfence();
+        arrive_release_u32(counter);
+        const unsigned target = (unsigned)G * (unsigned)(j + 1);
+        unsigned it = 0;
+        while (ld_acquire_u32(counter) < target) {
+          if (++it > COOP_SPIN_LIMIT) {
+            atomicExch(err, 1);
+            s_abort = true;
+            break;
+          }
         }
       }
     }
     __syncthreads();
     if (s_abort) return;
-    // (3) the pivot: every CTA reduces the same candidates in the same way
+    // (3) the pivot, the pivot (U) row into shared memory, and the interchange
     if constexpr (sizeof(T) == 4) {
-      if (tid == 0) {
-        const unsigned long long key = __ldcg(best + j % 3);
-        // slot (j - 1) % 3 was read by every CTA before it arrived here; it is
-        // next used at column j + 2, after the barrier this CTA passes later
-        if (g == 0 && j >= 1) atomicExch(best + (j - 1) % 3, 0ull);
-        const bool zero = (key >> 32) == 0ull;
-        const int row = zero ? dr : (int)(0xffffffffu - (unsigned)(key & 0xffffffffull));
-        s_zero = zero;
-        s_row = row;
-        s_win = zero ? -1 : (row - k0) / chunk;
-        if (g == 0) {
-          ipiv[dr] = row;
-          if (zero && *info == 0) *info = dr + 1;
+      if (wid == 0) {
+        int row = 0, win = -1, zi = 0;
+        if (lane == 0) {
+          const unsigned long long key = __ldcg(best + j % 3);
+          // slot (j - 1) % 3 was read by every CTA before it arrived here; it
+          // is next used at column j + 2, after the barrier this CTA passes later
+          if (g == 0 && j >= 1) atomicExch(best + (j - 1) % 3, 0ull);
+          zi = (key >> 32) == 0ull;
+          row = zi ? dr : (int)(0xffffffffu - (unsigned)(key & 0xffffffffull));
+          win = zi ? -1 : (row - k0) / chunk;
+          if (g == 0) {
+            ipiv[dr] = row;
+            if (zi && *info == 0) *info = dr + 1;
+          }
+          s_zero = zi != 0;
+          s_row = row;
+        }
+        row = __shfl_sync(0xffffffffu, row, 0);
+        win = __shfl_sync(0xffffffffu, win, 0);
+        for (int c = lane; c < w; c += 32)
+          prow[c] = (row == dr || win < 0) ? __ldcg(drow + par * w + c)
+                                           : __ldcg(cdata + (int64_t)(par * G + win) * w + c);
+        __syncwarp();
+        if (row != dr) {
+          if (dr >= rbeg && dr < rend)
+            for (int c = lane; c < w; c += 32) P[(dr - rbeg) * w + c] = prow[c];
+          if (row >= rbeg && row < rend)
+            for (int c = lane; c < w; c += 32) P[(row - rbeg) * w + c] = __ldcg(drow + par * w + c);
         }
       }
       __syncthreads();
-    }
+    } else {
     bv = T(-1);
     bi = 0x7fffffff;
     int bw = 0;
@@ -390,47 +411,49 @@ __global__ void __launch_bounds__(COOP_THREADS)
     }
     __syncthreads();
     }
-    const int p = s_row;
-    const bool zero = s_zero;
-    for (int c = tid; c < w; c += COOP_THREADS) {
-      T2 v;
-      if (p == dr || s_win < 0) {
-        const T2 *src = drow + par * w + c;
-        v = __ldcg(src);
-      } else {
-        v = __ldcg(cdata + (int64_t)(par * G + s_win) * w + c);
+      const int p = s_row;
+      for (int c = tid; c < w; c += COOP_THREADS) {
+        T2 v;
+        if (p == dr || s_win < 0) {
+          const T2 *src = drow + par * w + c;
+          v = __ldcg(src);
+        } else {
+          v = __ldcg(cdata + (int64_t)(par * G + s_win) * w + c);
+        }
+        prow[c] = v;
       }
-      prow[c] = v;
+      __syncthreads();
+      if (p != dr) {
+        if (dr >= rbeg && dr < rend)
+          for (int c = tid; c < w; c += COOP_THREADS) P[(dr - rbeg) * w + c] = prow[c];
+        if (p >= rbeg && p < rend)
+          for (int c = tid; c < w; c += COOP_THREADS) P[(p - rbeg) * w + c] = __ldcg(drow + par * w + c);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    if (p != dr) {
-      if (dr >= rbeg && dr < rend)
-        for (int c = tid; c < w; c += COOP_THREADS) P[(dr - rbeg) * w + c] = prow[c];
-      if (p >= rbeg && p < rend)
-        for (int c = tid; c < w; c += COOP_THREADS) P[(p - rbeg) * w + c] = __ldcg(drow + par * w + c);
-    }
-    __syncthreads();
-    // scale column j below the diagonal, then the rank-1 update of columns > j
+    // scale column j below the diagonal and the rank-1 update of columns > j,
+    // one warp per row (the row's multiplier is read before it is overwritten)
+    const bool zero = s_zero;
     const T2 pv = prow[j];
     const cx<T> rp = zero ? cx<T>{0, 0} : crecip(cx<T>{pv.x, pv.y});
-    for (int i = tid; i < nloc; i += COOP_THREADS) {
-      if (rbeg + i <= dr || zero) continue;
-      const T2 a = P[i * w + j];
-      const cx<T> l = cmul(cx<T>{a.x, a.y}, rp);
-      P[i * w + j] = V2<T>::make(l.r, l.i);
-    }
-    __syncthreads();
-    const int wr = w - j - 1;
-    if (wr > 0)
-      for (int idx = tid; idx < nloc * wr; idx += COOP_THREADS) {
-        const int i = idx / wr, c = j + 1 + idx % wr;
-        if (rbeg + i <= dr) continue;
-        const T2 l = P[i * w + j], u = prow[c];
+    for (int i = wid; i < nloc; i += COOP_THREADS / 32) {
+      if (rbeg + i <= dr) continue;
+      const T2 a0 = P[i * w + j];
+      T2 l = a0;
+      if (!zero) {
+        const cx<T> ls = cmul(cx<T>{a0.x, a0.y}, rp);
+        l = V2<T>::make(ls.r, ls.i);
+      }
+      __syncwarp();
+      if (lane == 0) P[i * w + j] = l;
+      for (int c = j + 1 + lane; c < w; c += 32) {
+        const T2 u = prow[c];
         T2 a = P[i * w + c];
         a.x -= l.x * u.x - l.y * u.y;
         a.y -= l.x * u.y + l.y * u.x;
         P[i * w + c] = a;
       }
+    }
     __syncthreads();
   }
   for (int idx = tid; idx < nloc * w; idx += COOP_THREADS) {
