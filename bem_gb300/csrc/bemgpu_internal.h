@@ -200,6 +200,8 @@ int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int 
 int bem_ctri_inverses(bemgpu_ctx_s *ctx, const float *LU, int64_t ld, int n, float *Linv, float *Uinv,
                       cudaStream_t st);
 // B <- U^{-1} L^{-1} P B with the explicit inverses (tmp: n x nrhs complex64).
+int bem_capply_inverse_identity(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv,
+                                int row0, float *B, int64_t ldb, int nrhs, float *tmp, cudaStream_t st);
 int bem_capply_inverse(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv, float *B,
                        int64_t ldb, int nrhs, float *tmp, cudaStream_t st);
 // complex64 GEMM: tensor cores where the shape allows (gemm_tc.cu), else FMA pipes.

@@ -1272,6 +1272,48 @@ int bem_ctri_inverses(bemgpu_ctx_s *ctx, const float *LU, int64_t ld, int n, flo
   return BEMGPU_OK;
 }
 
+namespace {
+
+// T(:, c) = Linv(:, pos(row0 + c)): L^-1 applied to the interchanged identity
+// column row0 + c, where pos follows that column's 1 through the row
+// interchanges ipiv[0..n) (laswp order).
+__global__ void gather_linv_cols_kernel(const float *__restrict__ Linv, int n, const int *__restrict__ ipiv, int row0,
+                                        int ncols, float *__restrict__ T) {
+  __shared__ int s_pos;
+  const int c = blockIdx.x;
+  if (c >= ncols) return;
+  if (threadIdx.x == 0) {
+    int pos = row0 + c;
+    for (int k = 0; k < n; k++) {
+      const int p = ipiv[k];
+      if (pos == k) pos = p;
+      else if (pos == p) pos = k;
+    }
+    s_pos = pos;
+  }
+  __syncthreads();
+  const float2 *src = reinterpret_cast<const float2 *>(Linv) + (int64_t)n * s_pos;
+  float2 *dst = reinterpret_cast<float2 *>(T) + (int64_t)n * c;
+  for (int r = threadIdx.x; r < n; r += blockDim.x) dst[r] = src[r];
+}
+
+}  // namespace
+
+// B = W32^-1 E_t for the identity columns row0 .. row0 + nrhs: the interchanges
+// and L^-1 reduce to gathering columns of L^-1, then one product with U^-1.
+int bem_capply_inverse_identity(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv,
+                                int row0, float *B, int64_t ldb, int nrhs, float *tmp, cudaStream_t st) {
+  {
+    ProfScope ps(ctx, BEMGPU_K_SOLVE_GEMM, st, 0.0, 16.0 * (double)n * nrhs);
+    gather_linv_cols_kernel<<<nrhs, 256, 0, st>>>(Linv, n, d_ipiv, row0, nrhs, tmp);
+    ctx->launches++;
+  }
+  if (ctx->gemm_engine != 2 && n >= 64 && nrhs >= 64)
+    return bem_cgemm_tc(ctx, BEMGPU_K_SOLVE_GEMM, n, nrhs, n, 1.f, Uinv, n, tmp, n, B, ldb, TC_OUT_F32, 0, st, 2);
+  const float one[2] = {1.f, 0.f}, zero[2] = {0.f, 0.f};
+  return bem_cgemm(ctx, BEMGPU_K_SOLVE_GEMM, 'N', n, nrhs, n, one, Uinv, n, tmp, n, zero, B, ldb, st);
+}
+
 int bem_capply_inverse(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv, float *B,
                        int64_t ldb, int nrhs, float *tmp, cudaStream_t st) {
   {

@@ -175,13 +175,6 @@ __global__ void identity_cols_c128_kernel(double *Y, int64_t ld, int n, int row0
   reinterpret_cast<double2 *>(Y)[r + ld * (int64_t)c] = make_double2(r == row0 + c ? 1.0 : 0.0, 0.0);
 }
 
-__global__ void identity_cols_c64_kernel(float *Y, int64_t ld, int n, int row0, int ncols) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
-  if (r >= n) return;
-  reinterpret_cast<float2 *>(Y)[r + ld * (int64_t)c] = make_float2(r == row0 + c ? 1.f : 0.f, 0.f);
-}
-
 // out = 1/4 sum of the np partial (re, im) pairs; one CTA of 256 threads, fixed
 // summation order (deterministic).
 __global__ void __launch_bounds__(256) trace_final_kernel(const double *partial, int np, double *out) {
@@ -385,9 +378,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   if (!rc) rc = bem_ctri_inverses(ctx, b.W32, n, n, b.Linv, b.Uinv, st);
   if (rc) return rc;
   cudaEventRecord(ev[2], st);
-  identity_cols_c64_kernel<<<gm, 256, 0, st>>>(b.R32, n, n, ns2, nt2);
-  ctx->launches++;
-  rc = bem_capply_inverse(ctx, b.Linv, b.Uinv, n, b.ipiv, b.R32, n, nt2, b.T32, st);
+  rc = bem_capply_inverse_identity(ctx, b.Linv, b.Uinv, n, b.ipiv, ns2, b.R32, n, nt2, b.T32, st);
   if (rc) return rc;
   update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 0, nullptr);
   ctx->launches++;
