@@ -95,6 +95,7 @@ struct bemgpu_ctx_s {
   int gemm_engine = 0;   // complex64 LU/solve GEMMs: 0 tensor cores where possible, 2 FMA pipes only
   int acc_engine = 0;    // residual/trace GEMMs with FP64 output: same choices
   int solver = 0;        // mixed path: 0 complex64 with FP64-class escalation, 1 complex64, 2 FP64-class
+  double escalate_tol = 1e-6;  // complex64 refinement error estimate above which the solve escalates
   // live kernel statistics
   bool prof = false;
   struct ProfRec {

@@ -425,7 +425,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     if (err < 3e-7 || err > 0.5 * err_prev) break;
   }
   int solver = 1;
-  if (ctx->solver == 0 && !(err <= 1e-6)) {
+  if (ctx->solver == 0 && !(err <= ctx->escalate_tol)) {
     // the complex64 factors are not accurate enough for this W (refinement
     // diverged or stalled above the tolerance, or a zero pivot): factor W in
     // FP64-class arithmetic on the tensor cores and refine with that

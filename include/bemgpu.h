@@ -112,6 +112,9 @@ int bemgpu_ctx_set_engines(bemgpu_ctx_t ctx, int gemm, int acc64);
  * FP64-class tensor-core LU when its refinement does not converge (default);
  * 1 = complex64 only; 2 = FP64-class only.  No reference counterpart. */
 int bemgpu_ctx_set_solver(bemgpu_ctx_t ctx, int mode);
+/* Error estimate of the complex64 refinement above which mode 0 escalates to
+ * the FP64-class factorization (default 1e-6, the mixed path's bound). */
+int bemgpu_ctx_set_escalation_tol(bemgpu_ctx_t ctx, double tol);
 /* Failure-path self-test: one kernel polls a flag that nothing sets, gives up
  * after `spins` polls (or about a second), and records a timeout exactly as the
  * library's bounded waits do; returns BEMGPU_ERR_TIMEOUT and leaves the context

@@ -111,3 +111,26 @@ def test_fp64_class_tensor_core_lu_matches_fp64_path():
         info = {}
         P0 = api.CalcHeatTransfer(1e-6, eV, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
         assert info["solver"] == 1 and abs(P0 / P64 - 1) < 1e-6
+
+
+def test_escalation_to_fp64_class_lu():
+    """Mode 0 escalates when the complex64 refinement's error estimate stays
+    above the tolerance: with a tolerance no estimate can meet, every solve
+    takes the FP64-class factorization and still meets the FP64 path."""
+    v, t = mesh.icosphere(1.0, 2, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    b1 = b2.translated(mesh.gap_translation(v, v, 0.1))
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    ctx = api.Context(0)
+    top, s, tt = api.parseShapes(b1, b2, d, d, ctx)
+    L = _lib.load()
+    assert L.bemgpu_ctx_set_escalation_tol(ctx.handle, 0.0) == 0
+    P64 = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, tt, precision=_lib.PREC_FP64)
+    info = {}
+    P = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+    assert info["solver"] == 2 and info["err_est"] < 1e-6
+    assert abs(P / P64 - 1) < 1e-8
+    assert L.bemgpu_ctx_set_escalation_tol(ctx.handle, 1e-6) == 0
+    info = {}
+    api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+    assert info["solver"] == 1
