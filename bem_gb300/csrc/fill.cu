@@ -951,6 +951,131 @@ __device__ __forceinline__ df warp_sum_df(df v) {
 }
 
 // DF: the smooth inner rule in double-float (near_inner_df), else FP64.
+// The rest of one near pair in double-float once its nine L and K sums are in
+// acc (spread over the warp's lanes): the warp sums, the neighbour-edge K
+// correction of src/Impedance.cpp:301-324 (near_edge_df), and the scatter of
+// the nine (c L, c K) into the half-pair blocks as float pairs.
+__device__ __noinline__ void near_finish_df(const TriRec &T, const TriRec &S, int same, const NearPairDF &pc,
+                                            const NearAccDF &acc, HalfPairBlock *H, int ntr) {
+  const int lane = threadIdx.x & 31;
+  const int nht = T.nh, nhs = S.nh;
+  z1 L[9], K[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    L[k] = {df_to_double(warp_sum_df(acc.L[k].r)), df_to_double(warp_sum_df(acc.L[k].i))};
+    K[k] = {df_to_double(warp_sum_df(acc.K[k].r)), df_to_double(warp_sum_df(acc.K[k].i))};
+  }
+  if (!same) {
+    df3 Kd[3][3];
+    const df z = {0.f, 0.f};
+#pragma unroll
+    for (int e = 0; e < 3; e++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) Kd[e][i] = {z, z, z};
+    for (int idx = lane; idx < 45; idx += 32) {
+      const int e = idx / 15, q = idx - e * 15;
+      const df3 v0 = e == 0 ? pc.Sf.p0 : (e == 1 ? pc.Sf.p1 : pc.Sf.p2);
+      const df3 v1 = e == 0 ? pc.Sf.v01 : (e == 1 ? pc.Sf.v12 : pc.Sf.v20);
+      const df3 v = df3_add(v0, df3_scale(df_make(c_line15[q][0]), v1));
+      near_edge_df(pc, nht, v, df_make(c_line15[q][1]), Kd[e]);
+    }
+    d3 Ke[3][3];
+#pragma unroll
+    for (int e = 0; e < 3; e++)
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+        Ke[e][i] = {df_to_double(warp_sum_df(Kd[e][i].x)), df_to_double(warp_sum_df(Kd[e][i].y)),
+                    df_to_double(warp_sum_df(Kd[e][i].z))};
+    const double c = 0.125 * T.Ai * S.Ai;
+    const d3 m01 = ld3(S.m01), m12 = ld3(S.m12), m20 = ld3(S.m20);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        if (i >= nht || j >= nhs) continue;
+        const d3 v = ld3(T.hp0[i]) - ld3(S.hp0[j]);
+        K[i * 3 + j].r += c * (dot(cross(v, m01), Ke[0][i]) / S.nv01i + dot(cross(v, m12), Ke[1][i]) / S.nv12i +
+                               dot(cross(v, m20), Ke[2][i]) / S.nv20i);
+      }
+  }
+  if (lane < nht * nhs) {
+    const int i = lane / nhs, j = lane - (lane / nhs) * nhs;
+    z1 Lv = {0, 0}, Kv = {0, 0};
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      if (k == i * 3 + j) { Lv = L[k]; Kv = K[k]; }
+    const double c = scatter_coef(T, i, S, j);
+    const z1 cL = zscale(c, Lv), cK = zscale(c, Kv);
+    store_block_df(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], df_make(cL.r), df_make(cL.i), df_make(cK.r),
+                   df_make(cK.i));
+  }
+}
+
+// Near pairs in double-float, two pairs per warp: the 2 x 105 outer nodes of
+// the pair couple are spread over the lanes in 7 rounds of 32 (94 % of the
+// lanes busy, against 82 % for 105 nodes in 4 rounds); each lane adds to the
+// sums of the pair its node belongs to, and the warp finishes the pairs one
+// after the other.
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_df_kernel(
+    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
+    GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
+  __shared__ __align__(16) float s_nodes[NEAR_WARPS][2][BEMGPU_TRI_RULE91_N][8];
+  __shared__ float s_outer[BEMGPU_TRI_RULE105_N][6];
+  __shared__ NearPairDF s_pc[NEAR_WARPS][2];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
+    for (int c = 0; c < 3; c++) {
+      const df v = df_make(c_rule105[u][c]);
+      s_outer[u][2 * c] = v.hi;
+      s_outer[u][2 * c + 1] = v.lo;
+    }
+  __syncthreads();
+  const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
+  for (int64_t p0 = 2 * ((int64_t)blockIdx.x * NEAR_WARPS + wid); p0 < npairs; p0 += 2 * nw) {
+    const int np2 = p0 + 1 < npairs ? 2 : 1;
+    NearPair npr[2];
+    npr[0] = list[p0];
+    npr[1] = list[np2 == 2 ? p0 + 1 : p0];
+    // inner nodes l = r_s - P_s and weights of both pairs, then their records
+    for (int it = lane; it < np2 * BEMGPU_TRI_RULE91_N; it += 32) {
+      const int k = it >= BEMGPU_TRI_RULE91_N ? 1 : 0, u = it - k * BEMGPU_TRI_RULE91_N;
+      const TriRec &S = Sr[npr[k].s];
+      const d3 l = c_rule91[u][0] * ld3(S.v01) + c_rule91[u][1] * ld3(S.v02);
+      const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const df v = df_make(vals[c]);
+        s_nodes[wid][k][u][2 * c] = v.hi;
+        s_nodes[wid][k][u][2 * c + 1] = v.lo;
+      }
+    }
+    if (lane < np2) near_pair_df_setup(Tr[npr[lane].t], Sr[npr[lane].s], g, s_pc[wid][lane]);
+    __syncwarp();
+    NearAccDF acc[2];
+    const df z = {0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      acc[0].L[k] = {z, z}; acc[0].K[k] = {z, z};
+      acc[1].L[k] = {z, z}; acc[1].K[k] = {z, z};
+    }
+    for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
+      const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
+      const NearPairDF &pc = s_pc[wid][k];
+      const float *o = s_outer[q];
+      const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
+      const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
+      const df3 rs = df3_sub(rt1, pc.sPs);
+      InnerMomDF mom;
+      near_inner_df<1>(s_nodes[wid][k], &rs, g, &mom);
+      near_outer_df(mom, pc, Tr[npr[k].t].nh, Sr[npr[k].s].nh, rt1, wq, acc[k]);
+    }
+    for (int k = 0; k < np2; k++)
+      near_finish_df(Tr[npr[k].t], Sr[npr[k].s], npr[k].same, s_pc[wid][k], acc[k], H, ntr);
+    __syncwarp();
+  }
+}
+
 template <bool DF>
 __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
@@ -1397,11 +1522,12 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   if (nl->n > 0) {
-    int64_t blocks = (nl->n + NEAR_WARPS - 1) / NEAR_WARPS;
+    const int per_block = mode == FILL_DF ? 2 * NEAR_WARPS : NEAR_WARPS;  // the df kernel takes two pairs per warp
+    int64_t blocks = (nl->n + per_block - 1) / per_block;
     int nb = (int)std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 16);
     ProfScope ps(ctx, BEMGPU_K_FILL_NEAR, stream, near_flops, near_bytes);
     if (mode == FILL_DF)
-      near_pairs_kernel<true><<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
+      near_pairs_df_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
     else
       near_pairs_kernel<false><<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
     ctx->launches++;
