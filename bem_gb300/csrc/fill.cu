@@ -1076,30 +1076,19 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_df_kernel(
   }
 }
 
-template <bool DF>
+// Near pairs in FP64 (the plain path), one pair per warp: lanes take the
+// outer nodes, each runs the 91-node smooth inner rule, the analytic singular
+// terms and the close-pair contraction; the warp sums, adds the neighbour-edge
+// K correction and scatters.
 __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
     GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
-  __shared__ double s_nodes[NEAR_WARPS][DF ? 1 : BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
-  __shared__ __align__(16) float s_nodes_df[NEAR_WARPS][DF ? BEMGPU_TRI_RULE91_N : 1][8];
-  // double-float path: the outer rule (xi1, xi2, w as df) and one pair record per warp
-  __shared__ float s_outer_df[DF ? BEMGPU_TRI_RULE105_N : 1][6];
-  __shared__ NearPairDF s_pc[DF ? NEAR_WARPS : 1];
+  __shared__ double s_nodes[NEAR_WARPS][BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   double(*nodes)[4] = s_nodes[wid];
-  float(*nodes_df)[8] = s_nodes_df[wid];
   const z1 ksq = {g.ksqr, g.ksqi};
   const z1 k2 = {g.k2r, g.k2i};
-  if (DF) {
-    for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
-      for (int c = 0; c < 3; c++) {
-        const df v = df_make(c_rule105[u][c]);
-        s_outer_df[u][2 * c] = v.hi;
-        s_outer_df[u][2 * c + 1] = v.lo;
-      }
-    __syncthreads();
-  }
   for (int64_t p = (int64_t)blockIdx.x * NEAR_WARPS + wid; p < npairs; p += (int64_t)gridDim.x * NEAR_WARPS) {
     const NearPair np = list[p];
     const TriRec &T = Tr[np.t];
@@ -1110,18 +1099,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
       const d3 v01s = ld3(S.v01), v02s = ld3(S.v02);
       for (int u = lane; u < BEMGPU_TRI_RULE91_N; u += 32) {
         const d3 l = c_rule91[u][0] * v01s + c_rule91[u][1] * v02s;
-        if (DF) {
-          const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
-#pragma unroll
-          for (int c = 0; c < 4; c++) {
-            const df v = df_make(vals[c]);
-            nodes_df[u][2 * c] = v.hi;
-            nodes_df[u][2 * c + 1] = v.lo;
-          }
-        } else {
-          nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
-          nodes[u][3] = c_rule91[u][2];
-        }
+        nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
+        nodes[u][3] = c_rule91[u][2];
       }
     }
     __syncwarp();
@@ -1133,30 +1112,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     for (int k = 0; k < 9; k++) { L[k] = {0, 0}; K[k] = {0, 0}; }
     const d3 nS = ld3(S.n);
     const double Ai2 = 0.5 * S.Ai;
-    if (DF) {
-      NearPairDF &pc = s_pc[DF ? wid : 0];
-      if (lane == 0) near_pair_df_setup(T, S, g, pc);
-      __syncwarp();
-      NearAccDF acc;
-      const df z = {0.f, 0.f};
-#pragma unroll
-      for (int k = 0; k < 9; k++) { acc.L[k] = {z, z}; acc.K[k] = {z, z}; }
-      for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
-        const float *o = s_outer_df[DF ? q : 0];
-        const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
-        const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
-        const df3 rs = df3_sub(rt1, pc.sPs);
-        InnerMomDF mom;
-        near_inner_df<1>(nodes_df, &rs, g, &mom);
-        near_outer_df(mom, pc, nht, nhs, rt1, wq, acc);
-      }
-#pragma unroll
-      for (int k = 0; k < 9; k++) {
-        L[k] = {df_to_double(warp_sum_df(acc.L[k].r)), df_to_double(warp_sum_df(acc.L[k].i))};
-        K[k] = {df_to_double(warp_sum_df(acc.K[k].r)), df_to_double(warp_sum_df(acc.K[k].i))};
-      }
-    }
-    for (int q = lane; !DF && q < BEMGPU_TRI_RULE105_N; q += 32) {
+    for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
       const double w = c_rule105[q][2];
       const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
       const d3 rts = rt - Ps;
@@ -1238,7 +1194,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
       }
     }
 #pragma unroll
-    for (int k = 0; !DF && k < 9; k++) {
+    for (int k = 0; k < 9; k++) {
       L[k].r = warp_sum(L[k].r); L[k].i = warp_sum(L[k].i);
       K[k].r = warp_sum(K[k].r); K[k].i = warp_sum(K[k].i);
     }
@@ -1251,29 +1207,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
 #pragma unroll
         for (int i = 0; i < 3; i++) Ke[e][i] = {0, 0, 0};
       const d3 nT = ld3(T.n);
-      if (DF) {
-        const NearPairDF &pc = s_pc[DF ? wid : 0];
-        df3 Kd[3][3];
-        const df z = {0.f, 0.f};
-#pragma unroll
-        for (int e = 0; e < 3; e++)
-#pragma unroll
-          for (int i = 0; i < 3; i++) Kd[e][i] = {z, z, z};
-        for (int idx = lane; idx < 45; idx += 32) {
-          const int e = idx / 15, q = idx - e * 15;
-          const df3 v0 = e == 0 ? pc.Sf.p0 : (e == 1 ? pc.Sf.p1 : pc.Sf.p2);
-          const df3 v1 = e == 0 ? pc.Sf.v01 : (e == 1 ? pc.Sf.v12 : pc.Sf.v20);
-          const df3 v = df3_add(v0, df3_scale(df_make(c_line15[q][0]), v1));
-          near_edge_df(pc, nht, v, df_make(c_line15[q][1]), Kd[e]);
-        }
-#pragma unroll
-        for (int e = 0; e < 3; e++)
-#pragma unroll
-          for (int i = 0; i < 3; i++)
-            Ke[e][i] = {df_to_double(warp_sum_df(Kd[e][i].x)), df_to_double(warp_sum_df(Kd[e][i].y)),
-                        df_to_double(warp_sum_df(Kd[e][i].z))};
-      }
-      for (int idx = lane; !DF && idx < 45; idx += 32) {
+      for (int idx = lane; idx < 45; idx += 32) {
         const int e = idx / 15, q = idx - e * 15;
         const d3 v0 = e == 0 ? ld3(S.p0) : (e == 1 ? ld3(S.p1) : ld3(S.p2));
         const d3 v1 = e == 0 ? ld3(S.v01) : (e == 1 ? ld3(S.v12) : ld3(S.v20));
@@ -1294,7 +1228,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
         }
       }
 #pragma unroll
-      for (int e = 0; !DF && e < 3; e++)
+      for (int e = 0; e < 3; e++)
 #pragma unroll
         for (int i = 0; i < 3; i++) {
           Ke[e][i].x = warp_sum(Ke[e][i].x);
@@ -1320,12 +1254,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
       for (int k = 0; k < 9; k++)
         if (k == i * 3 + j) { Lv = L[k]; Kv = K[k]; }
       const double c = scatter_coef(T, i, S, j);
-      const z1 cL = zscale(c, Lv), cK = zscale(c, Kv);
-      if (DF)
-        store_block_df(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], df_make(cL.r), df_make(cL.i),
-                       df_make(cK.r), df_make(cK.i));
-      else
-        store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], cL, cK);
+      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, Lv), zscale(c, Kv));
     }
     __syncwarp();
   }
@@ -1529,7 +1458,7 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
     if (mode == FILL_DF)
       near_pairs_df_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
     else
-      near_pairs_kernel<false><<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
+      near_pairs_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -1690,7 +1619,7 @@ extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree
   if (!pairs.empty()) {
     const int64_t np = (int64_t)pairs.size();
     const int nb = (int)std::min<int64_t>((np + NEAR_WARPS - 1) / NEAR_WARPS, (int64_t)ctx->num_sms * 16);
-    near_pairs_kernel<false><<<nb, 32 * NEAR_WARPS, 0, st>>>(t->d_rec, s->d_rec, dnear, np, gd, H, t->nrwg);
+    near_pairs_kernel<<<nb, 32 * NEAR_WARPS, 0, st>>>(t->d_rec, s->d_rec, dnear, np, gd, H, t->nrwg);
     ctx->launches++;
   }
   dim3 gblk(128);
