@@ -543,8 +543,13 @@ __global__ void __launch_bounds__(256) trsm_block_kernel(const T *Ad, int64_t ld
 template <typename T, int BM, int BN, int TM, int TN, int BK, bool CONJ_A, typename TC = T, bool COMP = false>
 __global__ void __launch_bounds__(256) cgemm_fma_kernel(int m, int n, int k, cx<T> alpha, const T *__restrict__ A,
                                                         int64_t lda, const T *__restrict__ B, int64_t ldb, cx<TC> beta,
-                                                        TC *__restrict__ C, int64_t ldc) {
+                                                        TC *__restrict__ C, int64_t ldc, int64_t sA, int64_t sB,
+                                                        int64_t sC) {
   typedef typename V2<T>::type T2;
+  // strided batch: problem blockIdx.z (strides in elements of T / TC)
+  A += sA * blockIdx.z;
+  B += sB * blockIdx.z;
+  C += sC * blockIdx.z;
   constexpr int TX = BN / TN, TY = BM / TM;
   static_assert(TX * TY == 256, "256 threads");
   __shared__ T2 As[BK][BM];
@@ -695,10 +700,10 @@ int gemm_fma(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const T
                2.0 * sizeof(T) * ((double)m * k + (double)k * n + 2.0 * m * n));
   if (opA == 'C') {
     cgemm_fma_kernel<T, G::BM, G::BN, G::TM, G::TN, G::BK, true>
-        <<<grd, 256, 0, stream>>>(m, n, k, al, A, lda, B, ldb, be, C, ldc);
+        <<<grd, 256, 0, stream>>>(m, n, k, al, A, lda, B, ldb, be, C, ldc, 0, 0, 0);
   } else {
     cgemm_fma_kernel<T, G::BM, G::BN, G::TM, G::TN, G::BK, false>
-        <<<grd, 256, 0, stream>>>(m, n, k, al, A, lda, B, ldb, be, C, ldc);
+        <<<grd, 256, 0, stream>>>(m, n, k, al, A, lda, B, ldb, be, C, ldc, 0, 0, 0);
   }
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
@@ -727,7 +732,7 @@ int bem_cgemm_comp64_fma(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, const
   cx<double> be = {beta[0], beta[1]};
   ProfScope ps(ctx, kind, stream, 8.0 * m * n * k, 8.0 * ((double)m * k + (double)k * n) + 32.0 * m * n);
   cgemm_fma_kernel<float, 64, 64, 4, 4, 8, false, double, true>
-      <<<grd, 256, 0, stream>>>(m, n, k, al, A, lda, B, ldb, be, C, ldc);
+      <<<grd, 256, 0, stream>>>(m, n, k, al, A, lda, B, ldb, be, C, ldc, 0, 0, 0);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   return BEMGPU_OK;
@@ -1213,26 +1218,55 @@ __global__ void tri_extract_kernel(const float *__restrict__ LU, int64_t ld, int
   reinterpret_cast<float2 *>(D)[r + (int64_t)n * c] = v;
 }
 
-// Recursive in-place inversion of the triangular block X[o:o+m, o:o+m] (ld n).
-int tri_inv_rec(bemgpu_ctx_s *ctx, bool upper, float *X, int64_t n, int o, int m, float *tmp, cudaStream_t st) {
-  float *Xo = X + 2 * ((int64_t)o + n * o);
-  if (m <= NB) return BEMGPU_OK;  // diagonal blocks are inverted up front (tri_inv_block_kernel)
-  const int m1 = ((m / 2 + NB - 1) / NB) * NB, m2 = m - m1;
-  int rc = tri_inv_rec(ctx, upper, X, n, o, m1, tmp, st);
-  if (!rc) rc = tri_inv_rec(ctx, upper, X, n, o + m1, m2, tmp, st);
-  if (rc) return rc;
+// In-place inversion of a triangle X (n x n, ld n) whose 64 x 64 diagonal
+// blocks are already inverted (tri_inv_block_kernel), bottom up: at block size
+// b the pairs of adjacent inverted b-blocks at offsets o = 0, 2b, 4b, ... are
+// joined, lower: X21 = -X22 (L21 X11), upper: X12 = -X11 (U12 X22).  Below
+// 512 all full pairs of a level are two strided-batch launches on the FMA
+// pipes (hundreds of tiny products become six launches); from 512 up each
+// pair is two tensor-core products.
+int tri_inv_bottom_up(bemgpu_ctx_s *ctx, bool upper, float *X, int n, float *tmp, cudaStream_t st) {
   const float one[2] = {1.f, 0.f}, mone[2] = {-1.f, 0.f}, zero[2] = {0.f, 0.f};
-  float *X11 = Xo, *X22 = X + 2 * ((int64_t)(o + m1) + n * (o + m1));
-  if (!upper) {
-    // X21 = -X22 (L21 X11): tmp (m2 x m1) = L21 X11, then X21 = -X22 tmp
-    float *X21 = X + 2 * ((int64_t)(o + m1) + n * o);
-    rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m2, m1, m1, one, X21, n, X11, n, zero, tmp, m2, st);
-    if (!rc) rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m2, m1, m2, mone, X22, n, tmp, m2, zero, X21, n, st);
-  } else {
-    // X12 = -X11 (U12 X22): tmp (m1 x m2) = U12 X22, then X12 = -X11 tmp
-    float *X12 = X + 2 * ((int64_t)o + n * (o + m1));
-    rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m1, m2, m2, one, X12, n, X22, n, zero, tmp, m1, st);
-    if (!rc) rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', m1, m2, m1, mone, X11, n, tmp, m1, zero, X12, n, st);
+  int rc = BEMGPU_OK;
+  for (int b = NB; b < n && !rc; b *= 2) {
+    const int full = n / (2 * b);  // pairs with both blocks b wide
+    const int o_last = full * 2 * b;
+    const int b2_last = std::min(b, n - o_last - b);  // ragged pair at o_last, if any
+    auto at = [&](int r, int c) { return X + 2 * ((int64_t)r + (int64_t)n * c); };
+    if (b < 512 && full > 0) {
+      typedef GemmCfg<float> G;
+      const dim3 grd((b + G::BM - 1) / G::BM, (b + G::BN - 1) / G::BN, full);
+      const int64_t sx = 2 * ((int64_t)2 * b + (int64_t)n * 2 * b), st_ = 2 * (int64_t)b * b;
+      const cx<float> c1 = {1.f, 0.f}, cm1 = {-1.f, 0.f}, c0 = {0.f, 0.f};
+      ProfScope ps(ctx, BEMGPU_K_TRSM, st, 16.0 * full * (double)b * b * b, 48.0 * full * (double)b * b);
+      if (!upper) {
+        cgemm_fma_kernel<float, G::BM, G::BN, G::TM, G::TN, G::BK, false><<<grd, 256, 0, st>>>(
+            b, b, b, c1, at(b, 0), n, at(0, 0), n, c0, tmp, b, sx, sx, st_);
+        cgemm_fma_kernel<float, G::BM, G::BN, G::TM, G::TN, G::BK, false><<<grd, 256, 0, st>>>(
+            b, b, b, cm1, at(b, b), n, tmp, b, c0, at(b, 0), n, sx, st_, sx);
+      } else {
+        cgemm_fma_kernel<float, G::BM, G::BN, G::TM, G::TN, G::BK, false><<<grd, 256, 0, st>>>(
+            b, b, b, c1, at(0, b), n, at(b, b), n, c0, tmp, b, sx, sx, st_);
+        cgemm_fma_kernel<float, G::BM, G::BN, G::TM, G::TN, G::BK, false><<<grd, 256, 0, st>>>(
+            b, b, b, cm1, at(0, 0), n, tmp, b, c0, at(0, b), n, sx, st_, sx);
+      }
+      ctx->launches += 2;
+      BEM_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    for (int pi = (b < 512 ? full : 0); pi <= full && !rc; pi++) {
+      const int o = pi * 2 * b, bb = pi < full ? b : b2_last;
+      if (bb <= 0) continue;
+      if (!upper) {
+        rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', bb, b, b, one, at(o + b, o), n, at(o, o), n, zero, tmp, bb, st);
+        if (!rc)
+          rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', bb, b, bb, mone, at(o + b, o + b), n, tmp, bb, zero, at(o + b, o), n,
+                         st);
+      } else {
+        rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', b, bb, bb, one, at(o, o + b), n, at(o + b, o + b), n, zero, tmp, b, st);
+        if (!rc)
+          rc = bem_cgemm(ctx, BEMGPU_K_TRSM, 'N', b, bb, b, mone, at(o, o), n, tmp, b, zero, at(o, o + b), n, st);
+      }
+    }
   }
   return rc;
 }
@@ -1265,8 +1299,8 @@ int bem_ctri_inverses(bemgpu_ctx_s *ctx, const float *LU, int64_t ld, int n, flo
     tri_inv_block_kernel<true><<<nb, 64, TRI_INV_SMEM, st>>>(Uinv, n, n);
     ctx->launches += 2;
   }
-  int rc = tri_inv_rec(ctx, false, Linv, n, 0, n, tmp, st);
-  if (!rc) rc = tri_inv_rec(ctx, true, Uinv, n, 0, n, tmp, st);
+  int rc = tri_inv_bottom_up(ctx, false, Linv, n, tmp, st);
+  if (!rc) rc = tri_inv_bottom_up(ctx, true, Uinv, n, tmp, st);
   if (rc) return rc;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   return BEMGPU_OK;
