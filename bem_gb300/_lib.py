@@ -38,6 +38,7 @@ EXPORTED = [
     "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error", "bemgpu_farm_set_budget",
     "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint",
     "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol",
+    "bemgpu_zgemm_exact_quantized",
 ]
 
 
@@ -104,6 +105,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_cgemm": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_cgemm_acc64": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_zgemm_exact": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
+        "bemgpu_zgemm_exact_quantized": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32]),
         "bemgpu_heat_transfer": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(ctypes.c_double), P(SolveInfo)]),
         "bemgpu_farm_create": (i32, [i32, i32, P(vp)]),
         "bemgpu_farm_destroy": (i32, [vp]),

@@ -229,12 +229,15 @@ struct ExactOperand {
   int rows = 0, k = 0, slices = 0;
   int64_t rows_p = 0, kp = 0;
   bool is_a = true;
+  bool exact = false;   // B operand replaced by its quantized value (its slices are exact)
 };
 bool bem_exact_available();
 // Slices sign * M (complex128, column-major, leading dimension ld): role A:
 // M is rows x k; role B: M is k x rows.  Workspace named by `name`.
+// quantize: M itself (role B, sign 1) is overwritten with the value its
+// slices represent, so that products with it keep every level of A's slices.
 int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
-                   double sign, int slices, ExactOperand &op, cudaStream_t st);
+                   double sign, int slices, ExactOperand &op, cudaStream_t st, double *quantize = nullptr);
 // C (+)= A B from prepared operands (complex128 C, column-major, ldc).
 int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const ExactOperand &b, double *C, int64_t ldc,
                    int accumulate, cudaStream_t st);

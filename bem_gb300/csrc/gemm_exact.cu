@@ -47,26 +47,61 @@ constexpr int EX_SCALE_TARGET = 0;  // largest magnitude of a matrix is scaled t
                                     // and their sums stay inside FP32's range
 constexpr int EX_FLUSH_E = -80;     // blocks whose maximum (scaled) is below 2^-80 are zero (slices >= 2^-120)
 
-template <int SL>
-__host__ __device__ constexpr int ex_stage_bytes() { return SL * (EX_A_TILE + EX_B_TILE); }
-template <int SL>
-__host__ __device__ constexpr int ex_smem_bytes() { return EX_STAGES * ex_stage_bytes<SL>() + 1024 + 256; }
+template <int SA, int SB>
+__host__ __device__ constexpr int ex_stage_bytes() { return SA * EX_A_TILE + SB * EX_B_TILE; }
+template <int SA, int SB>
+__host__ __device__ constexpr int ex_smem_bytes() { return EX_STAGES * ex_stage_bytes<SA, SB>() + 1024 + 256; }
 
-// product p (level-major order) -> level, slice of A, slice of B
-__host__ __device__ constexpr int ex_level(int p) { return p < 1 ? 0 : p < 3 ? 1 : p < 6 ? 2 : p < 10 ? 3 : 4; }
-__host__ __device__ constexpr int ex_first(int level) { return level * (level + 1) / 2; }
+// The slice products of an (SA, SB) product: (a, b) with a < SA, b < SB and
+// level a + b < SA, in level-major order (a ascending within a level).  SA =
+// SB is the truncated square of a plain product; SB < SA multiplies A by an
+// operand that its SB slices represent exactly (quantized), so every product
+// up to level SA - 1 is kept.
+template <int SA, int SB>
+struct ExProducts {
+  __host__ __device__ static constexpr int count() {
+    int c = 0;
+    for (int L = 0; L < SA; L++)
+      for (int a = 0; a <= L && a < SA; a++)
+        if (L - a < SB) c++;
+    return c;
+  }
+  // level of product p (fst: a of product p)
+  __host__ __device__ static constexpr int level(int p) {
+    int c = 0;
+    for (int L = 0; L < SA; L++)
+      for (int a = 0; a <= L && a < SA; a++)
+        if (L - a < SB) {
+          if (c == p) return L;
+          c++;
+        }
+    return 0;
+  }
+  __host__ __device__ static constexpr int a_of(int p) {
+    int c = 0;
+    for (int L = 0; L < SA; L++)
+      for (int a = 0; a <= L && a < SA; a++)
+        if (L - a < SB) {
+          if (c == p) return a;
+          c++;
+        }
+    return 0;
+  }
+  __host__ __device__ static constexpr bool first(int p) { return p == 0 || level(p - 1) != level(p); }
+};
 
 struct ExMaps {
   CUtensorMap a[5];
   CUtensorMap b[5];
 };
 
-template <int SL>
+template <int SA, int SB>
 __global__ void __launch_bounds__(EX_THREADS, 1)
     ex_gemm_kernel(const __grid_constant__ ExMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf, int mvalid,
                    int nvalid, int accumulate, const int *__restrict__ shifts, int *err) {
-  constexpr int NP = SL * (SL + 1) / 2;
-  constexpr int STAGE = ex_stage_bytes<SL>();
+  typedef ExProducts<SA, SB> PR;
+  constexpr int NP = PR::count();
+  constexpr int STAGE = ex_stage_bytes<SA, SB>();
   extern __shared__ unsigned char ex_smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(ex_smem_raw) + 1023) &
                                                           ~(uintptr_t)1023);
@@ -112,10 +147,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         mbar_expect_tx(&full[s], STAGE);
         unsigned char *st = smem + s * STAGE;
 #pragma unroll
-        for (int a = 0; a < SL; a++) tma_load_2d(st + a * EX_A_TILE, &maps.a[a], kt * EX_BK, m0, &full[s]);
+        for (int a = 0; a < SA; a++) tma_load_2d(st + a * EX_A_TILE, &maps.a[a], kt * EX_BK, m0, &full[s]);
 #pragma unroll
-        for (int b = 0; b < SL; b++)
-          tma_load_2d(st + SL * EX_A_TILE + b * EX_B_TILE, &maps.b[b], kt * EX_BK, n0, &full[s]);
+        for (int b = 0; b < SB; b++)
+          tma_load_2d(st + SA * EX_A_TILE + b * EX_B_TILE, &maps.b[b], kt * EX_BK, n0, &full[s]);
         issued = kt + 1;
       }
       // copies still in flight after an early stop land before the CTA exits
@@ -139,10 +174,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         for (int ks = 0; ks < EX_BK / 16; ks++) {
 #pragma unroll
           for (int p = 0; p < NP; p++) {
-            const int level = ex_level(p), a = p - ex_first(level), bb = level - a;
+            const int level = PR::level(p), a = PR::a_of(p), bb = level - a;
             const uint64_t da = dbase + (uint64_t)((a * EX_A_TILE + ks * 32) >> 4);
-            const uint64_t db = dbase + (uint64_t)((SL * EX_A_TILE + bb * EX_B_TILE + ks * 32) >> 4);
-            const bool first = opening && ks == 0 && p == ex_first(level);
+            const uint64_t db = dbase + (uint64_t)((SA * EX_A_TILE + bb * EX_B_TILE + ks * 32) >> 4);
+            const bool first = opening && ks == 0 && PR::first(p);
             if (level <= 2)
               tc_mma(tmem + (uint32_t)((3 * b + level) * EX_BN), da, db, idesc, first ? 0u : 1u);
             else
@@ -195,7 +230,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[b]);
     }
-    if (ok && SL > 3) {
+    if (ok && SA > 3) {
       int got = 1;
       if (lane == 0) got = mbar_wait(fin, 0, err) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, got, 0) != 0;
@@ -207,10 +242,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
       float z3[8], z4[8];
 #pragma unroll
       for (int j = 0; j < 8; j++) z3[j] = z4[j] = 0.f;
-      if (ok && SL > 3) {
+      if (ok && SA > 3) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         tc_ld8(lane_base + (uint32_t)(6 * EX_BN) + 8 * q, z3);
-        if (SL > 4) tc_ld8(lane_base + (uint32_t)(7 * EX_BN) + 8 * q, z4);
+        if (SA > 4) tc_ld8(lane_base + (uint32_t)(7 * EX_BN) + 8 * q, z4);
       }
       if (ok && rho < mvalid) {
 #pragma unroll
@@ -349,10 +384,13 @@ __global__ void ex_prep_a_kernel(const double *__restrict__ A, int64_t lda, int 
 
 // B' slices (Np x Kp): row c = column c of complex128 B (k x n); blocks of 64
 // complex rows (two warps).
+// Bq: when given, B itself is replaced by the value its slices represent
+// exactly (quantized to the block fixed point), so that a product with it can
+// keep every slice level of the other operand.
 template <int SL>
 __global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int k, int n,
                                  const unsigned *amax, int *shift, __nv_bfloat16 *__restrict__ S, int64_t Np,
-                                 int64_t Kp) {
+                                 int64_t Kp, double *Bq) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   const bool active = 2 * q < Kp;
@@ -373,6 +411,15 @@ __global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int 
 #pragma unroll
   for (int l = 0; l < SL; l++)
     reinterpret_cast<__nv_bfloat162 *>(S + l * plane + i0)[0] = __halves2bfloat162(sr[l], si[l]);
+  if (Bq && c < n && q < k) {
+    double qr = 0.0, qi = 0.0;  // exact: at most 8 SL + 1 significant bits
+#pragma unroll
+    for (int l = 0; l < SL; l++) {
+      qr += (double)__bfloat162float(sr[l]);
+      qi += (double)__bfloat162float(si[l]);
+    }
+    reinterpret_cast<double2 *>(Bq)[q + ldb * (int64_t)c] = make_double2(ldexp(qr, -g), ldexp(qi, -g));
+  }
 }
 
 bool ex_maps(CUtensorMap *maps, const __nv_bfloat16 *S, int slices, int64_t rows, int64_t kp, int box_rows) {
@@ -396,7 +443,7 @@ size_t bem_exact_operand_bytes(bool is_a, int rows, int k, int slices) {
 }
 
 int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
-                   double sign, int slices, ExactOperand &op, cudaStream_t st) {
+                   double sign, int slices, ExactOperand &op, cudaStream_t st, double *quantize) {
   if (slices < 3 || slices > 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
   if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
@@ -413,6 +460,9 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
   op.kp = kp;
   op.slices = slices;
   op.is_a = is_a;
+  op.exact = quantize != nullptr;
+  if (quantize && (is_a || quantize != M || sign != 1.0))
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: only a B operand is quantized, in place, unscaled");
   unsigned *amax = reinterpret_cast<unsigned *>(op.aux + 8);
   {
     ProfScope ps(ctx, BEMGPU_K_SLICE, st, 0.0, 16.0 * (double)rows * k * 2 + 4.0 * slices * (double)rp * kp);
@@ -430,11 +480,11 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
         ex_prep_a_kernel<3><<<grid, 128, 0, st>>>(M, ld, rows, k, sign, amax, op.aux, S, rp, kp);
     } else {
       if (slices == 5)
-        ex_prep_b_kernel<5><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
+        ex_prep_b_kernel<5><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
       else if (slices == 4)
-        ex_prep_b_kernel<4><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
+        ex_prep_b_kernel<4><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
       else
-        ex_prep_b_kernel<3><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp);
+        ex_prep_b_kernel<3><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
     }
     ctx->launches++;
   }
@@ -444,24 +494,31 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
 
 int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const ExactOperand &b, double *C, int64_t ldc,
                    int accumulate, cudaStream_t st) {
-  // SL = the slices of B; A may carry more (its leading SL slices are used:
-  // products of levels < SL, error ~2^(-8 SL) of the blocks' maxima)
+  // A plain B: SB = SA = the slices of B (A may carry more; its leading ones
+  // are used), products of levels < SB, error ~2^(-8 SB) of the blocks'
+  // maxima.  A quantized B (exactly its SB slices): SA = the slices of A,
+  // every product of level < SA kept.
   if (!a.is_a || b.is_a || a.k != b.k || a.kp != b.kp || a.slices < b.slices)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: operands do not match");
-  const int m = a.rows, n = b.rows, SL = b.slices;
+  const int m = a.rows, n = b.rows, SB = b.slices, SA = b.exact ? a.slices : b.slices;
+  if (!((SA == SB && SA >= 3 && SA <= 5) || (SA == 5 && SB == 3)))
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: slices (%d, %d) not built", SA, SB);
+  const int SL = SB;
   ExMaps maps;
-  if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SL, a.rows_p, a.kp, EX_BM) ||
-      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SL, b.rows_p, b.kp, EX_BN))
+  if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SA, a.rows_p, a.kp, EX_BM) ||
+      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SB, b.rows_p, b.kp, EX_BN))
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "exact gemm: tensor map encoding failed");
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
   if (!err) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
   if (!ctx->ex_ready) {
-    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           ex_smem_bytes<5>()));
-    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           ex_smem_bytes<4>()));
-    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           ex_smem_bytes<3>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<5, 5>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<4, 4>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<3, 3>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<5, 3>()));
     ctx->ex_ready = true;
   }
   if (!ctx->tc_err_ready) {
@@ -473,22 +530,24 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   if (!shifts) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(shifts, a.aux, sizeof(int), cudaMemcpyDeviceToDevice, st));
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(shifts + 1, b.aux, sizeof(int), cudaMemcpyDeviceToDevice, st));
-  const int np = SL * (SL + 1) / 2;
   ProfScope ps(ctx, kind, st, 8.0 * m * (double)n * a.k,
-               2.0 * SL * ((double)a.rows_p * a.kp * ((b.rows_p + EX_BN - 1) / EX_BN) / 8.0 + (double)b.rows_p * b.kp) +
-                   16.0 * m * (double)n * (accumulate ? 2 : 1));
-  (void)np;
+               2.0 * SA * ((double)a.rows_p * a.kp * ((b.rows_p + EX_BN - 1) / EX_BN) / 8.0) +
+                   2.0 * SB * (double)b.rows_p * b.kp + 16.0 * m * (double)n * (accumulate ? 2 : 1));
+  (void)SL;
   const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / EX_BN));
   const int ktiles = (int)(a.kp / EX_BK);
-  if (SL == 5)
-    ex_gemm_kernel<5><<<grid, EX_THREADS, ex_smem_bytes<5>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
-                                                                    shifts, err);
-  else if (SL == 4)
-    ex_gemm_kernel<4><<<grid, EX_THREADS, ex_smem_bytes<4>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
-                                                                    shifts, err);
+  if (SA == 5 && SB == 3)
+    ex_gemm_kernel<5, 3><<<grid, EX_THREADS, ex_smem_bytes<5, 3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
+                                                                          accumulate, shifts, err);
+  else if (SA == 5)
+    ex_gemm_kernel<5, 5><<<grid, EX_THREADS, ex_smem_bytes<5, 5>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
+                                                                          accumulate, shifts, err);
+  else if (SA == 4)
+    ex_gemm_kernel<4, 4><<<grid, EX_THREADS, ex_smem_bytes<4, 4>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
+                                                                          accumulate, shifts, err);
   else
-    ex_gemm_kernel<3><<<grid, EX_THREADS, ex_smem_bytes<3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate,
-                                                                    shifts, err);
+    ex_gemm_kernel<3, 3><<<grid, EX_THREADS, ex_smem_bytes<3, 3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
+                                                                          accumulate, shifts, err);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   return BEMGPU_OK;
@@ -508,5 +567,23 @@ extern "C" int bemgpu_zgemm_exact(bemgpu_ctx_t ctx, int m, int n, int k, const d
   if (rc) return rc;
   BEM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   if (bem_tc_error(ctx, true)) return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "zgemm_exact: a pipeline wait ran out");
+  return BEMGPU_OK;
+}
+
+extern "C" int bemgpu_zgemm_exact_quantized(bemgpu_ctx_t ctx, int m, int n, int k, const double *dA, int64_t lda,
+                                            double *dB, int64_t ldb, double *dC, int64_t ldc, int accumulate) {
+  if (!ctx || !dA || !dB || !dC || m < 1 || n < 1 || k < 1 || lda < m || ldb < k || ldc < m)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "zgemm_exact_quantized: bad arguments");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (!bem_exact_available()) return bem_fail(ctx, BEMGPU_ERR_CUDA, "zgemm_exact_quantized: tensor maps unavailable");
+  ExactOperand a, b;
+  int rc = bem_exact_prep(ctx, "cabi_a", true, dA, lda, m, k, 1.0, 5, a, ctx->stream);
+  if (!rc) rc = bem_exact_prep(ctx, "cabi_b", false, dB, ldb, n, k, 1.0, 3, b, ctx->stream, dB);
+  if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_TRACE, a, b, dC, ldc, accumulate, ctx->stream);
+  if (rc) return rc;
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (bem_tc_error(ctx, true))
+    return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "zgemm_exact_quantized: a pipeline wait ran out");
   return BEMGPU_OK;
 }

@@ -398,7 +398,10 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     // steps add -W dY of the last correction (3-slice product)
     ExactOperand opY;
     if (iters == 0) {
-      rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, MIXED_SLICES, opY, st);
+      // the first iterate (complex64 accuracy) is quantized to 3 slices in
+      // place; W's 5 slices times those 3 then need 12 slice products, not 15,
+      // for the same 2^-40 residual
+      rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, DELTA_SLICES, opY, st, b.Y);
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
     } else {
       rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opY, st);

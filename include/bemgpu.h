@@ -212,6 +212,13 @@ int bemgpu_cgemm_acc64(bemgpu_ctx_t ctx, int m, int n, int k, const float *dA, i
  * residual and the trace (src/HeatTransfer.cpp:40-58).  Synchronous. */
 int bemgpu_zgemm_exact(bemgpu_ctx_t ctx, int m, int n, int k, const double *dA, int64_t lda, const double *dB,
                        int64_t ldb, double *dC, int64_t ldc, int accumulate, int slices);
+/* The same with B quantized in place to the 3-slice block fixed point (B is
+ * overwritten with the value its slices represent exactly) and A in 5 slices:
+ * every slice product up to level 4 is kept (12 products), so C = A B to
+ * ~2^-40 of |A||B| for the quantized B.  The refinement uses this form for
+ * the residual of its first, complex64-accurate iterate. */
+int bemgpu_zgemm_exact_quantized(bemgpu_ctx_t ctx, int m, int n, int k, const double *dA, int64_t lda, double *dB,
+                                 int64_t ldb, double *dC, int64_t ldc, int accumulate);
 
 /* ---- per-frequency solve ---- */
 /* CalcHeatTransfer: top is the two-body tree (s's RWGs first, then t's),

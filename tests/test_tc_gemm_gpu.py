@@ -200,3 +200,35 @@ def test_exact_gemm_dynamic_range_and_scaling():
     ref = A @ B
     scale = np.abs(A) @ np.abs(B)
     assert np.max(np.abs(got - ref) / scale) < 1e-9
+
+
+@pytest.mark.parametrize("m,n,k", [(64, 64, 16), (130, 70, 300), (300, 200, 1000)])
+def test_exact_gemm_with_quantized_b(m, n, k):
+    """B quantized in place to its 3-slice block fixed point, A in 5 slices:
+    the returned B differs from the input by at most ~2^-25 of its blocks'
+    maxima, and A times that quantized B is exact to ~2^-40 of the blocks'
+    maxima products (all 12 slice products of level <= 4 kept)."""
+    import torch
+    rng = np.random.default_rng(m + 7 * n + k)
+    A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))) * np.exp(rng.uniform(-8, 8, (k, n)))
+    C0 = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    ctx = api.default_context()
+    for acc in (0, 1):
+        dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+        dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+        dC = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda()
+        torch.cuda.synchronize()
+        rc = _lib.load().bemgpu_zgemm_exact_quantized(ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), m,
+                                                      ctypes.c_void_p(dB.data_ptr()), k,
+                                                      ctypes.c_void_p(dC.data_ptr()), m, acc)
+        assert rc == 0, _lib.load().bemgpu_ctx_last_error(ctx.handle)
+        Bq = dB.cpu().numpy().T
+        C = dC.cpu().numpy().T
+        assert np.max(np.abs(Bq - B)) <= 2.0 ** -23 * np.max(np.abs(B)), "quantization beyond its bound"
+        ref = A @ Bq + (C0 if acc else 0)
+        # the bound is per 64-deep K block, relative to the block maxima of a
+        # row of A and a column of B (B spans 7 decades here)
+        scale = k * np.outer(np.abs(A).max(axis=1), np.abs(Bq).max(axis=0))
+        err = np.max(np.abs(C - ref) / scale)
+        assert err < 2.0 ** -38, (acc, err)
