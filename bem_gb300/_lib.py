@@ -31,7 +31,7 @@ EXPORTED = [
     "bemgpu_ctx_create", "bemgpu_ctx_destroy", "bemgpu_ctx_last_error", "bemgpu_version",
     "bemgpu_ctx_stream", "bemgpu_ctx_launches", "bemgpu_ctx_set_engines", "bemgpu_prof_enable", "bemgpu_prof_query",
     "bemgpu_geom_create", "bemgpu_geom_destroy", "bemgpu_tree_create", "bemgpu_tree_destroy",
-    "bemgpu_tree_size", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
+    "bemgpu_tree_size", "bemgpu_mesh_rwgs", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
     "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64", "bemgpu_zgemm_exact",
     "bemgpu_farm_create", "bemgpu_farm_destroy", "bemgpu_farm_lanes", "bemgpu_farm_lane_ctx", "bemgpu_farm_submit",
@@ -95,6 +95,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_tree_create": (i32, [vp, dp, i32, P(vp)]),
         "bemgpu_tree_destroy": (i32, [vp]),
         "bemgpu_tree_size": (i32, [vp]),
+        "bemgpu_mesh_rwgs": (i32, [dp, i32, i32, dp, i32, P(i32)]),
         "bemgpu_green_init": (i32, [dp, dp, dp, i32, P(Green)]),
         "bemgpu_options_default": (None, [P(Options)]),
         "bemgpu_theta": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),

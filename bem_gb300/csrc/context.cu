@@ -475,6 +475,53 @@ int bemgpu_tree_destroy(bemgpu_tree_t t) {
 
 int bemgpu_tree_size(bemgpu_tree_t t) { return t ? t->nrwg : BEMGPU_ERR_ARG; }
 
+// Edge creation of ShapeMesh::ShapeMesh (src/ShapeMesh.cpp:857-928): the
+// triangles are visited in order, and each edge (v0,v1), (v1,v2), (v2,v0) of
+// the current triangle whose other triangle has not been visited yet becomes
+// an RWG (current triangle positive, src/RWG.cpp:5).  A triangle is visited
+// before every triangle of larger index, so "not visited" is "larger index".
+// The edge -> triangles map is a sort of the 3 nt directed edges by their
+// undirected key instead of the reference's per-vertex edge lists.
+int bemgpu_mesh_rwgs(const int *tri, int nt, int nv, int *rwg, int cap, int *nrwg) {
+  if (!tri || !nrwg || nt < 1 || nv < 3 || cap < 0 || (cap > 0 && !rwg)) return BEMGPU_ERR_ARG;
+  *nrwg = 0;
+  const size_t ne = 3 * (size_t)nt;
+  std::vector<std::pair<uint64_t, uint32_t>> e(ne);  // (undirected key, 3 t + k)
+  for (size_t s = 0; s < ne; s++) {
+    int u = tri[s], v = tri[s - s % 3 + (s % 3 + 1) % 3];
+    if (u < 0 || u >= nv || v < 0 || v >= nv || u == v) return BEMGPU_ERR_MESH;
+    uint64_t lo = (uint64_t)std::min(u, v), hi = (uint64_t)std::max(u, v);
+    e[s] = {lo << 32 | hi, (uint32_t)s};
+  }
+  std::sort(e.begin(), e.end());
+  std::vector<int> other(ne, -1);
+  for (size_t i = 0; i < ne;) {
+    size_t j = i;
+    while (j < ne && e[j].first == e[i].first) j++;
+    // a closed 2-manifold has exactly two triangles on every edge
+    if (j - i != 2) return BEMGPU_ERR_MESH;
+    uint32_t a = e[i].second, b = e[i + 1].second;
+    if (a / 3 == b / 3) return BEMGPU_ERR_MESH;
+    other[a] = (int)(b / 3);
+    other[b] = (int)(a / 3);
+    i = j;
+  }
+  int n = 0;
+  for (size_t s = 0; s < ne; s++) {
+    int t = (int)(s / 3), nb = other[s];
+    if (nb <= t) continue;
+    if (n < cap) {
+      rwg[4 * (size_t)n + 0] = t;
+      rwg[4 * (size_t)n + 1] = nb;
+      rwg[4 * (size_t)n + 2] = tri[s];
+      rwg[4 * (size_t)n + 3] = tri[s - s % 3 + (s % 3 + 1) % 3];
+    }
+    n++;
+  }
+  *nrwg = n;
+  return n <= cap ? BEMGPU_OK : BEMGPU_ERR_ARG;
+}
+
 int bemgpu_green_init(const double eps[2], const double mu[2], const double omega[2], int external,
                       bemgpu_green_t *out) {
   if (!eps || !mu || !omega || !out) return BEMGPU_ERR_ARG;

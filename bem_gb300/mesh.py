@@ -53,10 +53,13 @@ class Body:
         return float(np.sqrt((e * e).sum(1)).max())
 
     @staticmethod
-    def from_mesh(verts, tris) -> "Body":
+    def from_mesh(verts, tris, native: bool = False) -> "Body":
+        """``native``: build the RWG table in the C++ library
+        (``bemgpu_mesh_rwgs``, same rows) instead of in Python."""
         verts = np.ascontiguousarray(verts, dtype=np.float64)
         tris = np.ascontiguousarray(tris, dtype=np.int32)
-        return Body(verts, tris, build_rwgs(tris))
+        rwg = build_rwgs_native(tris, verts.shape[0]) if native else build_rwgs(tris)
+        return Body(verts, tris, rwg)
 
     @staticmethod
     def from_reference_order(verts, tris, order) -> "Body":
@@ -87,6 +90,24 @@ def build_rwgs(tris: np.ndarray) -> np.ndarray:
                 out.append((ti, nb, u, v))
         touched[ti] = True
     return np.asarray(out, dtype=np.int32)
+
+
+def build_rwgs_native(tris: np.ndarray, nv: int) -> np.ndarray:
+    """The same table as ``build_rwgs`` from libbemgpu's host-side builder
+    (``bemgpu_mesh_rwgs``: a sort of the directed edges, no Python loop)."""
+    import ctypes
+    from . import _lib
+    tris = np.ascontiguousarray(tris, dtype=np.int32)
+    nt = tris.shape[0]
+    cap = (3 * nt) // 2
+    out = np.zeros((max(cap, 1), 4), dtype=np.int32)
+    n = ctypes.c_int()
+    rc = _lib.load().bemgpu_mesh_rwgs(tris.ctypes.data, nt, int(nv), out.ctypes.data, cap, ctypes.byref(n))
+    if rc == _lib.ERR_MESH:
+        raise ValueError("mesh is not a closed 2-manifold (an edge without exactly two triangles)")
+    if rc != 0:
+        raise _lib.BemGpuError(rc, f"bemgpu_mesh_rwgs: {n.value} RWGs for {nt} triangles")
+    return out[:n.value].copy()
 
 
 def _dedup(verts: np.ndarray, tris: np.ndarray, decimals: int = 12):

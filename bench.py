@@ -9,7 +9,14 @@ Lorentz model, gaps {20, 50, 100, 200, 500, 1000} nm x 64 frequencies in
 Synthetic meshes from bem_gb300.mesh (seeded), no dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--precision fp64|mixed] [--workload ico3|ico2|cube4|tip] [--lanes L]
+                  [--precision fp64|mixed] [--workload ico3|ico2|cube4|tip|slab|mix] [--lanes L]
+
+Other workloads: cube4 (two 1 um cubes, 4x4 squares per face, N = 1152, gap
+100 nm, 20 f); tip (a cone tip over a plate, uneven N per request); slab (two
+10 x 10 x 0.5 um slabs of 8190 RWGs each, N = 32760, gap 50 nm, 8 f in
+0.115-0.119 eV); mix (the serving mix: each request a frequency sweep over a
+random pair of bodies drawn from cubes, icospheres, thin slabs and cone tips,
+SiC or alumina, gap log-uniform 10-1000 nm, T1 uniform 300-600 K).
 
 Requests go through the request farm (bem_gb300.api.Farm): L lanes (default
 4), each a context with its own stream and host thread, keep L solves in
@@ -39,6 +46,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "spectral-power solves/s"
 SIC = (6.7, 0.0983, 0.120, 0.00059)
+ALUMINA = (3.1, 0.0787, 0.111, 0.0020)
 
 WORKLOADS = {
     # name: (generator kwargs, gaps um, freqs)
@@ -50,6 +58,16 @@ WORKLOADS = {
     # 4 x 4 x 0.5 um plate of 1920 edges, gap log-uniform 10-1000 nm, frequency
     # uniform 0.08-0.13 eV: requests of uneven N (4400-6800 unknowns)
     "tip": dict(kind="tip", requests=64, seed=7),
+    # two thin slabs facing each other across the gap (x is the 0.5 um side):
+    # 2 x 35 x 35 squares per face, 8190 RWG edges each, N = 32760; W alone is
+    # 17 GB in complex128
+    "slab": dict(kind="slab", gaps=[0.05], freqs=np.linspace(0.115, 0.119, 8)),
+    # the serving mix: per request a pair of bodies, each drawn from {cube of
+    # 288-1152 edges, icosphere L2-L3 (480 / 1920 edges), 10 x 10 x 0.5 um slab
+    # of 2142-4032 edges, cone tip of 300-1500 edges}, SiC or alumina, gap
+    # log-uniform 10-1000 nm, T1 uniform 300-600 K, T2 = 0, and a sweep of
+    # `sweep` frequencies in 0.08-0.13 eV
+    "mix": dict(kind="mix", requests=64, sweep=32, seed=11),
 }
 
 
@@ -65,34 +83,84 @@ def tip_requests(wl):
     out = []
     for _ in range(wl["requests"]):
         gap = float(np.exp(rng.uniform(np.log(0.01), np.log(1.0))))
-        na = int(rng.integers(12, 21))
-        nside = int(rng.integers(4, 20))
-        tv, tt = mesh.cone_tip(0.5, 1.0, float(rng.uniform(0.05, 0.2)), n_around=na, n_side=nside, n_cap=3, n_base=3)
+        tv, tt = _tip_mesh(rng)
         plate = mesh.Body.from_mesh(pv + np.array([0.0, 0.0, -gap - 0.25]), pt)
         out.append((mesh.Body.from_mesh(tv, tt), plate, float(rng.uniform(0.08, 0.13))))
     return out
 
 
+def _tip_mesh(rng):
+    from bem_gb300 import mesh
+    na = int(rng.integers(12, 21))
+    nside = int(rng.integers(4, 20))
+    return mesh.cone_tip(0.5, 1.0, float(rng.uniform(0.05, 0.2)), n_around=na, n_side=nside, n_cap=3, n_base=3)
+
+
+def _mix_mesh(rng):
+    from bem_gb300 import mesh
+    kind = int(rng.integers(4))
+    if kind == 0:
+        return mesh.cube(1.0, int(rng.integers(4, 9)))
+    if kind == 1:
+        return mesh.icosphere(1.0, int(rng.integers(2, 4)), jitter=0.02, seed=int(rng.integers(1 << 30)))
+    if kind == 2:
+        m = int(rng.integers(17, 25))
+        return mesh.box(0.5, 10.0, 10.0, 2, m, m)
+    return _tip_mesh(rng)
+
+
+def mix_requests(wl):
+    """(body 1, body 2, Lorentz constants, T1) per request of the serving mix;
+    body 1 sits the request's gap beyond body 2 along +x."""
+    from bem_gb300 import mesh
+    rng = np.random.default_rng(wl["seed"])
+    out = []
+    for _ in range(wl["requests"]):
+        v1, t1 = _mix_mesh(rng)
+        v2, t2 = _mix_mesh(rng)
+        gap = float(np.exp(rng.uniform(np.log(0.01), np.log(1.0))))
+        cfg = SIC if rng.integers(2) == 0 else ALUMINA
+        T1 = float(rng.uniform(300.0, 600.0))
+        b2 = mesh.Body.from_mesh(v2, t2)
+        b1 = mesh.Body.from_mesh(v1 + mesh.gap_translation(v1, v2, gap), t1)
+        out.append((b1, b2, cfg, T1))
+    return out
+
+
 def make_bodies(wl):
+    """(body 1, body 2, Lorentz constants of both bodies) per system."""
     from bem_gb300 import mesh
     if wl["kind"] == "tip":
-        return [(b1, b2) for (b1, b2, _) in tip_requests(wl)]
+        return [(b1, b2, SIC) for (b1, b2, _) in tip_requests(wl)]
+    if wl["kind"] == "mix":
+        return [(b1, b2, cfg) for (b1, b2, cfg, _) in mix_requests(wl)]
     if wl["kind"] == "ico":
         v, t = mesh.icosphere(1.0, wl["level"], jitter=0.02, seed=12345)
+    elif wl["kind"] == "slab":
+        v, t = mesh.box(0.5, 10.0, 10.0, 2, 35, 35)
     else:
         v, t = mesh.cube(1.0, wl["nsub"])
     b2 = mesh.Body.from_mesh(v, t)
     bodies = []
     for gap in wl["gaps"]:
         b1 = b2.translated(mesh.gap_translation(v, v, gap))
-        bodies.append((b1, b2))
+        bodies.append((b1, b2, SIC))
     return bodies
 
 
+def mix_freqs(wl):
+    return np.linspace(0.08, 0.13, wl["sweep"])
+
+
 def step_grid(wl):
+    """(system index, eV, T1) per step.  The mix walks its requests' sweeps
+    request-minor, so that consecutive steps are different requests."""
     if wl["kind"] == "tip":
-        return [(i, r[2]) for i, r in enumerate(tip_requests(wl))]
-    return [(gi, float(f)) for gi in range(len(wl["gaps"])) for f in wl["freqs"]]
+        return [(i, r[2], 300.0) for i, r in enumerate(tip_requests(wl))]
+    if wl["kind"] == "mix":
+        reqs = mix_requests(wl)
+        return [(i, float(f), reqs[i][3]) for f in mix_freqs(wl) for i in range(len(reqs))]
+    return [(gi, float(f), 300.0) for gi in range(len(wl["gaps"])) for f in wl["freqs"]]
 
 
 class ClockSampler:
@@ -157,6 +225,11 @@ def peaks():
 FP64_NOMINAL_TFLOPS = 1.25
 
 
+def _check_rc(rc):
+    if rc != 0:
+        raise RuntimeError(f"bemgpu call failed with status {rc}")
+
+
 def run_ours(args, rank, world):
     import ctypes
     import torch
@@ -167,9 +240,9 @@ def run_ours(args, rank, world):
     prec = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED_LA, "mixed-fp32fill": _lib.PREC_MIXED}[args.precision]
     ctx = api.Context(dev)
     L = _lib.load()
-    diel = api.FixedLorentz(*SIC)
+    diels = {SIC: api.FixedLorentz(*SIC), ALUMINA: api.FixedLorentz(*ALUMINA)}
     bodies = make_bodies(wl)
-    systems = [api.parseShapes(b1, b2, diel, diel, ctx) for (b1, b2) in bodies]
+    systems = [api.parseShapes(b1, b2, diels[c], diels[c], ctx) for (b1, b2, c) in bodies]
     grid = step_grid(wl)
     # each rank walks its own slice of the (gap, f) grid: independent solves, no collective
     order = grid[rank::world] if world > 1 else grid
@@ -178,11 +251,15 @@ def run_ours(args, rank, world):
     # and host thread, so consecutive solves overlap on the GPU
     farm = api.Farm(args.lanes, dev)
     lane_ctx = farm.lane_contexts()
+    solver = {"escalate": 0, "c64": 1, "fp64class": 2}[args.solver]
+    for c in lane_ctx:
+        _check_rc(L.bemgpu_ctx_set_solver(c, solver))
+    ctx.set_solver(solver)
 
     def job(k, sysset=None):
-        gi, f = order[k % len(order)]
+        gi, f, T1 = order[k % len(order)]
         top, s, t = (sysset or systems)[gi]
-        return (a, f, 300.0, 0.0, top, s, t)
+        return (a, f, T1, 0.0, top, s, t)
 
     farm.map([job(k) for k in range(args.warmup)], precision=prec, strict=False)
     if world > 1:
@@ -209,12 +286,24 @@ def run_ours(args, rank, world):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
 
-    # Serving: Poisson arrivals at 80 % of the measured throughput, each
-    # request one (gap, frequency) solve; latency = submit -> result ready
-    # (the farm's host clock), reported as p50 / p99.
+    # Serving: Poisson arrivals at 80 % of the measured throughput.  A request
+    # is one (gap, frequency) solve, or for the mix a sweep of `sweep`
+    # frequencies over one pair of bodies, all submitted at its arrival;
+    # latency = arrival -> last result ready (the farm's host clock), p50 / p99.
     serving = None
     if args.serve_requests > 0:
-        rate = 0.8 * args.steps * world / (ms / 1e3)
+        if wl["kind"] == "mix":
+            t1_of = {gi: T1 for (gi, _, T1) in grid}
+            mine = sorted({gi for (gi, _, _) in order})
+            per_req = []
+            for r in range(args.serve_requests):
+                gi = mine[r % len(mine)]
+                per_req.append([(a, float(f), t1_of[gi], 0.0, *systems[gi])
+                                for f in np.linspace(0.08, 0.13, args.sweep or wl["sweep"])])
+        else:
+            per_req = [[job(args.warmup + args.steps + k)] for k in range(args.serve_requests)]
+        solves = sum(len(r) for r in per_req)
+        rate = 0.8 * args.steps * world / (ms / 1e3) * args.serve_requests / solves
         rng = np.random.default_rng(2024)
         arrivals = np.cumsum(rng.exponential(1.0 / rate, args.serve_requests))
         t0s = time.perf_counter()
@@ -223,16 +312,20 @@ def run_ours(args, rank, world):
             dt = ta - (time.perf_counter() - t0s)
             if dt > 0:
                 time.sleep(dt)
-            tks.append(farm.submit(*job(args.warmup + args.steps + k), precision=prec))
+            tks.append([farm.submit(*j, precision=prec) for j in per_req[k]])
         lat = []
-        for tk in tks:
-            info = {}
-            farm.result(tk, info=info, strict=False)
-            lat.append(info["ms_latency"])
+        for req in tks:
+            worst = 0.0
+            for tk in req:
+                info = {}
+                farm.result(tk, info=info, strict=False)
+                worst = max(worst, info["ms_latency"])
+            lat.append(worst)
         span = time.perf_counter() - t0s
         serving = {"arrivals": "poisson", "rate_per_s": rate, "requests": len(tks),
+                   "solves_per_request": solves / len(tks),
                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                   "mean_ms": float(np.mean(lat)), "solves_per_s": len(tks) / span, "lanes": args.lanes}
+                   "mean_ms": float(np.mean(lat)), "solves_per_s": solves / span, "lanes": args.lanes}
 
     # e2e through the public API from host buffers: each step uploads its
     # geometry and trees from host arrays inside the timed region, submits the
@@ -245,13 +338,14 @@ def run_ours(args, rank, world):
     e2e_ev0.record()
     h2d = 0
     tickets = []
-    for k in range(args.steps):
-        gi, f = order[(args.warmup + k) % len(order)]
-        b1, b2 = bodies[gi]
+    e2e_steps = args.e2e_steps or args.steps
+    for k in range(e2e_steps):
+        gi, f, T1 = order[(args.warmup + k) % len(order)]
+        b1, b2, c = bodies[gi]
         xyz, tris, rwg, ns = _mesh.two_body(b1, b2)
-        sysk = api.parseShapes(b1, b2, diel, diel, ctx)
+        sysk = api.parseShapes(b1, b2, diels[c], diels[c], ctx)
         h2d += xyz.nbytes + tris.nbytes + rwg.nbytes * 2
-        tickets.append(farm.submit(a, f, 300.0, 0.0, *sysk, precision=prec))
+        tickets.append(farm.submit(a, f, T1, 0.0, *sysk, precision=prec))
         del sysk
     for tk in tickets:
         farm.result(tk, strict=False)
@@ -267,7 +361,7 @@ def run_ours(args, rank, world):
     # event-timed kernel durations, so the kernels are timed (CUDA events on
     # the launching stream, per kernel class) over solves run one at a time,
     # the same requests as the first timed steps.
-    n_prof = min(args.steps, 4)
+    n_prof = args.prof_steps or min(args.steps, 4)
     prof_jobs = [job(args.warmup + k) for k in range(n_prof)]
     api.CalcHeatTransfer(*job(0), precision=prec, strict=False)  # workspace of this context
     torch.cuda.synchronize()
@@ -284,30 +378,34 @@ def run_ours(args, rank, world):
         stats[name] = dict(launches=n.value, ms=t_ms.value, flops=fl.value, bytes=by.value)
     L.bemgpu_prof_enable(ctx.handle, 0)
 
-    n_unknowns = 2 * systems[0][0].rwgs
-    ns2 = 2 * systems[0][1].rwgs
-    nt2 = 2 * systems[0][2].rwgs
-    entries = n_unknowns ** 2 + ns2 ** 2 + nt2 ** 2
+    def entries(j):
+        n, ns2, nt2 = 2 * j[4].rwgs, 2 * j[5].rwgs, 2 * j[6].rwgs
+        return n ** 2 + ns2 ** 2 + nt2 ** 2
+
+    n_all = sorted({2 * sy[0].rwgs for sy in systems})
+    n_unknowns = n_all[0] if len(n_all) == 1 else f"{n_all[0]}-{n_all[-1]}"
     value = args.steps * world / (ms / 1e3)
-    fill_ms = sum(i["ms_fill"] for i in prof_infos) / len(prof_infos)
+    fill_s = sum(i["ms_fill"] for i in prof_infos) / 1e3
     pk, pk_kind = peaks()
     roof = roofline(stats, args.precision, pk, pk_kind)
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
-        "data": "synthetic (seeded jittered icospheres; no dataset)",
+        "data": "synthetic (seeded generated meshes; no dataset)",
         "config": workload_config(args, n_unknowns, world),
-        "fill_gentries_per_s": entries / (fill_ms / 1e3) / 1e9,
+        "fill_gentries_per_s": sum(entries(j) for j in prof_jobs) / fill_s / 1e9,
         "stage_ms": {k: sum(i[k] for i in prof_infos) / len(prof_infos)
                      for k in ("ms_fill", "ms_lu", "ms_solve", "ms_trace", "ms_refine")},
         "err_est": [i["err_est"] for i in infos], "refine_iters": [i["refine_iters"] for i in infos],
+        "factorization": {"complex64": sum(i["solver"] == 1 for i in infos),
+                          "fp64class": sum(i["solver"] == 2 for i in infos)},
         "kernel_ms_per_step": {k: v["ms"] / n_prof for k, v in stats.items()},
         "kernel_ms_note": f"stage and kernel-class times (and the fill rate) over {n_prof} solves run one at "
                           f"a time, without lane overlap",
         "roofline": roof,
         "gpu_launches": int(launches),
-        "e2e": {"value": args.steps / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / args.steps),
+        "e2e": {"value": e2e_steps / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
                 "d2h_bytes_per_step": 8 + 16 + 4},
         "clocks": clk.summary(),
         "serving": serving,
@@ -378,49 +476,86 @@ def workload_config(args, n_unknowns, world):
         name = (f"tip: {wl['requests']} requests, cone tip (300-1500 RWGs, apex 50-200 nm) over a 4x4x0.5 um "
                 f"plate (1920 RWGs), gap log-uniform 10-1000 nm, f uniform 0.08-0.13 eV, seed {wl['seed']}; "
                 f"N varies per request")
+    elif args.workload == "slab":
+        name = (f"slab: two 10x10x0.5 um slabs (5460 tris, 8190 RWGs each), N={n_unknowns}, SiC, gap 50 nm, "
+                f"{len(wl['freqs'])} f in 0.115-0.119 eV")
+    elif args.workload == "mix":
+        name = (f"mix: {wl['requests']} requests, each a pair of bodies from {{cube 288-1152, icosphere L2-L3, "
+                f"10x10x0.5 um slab 2142-4032, cone tip 300-1500 RWGs}}, SiC or alumina, gap log-uniform "
+                f"10-1000 nm, T1 300-600 K, sweep of {args.sweep or wl['sweep']} f in 0.08-0.13 eV "
+                f"(timed steps: one f of each request in turn), seed {wl['seed']}")
     else:
         name = args.workload
+    n_max = n_unknowns if isinstance(n_unknowns, int) else int(str(n_unknowns).split("-")[-1])
     return {"workload": name, "precision": args.precision, "N": n_unknowns, "parallelism": f"replicas x{world}",
-            "lanes": getattr(args, "lanes", 1),
-            "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_unknowns ** 2 * 16 / 1e6)}
+            "lanes": getattr(args, "lanes", 1), "solver": getattr(args, "solver", "escalate"),
+            "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_max ** 2 * 16 / 1e6)}
 
 
-def run_reference_sample(wl_name, threads=None, frac=None):
-    """Times the oracle port (the reference path restated on the CPU) on a
-    bounded sample of one solve: the three fills over a fraction of the test
-    triangles (scaled up), and the dense algebra at full size."""
+LA_FULL_MAX = 8192
+
+
+def _reference_solve_time(b1, b2, cfg, f, threads, frac=None):
+    """Seconds of one solve of the oracle port: the three fills over a
+    fraction of the test triangles (scaled up by the triangle count) and the
+    dense algebra (inverse and the two products of the trace) at full size,
+    or at n = 4096 scaled by (n / 4096)^3 above n = LA_FULL_MAX."""
     from bem_gb300 import mesh
     from oracle import oracle
-    wl = WORKLOADS[wl_name]
-    (b1, b2) = make_bodies(wl)[0]
     xyz, tris, rwg, ns = mesh.two_body(b1, b2)
     ntri = b1.nt + b2.nt
     frac = frac or (1.0 if ntri <= 500 else 64.0 / ntri)
-    threads = threads or os.cpu_count() or 1
-    f = float(wl["freqs"][0])
     om = oracle.dimensionless_omega(1e-6, f)
-    eps = oracle.lorentz_eps(f, *SIC)
+    eps = oracle.lorentz_eps(f, *cfg)
     t0 = time.perf_counter()
     k = max(1, int(round(frac * ntri)))
     oracle.zts(xyz, tris, rwg, rwg, 1 + 0j, 1 + 0j, om, tri_range=(0, k), nthreads=threads)
     k1 = max(1, int(round(frac * b1.nt)))
     oracle.zts(xyz, tris, rwg[:ns], rwg[:ns], eps, 1 + 0j, om, tri_range=(0, k1), nthreads=threads)
-    oracle.zts(xyz, tris, rwg[ns:], rwg[ns:], eps, 1 + 0j, om, tri_range=(0, k1), nthreads=threads)
+    k2 = max(1, int(round(frac * b2.nt)))
+    oracle.zts(xyz, tris, rwg[ns:], rwg[ns:], eps, 1 + 0j, om, tri_range=(0, k2), nthreads=threads)
+    # each call's time scales with its own test-triangle count; the sample
+    # keeps the three in proportion, so one factor scales the sum
     t_fill = (time.perf_counter() - t0) * (ntri / k)
     n = 2 * rwg.shape[0]
+    n_la = n if n <= LA_FULL_MAX else 4096
+    ns2 = min(2 * ns, n_la - 2) if n_la < n else 2 * ns
     rng = np.random.default_rng(0)
-    W = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + n * np.eye(n)
+    W = rng.standard_normal((n_la, n_la)) + 1j * rng.standard_normal((n_la, n_la)) + n_la * np.eye(n_la)
     t0 = time.perf_counter()
     Wi = np.linalg.inv(W)
-    ns2 = 2 * ns
     G = W[:ns2, :ns2]
     B1 = (G @ Wi[:ns2, :])[:, ns2:]
     B2 = (Wi[:, ns2:] @ W[ns2:, ns2:])[:ns2, :]
     _ = np.trace(B2.conj().T @ B1)
-    t_la = time.perf_counter() - t0
-    return {"solve_s": t_fill + t_la, "fill_s": t_fill, "la_s": t_la, "threads": threads, "n": n,
-            "sample": f"fills over {k}/{ntri} test triangles (x{ntri / k:.1f}) + full-size inverse/products, "
-                      f"n={n}, one frequency"}
+    t_la = (time.perf_counter() - t0) * (n / n_la) ** 3
+    note = f"fills over {k}/{ntri} test triangles (x{ntri / k:.1f}) + inverse/products at n={n_la}"
+    if n_la < n:
+        note += f" scaled by (n/{n_la})^3"
+    return t_fill + t_la, t_fill, t_la, n, note
+
+
+def run_reference_sample(wl_name, threads=None, frac=None):
+    """Times the oracle port (the reference path restated on the CPU) on a
+    bounded sample of the workload's solves: one solve for the fixed-geometry
+    workloads, the mean over the first four requests for the mix."""
+    wl = WORKLOADS[wl_name]
+    threads = threads or os.cpu_count() or 1
+    bodies = make_bodies(wl)
+    grid = step_grid(wl)
+    picks = range(min(4, len(bodies))) if wl["kind"] == "mix" else [0]
+    times, notes, ns = [], [], []
+    for gi in picks:
+        f = next(ff for (g, ff, _) in grid if g == gi)
+        b1, b2, cfg = bodies[gi]
+        tot, t_fill, t_la, n, note = _reference_solve_time(b1, b2, cfg, f, threads, frac)
+        times.append((tot, t_fill, t_la))
+        notes.append(note)
+        ns.append(n)
+    m = [float(np.mean([t[i] for t in times])) for i in range(3)]
+    sample = "; ".join(notes) + (f" (mean of {len(picks)} requests)" if len(picks) > 1 else ", one frequency")
+    return {"solve_s": m[0], "fill_s": m[1], "la_s": m[2], "threads": threads,
+            "n": ns[0] if len(set(ns)) == 1 else f"{min(ns)}-{max(ns)}", "sample": sample}
 
 
 def run_reference(args, rank, world):
@@ -453,6 +588,14 @@ def main():
     ap.add_argument("--lanes", type=int, default=4, help="farm lanes: solves in flight at once on the GPU")
     ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests of the Poisson-arrival serving measurement (0: skip)")
+    ap.add_argument("--solver", default="escalate", choices=["escalate", "c64", "fp64class"],
+                    help="mixed-path factorization: complex64 LU escalating to the FP64-class LU when the "
+                         "refinement does not converge (default), complex64 only, FP64-class only")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="solves of the end-to-end segment (default: --steps)")
+    ap.add_argument("--prof-steps", type=int, default=0,
+                    help="solves run one at a time for the kernel statistics (default: min(--steps, 4))")
+    ap.add_argument("--sweep", type=int, default=0,
+                    help="frequencies per serving request of the mix workload (default: the workload's 32)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     if world > 1 and args.impl == "ours":

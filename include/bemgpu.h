@@ -154,6 +154,14 @@ int bemgpu_geom_destroy(bemgpu_geom_t g);
 int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t *out);
 int bemgpu_tree_destroy(bemgpu_tree_t t);
 int bemgpu_tree_size(bemgpu_tree_t t);
+/* RWG table of one closed body, in the reference's edge-creation order
+ * (ShapeMesh::ShapeMesh, src/ShapeMesh.cpp:857-928): triangles in order, each
+ * edge (v0,v1), (v1,v2), (v2,v0) whose other triangle comes later becomes row
+ * {this triangle, the other, the edge's vertices in this triangle's order}.
+ * Writes min(cap, count) rows to rwg[4*cap] and the count (3 nt / 2) to
+ * *nrwg; BEMGPU_ERR_ARG when cap is below the count, BEMGPU_ERR_MESH when an
+ * edge does not have exactly two triangles.  Host only (no context). */
+int bemgpu_mesh_rwgs(const int *tri, int nt, int nv, int *rwg, int cap, int *nrwg);
 
 /* ---- Green's function / constants ---- */
 /* GreensFunction::init(eps, mu, omega) (src/GreensFunction.cpp:17-30). */

@@ -91,3 +91,31 @@ def test_sic_temperature_model():
     f = api.FixedLorentz(*api.SIC_CONFIG)
     from oracle import oracle
     assert f.eps(0.1) == pytest.approx(oracle.lorentz_eps(0.1, *api.SIC_CONFIG), rel=1e-15)
+
+
+def test_native_rwg_table_matches_python(lib):
+    """bemgpu_mesh_rwgs builds the reference's edge-creation order
+    (src/ShapeMesh.cpp:857-928) as mesh.build_rwgs does, row for row."""
+    from bem_gb300 import mesh
+    cases = [mesh.cube(1.0, 3), mesh.icosphere(1.0, 2, jitter=0.02, seed=3), mesh.box(0.5, 10.0, 10.0, 2, 17, 17),
+             mesh.cone_tip(0.5, 1.0, 0.1, n_around=13, n_side=5, n_cap=3, n_base=3)]
+    for v, t in cases:
+        want = mesh.build_rwgs(t)
+        got = mesh.build_rwgs_native(t, v.shape[0])
+        assert got.shape == (3 * t.shape[0] // 2, 4)
+        assert np.array_equal(got, want)
+        assert np.array_equal(mesh.Body.from_mesh(v, t, native=True).rwg, want)
+    # a capacity below the count reports the count
+    v, t = mesh.cube(1.0, 2)
+    out = np.zeros((4, 4), np.int32)
+    n = ctypes.c_int()
+    rc = lib.bemgpu_mesh_rwgs(np.ascontiguousarray(t, np.int32).ctypes.data, t.shape[0], v.shape[0],
+                              out.ctypes.data, 4, ctypes.byref(n))
+    assert rc == -1 and n.value == 3 * t.shape[0] // 2
+    # an open mesh (one triangle removed) and a bad vertex id are mesh errors
+    with pytest.raises(ValueError):
+        mesh.build_rwgs_native(t[1:], v.shape[0])
+    bad = t.copy()
+    bad[0, 0] = v.shape[0]
+    with pytest.raises(ValueError):
+        mesh.build_rwgs_native(bad, v.shape[0])
