@@ -36,7 +36,7 @@ EXPORTED = [
     "bemgpu_zts_noalloc", "bemgpu_cgemm", "bemgpu_cgemm_acc64", "bemgpu_zgemm_exact",
     "bemgpu_farm_create", "bemgpu_farm_destroy", "bemgpu_farm_lanes", "bemgpu_farm_lane_ctx", "bemgpu_farm_submit",
     "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error", "bemgpu_farm_set_budget",
-    "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint",
+    "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint", "bemgpu_ctx_solve_footprint",
     "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol",
     "bemgpu_zgemm_exact_quantized",
 ]
@@ -121,6 +121,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_ctx_workspace_bytes": (i64, [vp]),
         "bemgpu_ctx_trim": (i32, [vp]),
         "bemgpu_solve_footprint": (i64, [i32, i32, i32]),
+        "bemgpu_ctx_solve_footprint": (i64, [vp, i32, i32, i32]),
         "bemgpu_ctx_set_solver": (i32, [vp, i32]),
         "bemgpu_ctx_wait_selftest": (i32, [vp, i64]),
         "bemgpu_ctx_set_escalation_tol": (i32, [vp, ctypes.c_double]),

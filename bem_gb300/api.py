@@ -289,8 +289,11 @@ class FrequencySweep:
             sys.stderr.write(f"{filename}: {e.strerror}\n")
 
 
-def solve_footprint(s: RWGTree, t: RWGTree, precision: int = _lib.PREC_FP64) -> int:
-    """Device bytes one CalcHeatTransfer solve of these bodies needs at most."""
+def solve_footprint(s: RWGTree, t: RWGTree, precision: int = _lib.PREC_FP64, ctx: Context | None = None) -> int:
+    """Device bytes one CalcHeatTransfer solve of these bodies needs at most
+    (under ``ctx``'s solver mode when a context is given, else the default)."""
+    if ctx is not None:
+        return int(_lib.load().bemgpu_ctx_solve_footprint(ctx.handle, s.rwgs, t.rwgs, int(precision)))
     return int(_lib.load().bemgpu_solve_footprint(s.rwgs, t.rwgs, int(precision)))
 
 

@@ -139,7 +139,7 @@ void lane_main(bemgpu_farm_s *f, int lane) {
       job = f->queue.front();
       f->queue.pop_front();
       f->state[lane] = WAITING;
-      const int64_t need = bemgpu_solve_footprint(job.s->nrwg, job.t->nrwg, job.precision);
+      const int64_t need = bemgpu_ctx_solve_footprint(ctx, job.s->nrwg, job.t->nrwg, job.precision);
       ok = admit(f, lane, job.ticket, (size_t)need, lk);
       f->state[lane] = ok ? BUSY : IDLE;
       FarmResult &r = f->results[job.ticket];

@@ -96,25 +96,41 @@ namespace {
 // Device bytes of the solve-phase buffers (everything allocated after the
 // fill and gather), mirroring the allocation sites in mixed.cu, dense.cu,
 // gemm_tc.cu and gemm_exact.cu (mixed path) or below (FP64 path).
-size_t solve_phase_bytes(int Ns, int Nt, int precision) {
+// `solver` is the context's mixed-path mode (bemgpu_ctx_set_solver): with 2
+// (FP64-class only) the complex64 factors, inverses and their bf16x3 slice
+// planes are never allocated, and the FP64-class LU's inverted diagonal
+// blocks are; with 0 (escalation) both sets can be live in one solve.
+size_t solve_phase_bytes(int Ns, int Nt, int precision, int solver) {
   const size_t N = (size_t)Ns + Nt, n = 2 * N, ns2 = 2 * (size_t)Ns, nt2 = 2 * (size_t)Nt;
   const size_t nn = n * n, nm = n * nt2, st2 = ns2 * nt2;
   const size_t scratch = 8u << 20;  // LU panel candidates and rows (coop_*), flags, trace partials
   if (precision == BEMGPU_PREC_FP64)
     return 16 * nm + 2 * 16 * st2 + 4 * n + scratch;
-  size_t b = 3 * 8 * nn + 2 * 8 * nm + 16 * (ns2 * ns2 + nt2 * nt2) + 3 * 16 * nm + 3 * 16 * st2;
+  size_t b = 16 * (ns2 * ns2 + nt2 * nt2) + 3 * 16 * nm + 3 * 16 * st2;
   b += 4 * n + 16 * (((ns2 + 31) / 32) * ((nt2 + 31) / 32)) + 1024;
   // exact operands: -W, H1, H2 (5 slices), the iterate Y, the trace's X and X^H
   b += bem_exact_operand_bytes(true, (int)n, (int)n, 5) + bem_exact_operand_bytes(true, (int)ns2, (int)ns2, 5) +
        bem_exact_operand_bytes(true, (int)nt2, (int)nt2, 5) + bem_exact_operand_bytes(false, (int)nt2, (int)n, 5) +
        bem_exact_operand_bytes(false, (int)nt2, (int)ns2, 5) + bem_exact_operand_bytes(false, (int)ns2, (int)nt2, 5);
-  // bf16x3 slice planes: the largest product is the application of L^-1 / U^-1
-  // to the n x nt2 right-hand sides; the triangular inverses' halves are smaller
-  size_t a1, b1, a2, b2;
-  bem_cgemm_tc_bytes((int)n, (int)nt2, (int)n, a1, b1);
-  bem_cgemm_tc_bytes((int)(n / 2 + 64), (int)(n / 2 + 64), (int)(n / 2 + 64), a2, b2);
-  b += std::max(a1, a2) + std::max(b1, b2);
-  b += 8 * (n / 2 + 64) * (n / 2 + 64);  // triangular-inverse scratch
+  if (solver != 2) {
+    // complex64 W, L^-1, U^-1, and two n x nt2 complex64 right-hand sides
+    b += 3 * 8 * nn + 2 * 8 * nm;
+    // bf16x3 slice planes: the largest product is the application of L^-1 /
+    // U^-1 to the n x nt2 right-hand sides; the triangular inverses' halves
+    // are smaller
+    size_t a1, b1, a2, b2;
+    bem_cgemm_tc_bytes((int)n, (int)nt2, (int)n, a1, b1);
+    bem_cgemm_tc_bytes((int)(n / 2 + 64), (int)(n / 2 + 64), (int)(n / 2 + 64), a2, b2);
+    b += std::max(a1, a2) + std::max(b1, b2);
+    b += 8 * (n / 2 + 64) * (n / 2 + 64);  // triangular-inverse scratch
+  }
+  if (solver != 1) {
+    // FP64-class LU: the inverted 512 x 512 diagonal blocks of L and U, and
+    // the sliced operands of its K = 512 exact updates (an n x 512 panel, a
+    // 512 x n row block)
+    b += 2 * 16 * n * 512 + bem_exact_operand_bytes(true, (int)n, 512, 5) +
+         bem_exact_operand_bytes(false, (int)n, 512, 5);
+  }
   b += scratch;
   return b;
 }
@@ -128,7 +144,12 @@ size_t fill_phase_bytes(int Ns, int Nt) {
 
 extern "C" int64_t bemgpu_solve_footprint(int nrwg_s, int nrwg_t, int precision) {
   if (nrwg_s < 1 || nrwg_t < 1) return BEMGPU_ERR_ARG;
-  return (int64_t)(fill_phase_bytes(nrwg_s, nrwg_t) + solve_phase_bytes(nrwg_s, nrwg_t, precision));
+  return (int64_t)(fill_phase_bytes(nrwg_s, nrwg_t) + solve_phase_bytes(nrwg_s, nrwg_t, precision, 0));
+}
+
+extern "C" int64_t bemgpu_ctx_solve_footprint(bemgpu_ctx_t ctx, int nrwg_s, int nrwg_t, int precision) {
+  if (!ctx || nrwg_s < 1 || nrwg_t < 1) return BEMGPU_ERR_ARG;
+  return (int64_t)(fill_phase_bytes(nrwg_s, nrwg_t) + solve_phase_bytes(nrwg_s, nrwg_t, precision, ctx->solver));
 }
 
 extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
@@ -186,7 +207,7 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     // solves); otherwise keep them for the next request of this size.
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
-    const size_t held = bem_workspace_bytes(ctx), need = solve_phase_bytes(Ns, Nt, precision);
+    const size_t held = bem_workspace_bytes(ctx), need = solve_phase_bytes(Ns, Nt, precision, ctx->solver);
     const size_t fill = fill_phase_bytes(Ns, Nt);
     // solve-phase bytes not yet held (what the context holds beyond the fill
     // buffers is solve-phase workspace of an earlier request)

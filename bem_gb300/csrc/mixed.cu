@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(256) trace_final_kernel(const double *partial,
 namespace {
 
 struct MixedBufs {
-  float *W32, *R32, *Linv, *Uinv, *T32;
+  float *W32 = nullptr, *R32 = nullptr, *Linv = nullptr, *Uinv = nullptr, *T32 = nullptr;
   double *H1, *H2, *Y, *dY, *R64, *XH, *B1, *C, *partial;
   int *ipiv, *info;
   int ntiles;
@@ -319,11 +319,15 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   const size_t nn = (size_t)n * n, nm = (size_t)n * nt2, st2 = (size_t)ns2 * nt2;
   MixedBufs b;
   b.ntiles = ((ns2 + 31) / 32) * ((nt2 + 31) / 32);
-  b.W32 = (float *)bem_workspace(ctx, "m_W32", 8 * nn);
-  b.R32 = (float *)bem_workspace(ctx, "m_R32", 8 * nm);
-  b.Linv = (float *)bem_workspace(ctx, "m_Linv", 8 * nn);
-  b.Uinv = (float *)bem_workspace(ctx, "m_Uinv", 8 * nn);
-  b.T32 = (float *)bem_workspace(ctx, "m_T32", 8 * nm);
+  // the complex64 factors are not allocated when the context solves FP64-class only
+  const bool c64 = ctx->solver != 2;
+  if (c64) {
+    b.W32 = (float *)bem_workspace(ctx, "m_W32", 8 * nn);
+    b.R32 = (float *)bem_workspace(ctx, "m_R32", 8 * nm);
+    b.Linv = (float *)bem_workspace(ctx, "m_Linv", 8 * nn);
+    b.Uinv = (float *)bem_workspace(ctx, "m_Uinv", 8 * nn);
+    b.T32 = (float *)bem_workspace(ctx, "m_T32", 8 * nm);
+  }
   b.H1 = (double *)bem_workspace(ctx, "m_H1", 16 * (size_t)ns2 * ns2);
   b.H2 = (double *)bem_workspace(ctx, "m_H2", 16 * (size_t)nt2 * nt2);
   b.Y = (double *)bem_workspace(ctx, "m_Y", 16 * nm);
@@ -335,15 +339,17 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   b.partial = (double *)bem_workspace(ctx, "m_partial", 16 * (size_t)b.ntiles + 64);
   b.ipiv = (int *)bem_workspace(ctx, "m_ipiv", 4 * (size_t)n);
   b.info = (int *)bem_workspace(ctx, "m_info", 16);
-  const bool ok = b.W32 && b.R32 && b.Linv && b.Uinv && b.T32 && b.H1 && b.H2 && b.Y && b.dY && b.R64 && b.XH && b.B1 && b.C && b.partial && b.ipiv &&
-                  b.info;
+  const bool ok = (!c64 || (b.W32 && b.R32 && b.Linv && b.Uinv && b.T32)) && b.H1 && b.H2 && b.Y && b.dY && b.R64 &&
+                  b.XH && b.B1 && b.C && b.partial && b.ipiv && b.info;
   if (!ok) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: workspace allocation failed (n=%d)", n);
   cudaEvent_t *ev = ctx->ev;
   const dim3 gn((n + 255) / 256, n), gm((n + 255) / 256, nt2);
   {
-    ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, 24.0 * nn + 48.0 * ((double)ns2 * ns2 + (double)nt2 * nt2));
-    c128_to_c64_kernel<<<gn, 256, 0, st>>>(W, n, b.W32, n, n, n);
-    ctx->launches++;
+    ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, (c64 ? 24.0 * nn : 0.0) + 48.0 * ((double)ns2 * ns2 + (double)nt2 * nt2));
+    if (c64) {
+      c128_to_c64_kernel<<<gn, 256, 0, st>>>(W, n, b.W32, n, n, n);
+      ctx->launches++;
+    }
     sym64_kernel<<<dim3((ns2 + 255) / 256, ns2), 256, 0, st>>>(G1, ns2, ns2, b.H1);
     ctx->launches++;
     sym64_kernel<<<dim3((nt2 + 255) / 256, nt2), 256, 0, st>>>(G2, nt2, nt2, b.H2);

@@ -100,9 +100,14 @@ int64_t bemgpu_ctx_launches(bemgpu_ctx_t ctx);
 int64_t bemgpu_ctx_workspace_bytes(bemgpu_ctx_t ctx);
 int bemgpu_ctx_trim(bemgpu_ctx_t ctx);
 /* Device bytes one CalcHeatTransfer solve needs at most (fill scratch plus
- * solve buffers) for bodies of nrwg_s and nrwg_t RWGs: the admission figure of
- * the request farm.  No reference counterpart. */
+ * solve buffers) for bodies of nrwg_s and nrwg_t RWGs, with the default
+ * mixed-path solver (complex64 LU that may escalate to the FP64-class LU).
+ * No reference counterpart. */
 int64_t bemgpu_solve_footprint(int nrwg_s, int nrwg_t, int precision);
+/* The same for a solve on this context, under its solver mode
+ * (bemgpu_ctx_set_solver; FP64-class only needs no complex64 factors): the
+ * admission figure of the request farm's lanes. */
+int64_t bemgpu_ctx_solve_footprint(bemgpu_ctx_t ctx, int nrwg_s, int nrwg_t, int precision);
 /* Engines of the complex64 products: gemm = LU and correction solves,
  * acc64 = refinement residual and trace (FP64 output); 0 = the library's
  * choice (tensor cores where the shape allows), 1 = tensor cores where the

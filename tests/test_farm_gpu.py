@@ -100,14 +100,19 @@ def test_footprint_bounds_the_workspace():
     """bemgpu_solve_footprint is the admission figure: it must cover what a
     solve allocates, without overstating it by much."""
     L = _lib.load()
-    for level, prec in ((1, _lib.PREC_FP64), (2, _lib.PREC_FP64), (2, _lib.PREC_MIXED_LA)):
+    for level, prec, solver in ((1, _lib.PREC_FP64, 0), (2, _lib.PREC_FP64, 0), (2, _lib.PREC_MIXED_LA, 0),
+                                (2, _lib.PREC_MIXED_LA, 2)):
         ctx = api.Context(0)
+        ctx.set_solver(solver)
         top2, s2, t2 = api.parseShapes(*_bodies(level, 0.1), api.FixedLorentz(*api.SIC_CONFIG),
                                        api.FixedLorentz(*api.SIC_CONFIG), ctx)
         api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top2, s2, t2, precision=prec, strict=False)
         held = L.bemgpu_ctx_workspace_bytes(ctx.handle)
-        fp = api.solve_footprint(s2, t2, prec)
-        assert held <= fp <= 1.5 * held + (64 << 20), (level, prec, held, fp)
+        fp = api.solve_footprint(s2, t2, prec, ctx)
+        assert held <= fp <= 1.5 * held + (64 << 20), (level, prec, solver, held, fp)
+        if solver == 2:
+            # FP64-class only: no complex64 factors
+            assert fp < api.solve_footprint(s2, t2, prec)
         assert L.bemgpu_ctx_trim(ctx.handle) == 0 and L.bemgpu_ctx_workspace_bytes(ctx.handle) == 0
         # a trimmed context solves again and gives the same answer
         P1 = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top2, s2, t2, precision=prec, strict=False)
