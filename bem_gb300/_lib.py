@@ -29,7 +29,7 @@ ERR_NAMES = {ERR_ARG: "BEMGPU_ERR_ARG", ERR_OOM: "BEMGPU_ERR_OOM", ERR_CUDA: "BE
 # Every symbol include/bemgpu.h declares.
 EXPORTED = [
     "bemgpu_ctx_create", "bemgpu_ctx_destroy", "bemgpu_ctx_last_error", "bemgpu_version",
-    "bemgpu_ctx_stream", "bemgpu_ctx_launches", "bemgpu_ctx_set_engines", "bemgpu_prof_enable", "bemgpu_prof_query",
+    "bemgpu_ctx_stream", "bemgpu_ctx_launches", "bemgpu_ctx_set_engines", "bemgpu_prof_enable", "bemgpu_prof_query", "bemgpu_prof_query_tensor",
     "bemgpu_geom_create", "bemgpu_geom_destroy", "bemgpu_tree_create", "bemgpu_tree_destroy",
     "bemgpu_tree_size", "bemgpu_mesh_rwgs", "bemgpu_green_init", "bemgpu_options_default", "bemgpu_theta",
     "bemgpu_dimensionless_omega", "bemgpu_zts", "bemgpu_zts_host", "bemgpu_heat_transfer",
@@ -90,6 +90,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_ctx_set_engines": (i32, [vp, i32, i32]),
         "bemgpu_prof_enable": (i32, [vp, i32]),
         "bemgpu_prof_query": (i32, [vp, i32, P(i64), P(ctypes.c_double), P(ctypes.c_double), P(ctypes.c_double)]),
+        "bemgpu_prof_query_tensor": (i32, [vp, i32, P(ctypes.c_double)]),
         "bemgpu_geom_create": (i32, [vp, dp, i32, dp, i32, P(vp)]),
         "bemgpu_geom_destroy": (i32, [vp]),
         "bemgpu_tree_create": (i32, [vp, dp, i32, P(vp)]),

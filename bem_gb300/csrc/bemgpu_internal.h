@@ -102,6 +102,7 @@ struct bemgpu_ctx_s {
     int kind;
     cudaEvent_t a, b;
     double flops, bytes;
+    double tensor;  // bf16 tensor-core flops executed (slice products x 8 m n k), 0 off the tensor pipe
   };
   std::vector<ProfRec> prof_recs;
   std::vector<cudaEvent_t> ev_pool;
@@ -114,6 +115,7 @@ struct ProfScope {
   int kind;
   cudaStream_t st;
   double flops, bytes;
+  double tensor = 0.0;  // set by tensor-core products: bf16 flops executed
   cudaEvent_t a = nullptr;
   ProfScope(bemgpu_ctx_s *c, int k, cudaStream_t s, double f, double b);
   ~ProfScope();

@@ -147,7 +147,7 @@ ProfScope::~ProfScope() {
   if (a) {
     cudaEvent_t b = prof_event(ctx);
     cudaEventRecord(b, st);
-    ctx->prof_recs.push_back({kind, a, b, flops, bytes});
+    ctx->prof_recs.push_back({kind, a, b, flops, bytes, tensor});
   }
 }
 
@@ -211,6 +211,16 @@ int bemgpu_prof_query(bemgpu_ctx_t ctx, int kind, int64_t *launches, double *ms,
   if (ms) *ms = t;
   if (flops) *flops = f;
   if (bytes) *bytes = b;
+  return BEMGPU_OK;
+}
+
+int bemgpu_prof_query_tensor(bemgpu_ctx_t ctx, int kind, double *tensor_flops) {
+  if (!ctx || !tensor_flops || kind < 0 || kind >= BEMGPU_K_COUNT) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  double f = 0;
+  for (auto &r : ctx->prof_recs)
+    if (r.kind == kind) f += r.tensor;
+  *tensor_flops = f;
   return BEMGPU_OK;
 }
 

@@ -534,6 +534,13 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
                2.0 * SA * ((double)a.rows_p * a.kp * ((b.rows_p + EX_BN - 1) / EX_BN) / 8.0) +
                    2.0 * SB * (double)b.rows_p * b.kp + 16.0 * m * (double)n * (accumulate ? 2 : 1));
   (void)SL;
+  {
+    // slice products (a, b) with a < SA, b < SB, a + b < SA
+    int products = 0;
+    for (int i = 0; i < SA; i++)
+      for (int j = 0; j < SB; j++) products += (i + j < SA);
+    ps.tensor = products * ps.flops;
+  }
   const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / EX_BN));
   const int ktiles = (int)(a.kp / EX_BK);
   if (SA == 5 && SB == 3)

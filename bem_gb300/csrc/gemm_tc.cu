@@ -521,6 +521,7 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
   {
     const double cbytes = (out == TC_OUT_F32 ? 4.0 : 8.0) * 2.0 * m * n * (accumulate ? 2.0 : 1.0);
     ProfScope ps(ctx, kind, st, 8.0 * m * n * (double)k, 12.0 * ((double)Mp * Kp + (double)Np * Kp) + cbytes);
+    ps.tensor = 6.0 * ps.flops;  // slice products (a, b) with a + b <= 2 of 3 slices
     const dim3 grid((unsigned)(Mp / TC_BM), (unsigned)(Np / bn));
     const int kt = (int)(Kp / TC_BK);
     if (out == TC_OUT_F64_COMP)

@@ -375,7 +375,9 @@ def run_ours(args, rank, world):
         n = ctypes.c_int64()
         t_ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         L.bemgpu_prof_query(ctx.handle, kk, ctypes.byref(n), ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by))
-        stats[name] = dict(launches=n.value, ms=t_ms.value, flops=fl.value, bytes=by.value)
+        tf = ctypes.c_double()
+        L.bemgpu_prof_query_tensor(ctx.handle, kk, ctypes.byref(tf))
+        stats[name] = dict(launches=n.value, ms=t_ms.value, flops=fl.value, bytes=by.value, tensor=tf.value)
     L.bemgpu_prof_enable(ctx.handle, 0)
 
     def entries(j):
@@ -419,30 +421,29 @@ def run_ours(args, rank, world):
 
 # Kernel groups of the per-kind breakdown and the resource that bounds each.
 # "ex_gemm": the exact complex128 tensor-core product (refinement residual and
-# trace): 15 bf16 slice products per complex MAC; "tc_gemm": the bf16x3
-# complex64 products (LU trailing updates, triangular inverses, correction
-# solves): 6 bf16 products per complex MAC.
+# trace: 6 to 15 bf16 slice products per complex MAC, by the operands'
+# slices); "tc_gemm": the bf16x3 complex64 products (LU trailing updates,
+# triangular inverses, correction solves: 6 bf16 products per complex MAC),
+# or with the FP64-class factorization its exact products.  The library
+# reports the bf16 flops each kind executed (bemgpu_prof_query_tensor).
 GROUPS = {
-    "ex_gemm": (("refine_gemm", "trace"), "tensor", 15),
-    "tc_gemm": (("lu_gemm", "solve_gemm", "trsm"), "tensor", 6),
-    "fill": (("fill_near", "fill_far"), None, 0),
-    "lu_panel": (("lu_panel",), "latency", 0),
-    "memory": (("gather", "slice"), "hbm", 0),
+    "ex_gemm": (("refine_gemm", "trace"), "tensor"),
+    "tc_gemm": (("lu_gemm", "solve_gemm", "trsm"), "tensor"),
+    "fill": (("fill_near", "fill_far"), None),
+    "lu_panel": (("lu_panel",), "latency"),
+    "memory": (("gather", "slice"), "hbm"),
 }
 
 
 def roofline(stats, precision, pk, pk_kind, fp64class=False):
     """Roofline of the dominant kernel group of the timed region: algorithmic
-    flops (or bytes) per CUDA-event second against the measured peak.  With
-    the FP64-class factorization the LU, block-solve and triangular kinds are
-    exact products too (5 x 5 slices: 15 bf16 products per complex MAC)."""
+    flops (or bytes) per CUDA-event second against the measured peak."""
     groups = dict(GROUPS)
     if fp64class:
-        groups["ex_lu"] = (GROUPS["tc_gemm"][0], "tensor", 15)
-        del groups["tc_gemm"]
-    tot = {g: sum(stats[k]["ms"] for k in ks if k in stats) for g, (ks, _, _) in groups.items()}
+        groups["ex_lu"] = groups.pop("tc_gemm")
+    tot = {g: sum(stats[k]["ms"] for k in ks if k in stats) for g, (ks, _) in groups.items()}
     dom = max(tot, key=tot.get)
-    ks, bound, products = groups[dom]
+    ks, bound = groups[dom]
     ms = tot[dom]
     fl = sum(stats[k]["flops"] for k in ks if k in stats)
     by = sum(stats[k]["bytes"] for k in ks if k in stats)
@@ -463,11 +464,14 @@ def roofline(stats, precision, pk, pk_kind, fp64class=False):
     if bound == "tensor":
         ach = fl / (ms / 1e3) / 1e12
         peak = pk.get("bf16_tflops_sustained", 1700.0)
+        tens = sum(stats[k].get("tensor", 0.0) for k in ks if k in stats)
+        exe = tens / (ms / 1e3) / 1e12
         return dict(base, bound="tensor", achieved=ach, peak=peak, unit="TFLOP/s", frac=ach / peak,
                     peak_source=f"{pk_kind} bf16 sustained",
-                    executed_bf16_tflops=ach * products, executed_frac=ach * products / peak,
-                    note=f"algorithmic complex flops (8 m n k); the kernel issues {products} bf16 slice products "
-                         f"per complex MAC, so the tensor pipe runs {products}x the algorithmic rate")
+                    executed_bf16_tflops=exe, executed_frac=exe / peak,
+                    slice_products_per_mac=tens / fl if fl else None,
+                    note="achieved: algorithmic complex flops (8 m n k); executed: the bf16 slice products the "
+                         "kernels issued (library count), against the same bf16 peak")
     ach = by / (ms / 1e3) / 1e9
     out = dict(base, bound="hbm", achieved=ach, peak=pk["hbm_gbs"], unit="GB/s", frac=ach / pk["hbm_gbs"],
                peak_source=pk_kind)

@@ -145,6 +145,9 @@ int bemgpu_prof_enable(bemgpu_ctx_t ctx, int enable);
 /* Totals of one kernel class since the last enable: launches, device ms,
  * algorithmic flops and algorithmic DRAM bytes (synchronizes the context stream). */
 int bemgpu_prof_query(bemgpu_ctx_t ctx, int kind, int64_t *launches, double *ms, double *flops, double *bytes);
+/* bf16 tensor-core flops the same launches executed: for each product of
+ * sliced operands, its slice products x 8 m n k (0 for kinds off the tensor pipe). */
+int bemgpu_prof_query_tensor(bemgpu_ctx_t ctx, int kind, double *tensor_flops);
 
 /* ---- resident geometry and RWG trees ---- */
 /* Uploads vertices (xyz[3*nv]) and triangles (tri[3*nt], vertex ids, each

@@ -232,3 +232,46 @@ def test_exact_gemm_with_quantized_b(m, n, k):
         scale = k * np.outer(np.abs(A).max(axis=1), np.abs(Bq).max(axis=0))
         err = np.max(np.abs(C - ref) / scale)
         assert err < 2.0 ** -38, (acc, err)
+
+
+def test_tensor_flop_counts_per_product():
+    """bemgpu_prof_query_tensor reports the bf16 slice products each product
+    issued: 6 per complex MAC for the bf16x3 complex64 product, 15 / 10 / 6
+    for the exact product of 5 / 4 / 3 slices, 12 for 5 slices times a
+    3-slice quantized B; the FMA engine issues none."""
+    import torch
+    ctx = api.default_context()
+    L = _lib.load()
+    trace = _lib.K_NAMES.index("trace")
+    rng = np.random.default_rng(11)
+    m, n, k = 96, 80, 64
+
+    def counts(run):
+        L.bemgpu_prof_enable(ctx.handle, 1)
+        run()
+        nl, ms, fl, by = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        tf = ctypes.c_double()
+        assert L.bemgpu_prof_query(ctx.handle, trace, ctypes.byref(nl), ctypes.byref(ms), ctypes.byref(fl),
+                                   ctypes.byref(by)) == 0
+        assert L.bemgpu_prof_query_tensor(ctx.handle, trace, ctypes.byref(tf)) == 0
+        L.bemgpu_prof_enable(ctx.handle, 0)
+        return fl.value, tf.value
+
+    A32, B32 = _rand(rng, (m, k)), _rand(rng, (k, n))
+    fl, tf = counts(lambda: _gemm(A32, B32, np.zeros((m, n), np.complex64), 0, 1))
+    assert fl == 8.0 * m * n * k and tf == 6 * fl
+    fl, tf = counts(lambda: _gemm(A32, B32, np.zeros((m, n), np.complex64), 0, 2))
+    assert fl == 8.0 * m * n * k and tf == 0
+    A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    for slices, products in ((5, 15), (4, 10), (3, 6)):
+        fl, tf = counts(lambda: _zgemm_exact(A, B, np.zeros((m, n)), 0, slices))
+        assert fl == 8.0 * m * n * k and tf == products * fl, (slices, tf / fl)
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dC = torch.zeros((n, m), dtype=torch.complex128, device="cuda")
+    torch.cuda.synchronize()
+    fl, tf = counts(lambda: L.bemgpu_zgemm_exact_quantized(ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), m,
+                                                           ctypes.c_void_p(dB.data_ptr()), k,
+                                                           ctypes.c_void_p(dC.data_ptr()), m, 0))
+    assert fl == 8.0 * m * n * k and tf == 12 * fl
