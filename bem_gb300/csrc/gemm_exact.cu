@@ -35,11 +35,8 @@
 
 namespace {
 
-constexpr int EX_BM = 128, EX_BN = 64, EX_BK = 32;  // tile of D'; K step (bf16 elements, 64 bytes)
-constexpr int EX_STAGES = 3;
-constexpr int EX_DRAIN = 4;  // TMA stages per drain step (one exponent block of 64 complex)
-constexpr int EX_A_TILE = EX_BM * EX_BK * 2;  // 8 KB per slice
-constexpr int EX_B_TILE = EX_BN * EX_BK * 2;  // 4 KB per slice
+constexpr int EX_BM = 128, EX_BN = 64;  // tile of D'
+constexpr int EX_SMEM_MAX = 232448;      // dynamic shared memory of one CTA (227 KB)
 constexpr int EX_EPI_WARPS = 8;
 constexpr int EX_THREADS = 64 + 32 * EX_EPI_WARPS;
 constexpr int EX_TMEM_COLS = 512;  // 2 x levels 0..2 x 64 + levels 3, 4 x 64
@@ -47,10 +44,27 @@ constexpr int EX_SCALE_TARGET = 0;  // largest magnitude of a matrix is scaled t
                                     // and their sums stay inside FP32's range
 constexpr int EX_FLUSH_E = -80;     // blocks whose maximum (scaled) is below 2^-80 are zero (slices >= 2^-120)
 
+// K step of one TMA stage: 64 bf16 (128-byte rows, 128-byte swizzle) where two
+// stages fit in shared memory, else 32 (64-byte rows) in three stages (5 x 5
+// slices).  Wider rows move twice the bytes per TMA row request.  A drain
+// step is one exponent block: 128 realified K (64 complex).
 template <int SA, int SB>
-__host__ __device__ constexpr int ex_stage_bytes() { return SA * EX_A_TILE + SB * EX_B_TILE; }
+struct ExCfg {
+  static constexpr int BK = 2 * (SA * EX_BM + SB * EX_BN) * 64 * 2 + 1280 <= EX_SMEM_MAX ? 64 : 32;
+  static constexpr int A_TILE = EX_BM * BK * 2;
+  static constexpr int B_TILE = EX_BN * BK * 2;
+  static constexpr int STAGE = SA * A_TILE + SB * B_TILE;
+  static constexpr int STAGES = (EX_SMEM_MAX - 1280) / STAGE < 3 ? (EX_SMEM_MAX - 1280) / STAGE : 3;
+  static constexpr int DRAIN = 128 / BK;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static_assert(STAGES >= 2 && SMEM <= EX_SMEM_MAX, "exact gemm: shared memory");
+};
 template <int SA, int SB>
-__host__ __device__ constexpr int ex_smem_bytes() { return EX_STAGES * ex_stage_bytes<SA, SB>() + 1024 + 256; }
+__host__ __device__ constexpr int ex_smem_bytes() { return ExCfg<SA, SB>::SMEM; }
+// K step of the built (SA, SB) kernels, on the host
+inline int ex_bk(int SA, int SB) {
+  return SA == 5 && SB == 3 ? ExCfg<5, 3>::BK : SA == 5 ? ExCfg<5, 5>::BK : SA == 4 ? ExCfg<4, 4>::BK : ExCfg<3, 3>::BK;
+}
 
 // The slice products of an (SA, SB) product: (a, b) with a < SA, b < SB and
 // level a + b < SA, in level-major order (a ascending within a level).  SA =
@@ -100,8 +114,10 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
     ex_gemm_kernel(const __grid_constant__ ExMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf, int mvalid,
                    int nvalid, int accumulate, const int *__restrict__ shifts, int *err) {
   typedef ExProducts<SA, SB> PR;
+  typedef ExCfg<SA, SB> CF;
   constexpr int NP = PR::count();
-  constexpr int STAGE = ex_stage_bytes<SA, SB>();
+  constexpr int STAGE = CF::STAGE, EX_STAGES = CF::STAGES, EX_BK = CF::BK, EX_DRAIN = CF::DRAIN;
+  constexpr int EX_A_TILE = CF::A_TILE, EX_B_TILE = CF::B_TILE;
   extern __shared__ unsigned char ex_smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(ex_smem_raw) + 1023) &
                                                           ~(uintptr_t)1023);
@@ -169,7 +185,8 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;");
         // descriptors: one per stage, the tiles and K steps as compile-time
         // offsets added to its address field (which never carries: smem < 256 KB)
-        const uint64_t dbase = smem_desc_sw64(smem_u32(smem + s * STAGE));
+        const uint64_t dbase =
+            EX_BK == 64 ? smem_desc_sw128(smem_u32(smem + s * STAGE)) : smem_desc_sw64(smem_u32(smem + s * STAGE));
 #pragma unroll
         for (int ks = 0; ks < EX_BK / 16; ks++) {
 #pragma unroll
@@ -422,9 +439,11 @@ __global__ void ex_prep_b_kernel(const double *__restrict__ B, int64_t ldb, int 
   }
 }
 
-bool ex_maps(CUtensorMap *maps, const __nv_bfloat16 *S, int slices, int64_t rows, int64_t kp, int box_rows) {
+bool ex_maps(CUtensorMap *maps, const __nv_bfloat16 *S, int slices, int64_t rows, int64_t kp, int box_rows,
+             int bk) {
   for (int l = 0; l < slices; l++)
-    if (!make_map_bf16(&maps[l], S + l * rows * kp, rows, kp, EX_BK, box_rows, CU_TENSOR_MAP_SWIZZLE_64B))
+    if (!make_map_bf16(&maps[l], S + l * rows * kp, rows, kp, bk, box_rows,
+                       bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B))
       return false;
   return true;
 }
@@ -505,8 +524,9 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: slices (%d, %d) not built", SA, SB);
   const int SL = SB;
   ExMaps maps;
-  if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SA, a.rows_p, a.kp, EX_BM) ||
-      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SB, b.rows_p, b.kp, EX_BN))
+  const int bk = ex_bk(SA, SB);
+  if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SA, a.rows_p, a.kp, EX_BM, bk) ||
+      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SB, b.rows_p, b.kp, EX_BN, bk))
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "exact gemm: tensor map encoding failed");
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
   if (!err) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
@@ -542,7 +562,7 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
     ps.tensor = products * ps.flops;
   }
   const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / EX_BN));
-  const int ktiles = (int)(a.kp / EX_BK);
+  const int ktiles = (int)(a.kp / bk);
   if (SA == 5 && SB == 3)
     ex_gemm_kernel<5, 3><<<grid, EX_THREADS, ex_smem_bytes<5, 3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
                                                                           accumulate, shifts, err);
