@@ -225,6 +225,25 @@ def peaks():
 FP64_NOMINAL_TFLOPS = 1.25
 
 
+def shard_steps(grid, rank, world):
+    """Replicas: rank r takes steps r, r + world, ... of the grid (independent
+    solves, as the reference's task farm hands jobs to its servants)."""
+    return grid[rank::world] if world > 1 else list(grid)
+
+
+def max_over_ranks(x, world):
+    """The slowest rank's value (the timed region ends when every replica has
+    finished); the only cross-rank operation besides the barriers."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _check_rc(rc):
     if rc != 0:
         raise RuntimeError(f"bemgpu call failed with status {rc}")
@@ -245,7 +264,7 @@ def run_ours(args, rank, world):
     systems = [api.parseShapes(b1, b2, diels[c], diels[c], ctx) for (b1, b2, c) in bodies]
     grid = step_grid(wl)
     # each rank walks its own slice of the (gap, f) grid: independent solves, no collective
-    order = grid[rank::world] if world > 1 else grid
+    order = shard_steps(grid, rank, world)
     a = 1e-6
     # requests go through the farm: `lanes` contexts, each on its own stream
     # and host thread, so consecutive solves overlap on the GPU
@@ -279,12 +298,7 @@ def run_ours(args, rank, world):
         ev1.record()
         torch.cuda.synchronize()
     launches = sum(L.bemgpu_ctx_launches(c) for c in lane_ctx) - launches0
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
 
     # Serving: Poisson arrivals at 80 % of the measured throughput.  A request
     # is one (gap, frequency) solve, or for the mix a sweep of `sweep`
