@@ -37,7 +37,7 @@ EXPORTED = [
     "bemgpu_farm_create", "bemgpu_farm_destroy", "bemgpu_farm_lanes", "bemgpu_farm_lane_ctx", "bemgpu_farm_submit",
     "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error", "bemgpu_farm_set_budget",
     "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint", "bemgpu_ctx_solve_footprint",
-    "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol",
+    "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol", "bemgpu_ctx_set_fp64_fallback_tol",
     "bemgpu_zgemm_exact_quantized",
 ]
 
@@ -126,6 +126,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_ctx_set_solver": (i32, [vp, i32]),
         "bemgpu_ctx_wait_selftest": (i32, [vp, i64]),
         "bemgpu_ctx_set_escalation_tol": (i32, [vp, ctypes.c_double]),
+        "bemgpu_ctx_set_fp64_fallback_tol": (i32, [vp, ctypes.c_double]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -96,6 +96,7 @@ struct bemgpu_ctx_s {
   int acc_engine = 0;    // residual/trace GEMMs with FP64 output: same choices
   int solver = 0;        // mixed path: 0 complex64 with FP64-class escalation, 1 complex64, 2 FP64-class
   double escalate_tol = 1e-6;  // complex64 refinement error estimate above which the solve escalates
+  double fallback_tol = 1e-6;  // FP64-class error estimate above which mode 0 re-solves on the FP64 path
   // live kernel statistics
   bool prof = false;
   struct ProfRec {
@@ -262,5 +263,9 @@ int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const 
 
 // ---- mixed-precision solve (mixed.cu) ----
 // W (FP64, n x n, ld n), G1 (ns2 x ns2), G2 ((n-ns2) x (n-ns2)) as filled; writes S = 1/4 Tr(B2^H B1).
+// Returns BEM_SOLVE_ON_FP64_PATH, with W, G1 and G2 untouched, when mode 0's
+// FP64-class solve stays above ctx->fallback_tol: the caller then solves W
+// on the plain FP64 path.
+constexpr int BEM_SOLVE_ON_FP64_PATH = 100;
 int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
                     cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info);

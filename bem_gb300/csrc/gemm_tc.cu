@@ -675,6 +675,13 @@ extern "C" int bemgpu_ctx_set_escalation_tol(bemgpu_ctx_t ctx, double tol) {
   return BEMGPU_OK;
 }
 
+extern "C" int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol) {
+  if (!ctx || !(tol >= 0.0)) return bem_fail(ctx, BEMGPU_ERR_ARG, "set_fp64_fallback_tol: tol >= 0");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->fallback_tol = tol;
+  return BEMGPU_OK;
+}
+
 extern "C" int bemgpu_ctx_set_engines(bemgpu_ctx_t ctx, int gemm, int acc64) {
   if (!ctx || gemm < 0 || gemm > 2 || acc64 < 0 || acc64 > 2)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "set_engines: engines are 0 (choice), 1 (tensor cores), 2 (FMA pipes)");

@@ -131,6 +131,11 @@ size_t solve_phase_bytes(int Ns, int Nt, int precision, int solver) {
     b += 2 * 16 * n * 512 + bem_exact_operand_bytes(true, (int)n, 512, 5) +
          bem_exact_operand_bytes(false, (int)n, 512, 5);
   }
+  if (solver == 0) {
+    // escalation keeps W as filled: the FP64-class LU factors a copy, and the
+    // FP64-path fallback needs its own Y, B1, B2
+    b += 16 * nn + 16 * nm + 2 * 16 * st2;
+  }
   b += scratch;
   return b;
 }
@@ -141,6 +146,64 @@ size_t fill_phase_bytes(int Ns, int Nt) {
 }
 
 }  // namespace
+
+// The plain FP64 path after the fill: W = P L U by the FP64 LU, Y = W^-1 E_t,
+// symm of G1, G2 in place, the two products and the trace.  Records ev[2..4]
+// (after the LU, the solve, the trace).
+static int fp64_path_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, double *G1, double *G2, cudaStream_t st,
+                           double S[2], cudaEvent_t *ev) {
+  const int nt2 = n - ns2;
+  const double one_c[2] = {1.0, 0.0};
+  double *Y = (double *)bem_workspace(ctx, "Y", sizeof(double) * 2 * (size_t)n * nt2);
+  double *B1 = (double *)bem_workspace(ctx, "B1", sizeof(double) * 2 * (size_t)ns2 * nt2);
+  double *B2 = (double *)bem_workspace(ctx, "B2", sizeof(double) * 2 * (size_t)ns2 * nt2);
+  int *ipiv = (int *)bem_workspace(ctx, "ipiv", sizeof(int) * (size_t)n);
+  int *dinfo = (int *)bem_workspace(ctx, "info", sizeof(int));
+  const int TRB = 1024;
+  double *partial = (double *)bem_workspace(ctx, "trace_partial", sizeof(double) * 2 * TRB + 16);
+  if (!Y || !B1 || !B2 || !ipiv || !dinfo || !partial)
+    return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
+  double *dS = partial + 2 * TRB;
+  int rc = bem_zgetrf(ctx, W, n, n, ipiv, dinfo, st);
+  if (rc) return rc;
+  cudaEventRecord(ev[2], st);
+  {
+    ProfScope ps(ctx, BEMGPU_K_SOLVE_GEMM, st, 0.0, 16.0 * n * nt2);
+    identity_cols_kernel<<<dim3((n + 255) / 256, nt2), 256, 0, st>>>(Y, n, n, ns2, nt2);
+    ctx->launches++;
+  }
+  rc = bem_zgetrs(ctx, W, n, n, ipiv, Y, n, nt2, st);
+  if (rc) return rc;
+  cudaEventRecord(ev[3], st);
+  {
+    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 2.0 * ((double)ns2 * ns2 + (double)nt2 * nt2),
+                 32.0 * ((double)ns2 * ns2 + (double)nt2 * nt2));
+    sym_kernel<<<dim3((ns2 + 255) / 256, ns2), 256, 0, st>>>(G1, ns2, ns2);
+    ctx->launches++;
+    sym_kernel<<<dim3((nt2 + 255) / 256, nt2), 256, 0, st>>>(G2, nt2, nt2);
+    ctx->launches++;
+  }
+  const double zero_c[2] = {0.0, 0.0};
+  rc = bem_zgemm(ctx, BEMGPU_K_TRACE, 'N', ns2, nt2, ns2, one_c, G1, ns2, Y, n, zero_c, B1, ns2, st);
+  if (!rc) rc = bem_zgemm(ctx, BEMGPU_K_TRACE, 'N', ns2, nt2, nt2, one_c, Y, n, G2, nt2, zero_c, B2, ns2, st);
+  if (rc) return rc;
+  {
+    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 8.0 * ns2 * nt2, 32.0 * ns2 * nt2);
+    trace_partial_kernel<<<TRB, TR_THREADS, 0, st>>>(B1, B2, ns2, ns2, nt2, partial);
+    ctx->launches++;
+    trace_final_kernel<<<1, 32, 0, st>>>(partial, TRB, dS);
+    ctx->launches++;
+  }
+  cudaEventRecord(ev[4], st);
+  int hinfo = 0;
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(S, dS, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if (bem_tc_error(ctx, true))
+    return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "heat_transfer: a grid-barrier or pipeline wait ran out");
+  if (hinfo != 0) return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "heat_transfer: zero pivot at column %d", hinfo);
+  return BEMGPU_OK;
+}
 
 extern "C" int64_t bemgpu_solve_footprint(int nrwg_s, int nrwg_t, int precision) {
   if (nrwg_s < 1 || nrwg_t < 1) return BEMGPU_ERR_ARG;
@@ -223,6 +286,18 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     memset(&mi, 0, sizeof mi);
     double S[2] = {0, 0};
     rc = bem_mixed_solve(ctx, W, n, ns2, G1, G2, st, S, &mi);
+    if (rc == BEM_SOLVE_ON_FP64_PATH) {
+      // the FP64-class refinement stalled above the fallback tolerance: W is
+      // as filled, solve it on the plain FP64 path (FP64 LU, no refinement)
+      cudaEventRecord(ev[1], st);
+      rc = fp64_path_solve(ctx, W, n, ns2, G1, G2, st, S, ev);
+      if (rc) return rc;
+      mi.solver = 3;
+      mi.err_est = 0.0;
+      mi.ms_lu = elapsed(ev[1], ev[2]);
+      mi.ms_solve = elapsed(ev[2], ev[3]);
+      mi.ms_trace = elapsed(ev[3], ev[4]);
+    }
     if (rc && rc != BEMGPU_ERR_NO_CONVERGE) return rc;
     *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
     if (info) {
@@ -235,56 +310,10 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     }
     return rc;
   }
-  double *Y = (double *)bem_workspace(ctx, "Y", sizeof(double) * 2 * (size_t)n * nt2);
-  double *B1 = (double *)bem_workspace(ctx, "B1", sizeof(double) * 2 * (size_t)ns2 * nt2);
-  double *B2 = (double *)bem_workspace(ctx, "B2", sizeof(double) * 2 * (size_t)ns2 * nt2);
-  int *ipiv = (int *)bem_workspace(ctx, "ipiv", sizeof(int) * (size_t)n);
-  int *dinfo = (int *)bem_workspace(ctx, "info", sizeof(int));
-  const int TRB = 1024;
-  double *partial = (double *)bem_workspace(ctx, "trace_partial", sizeof(double) * 2 * TRB + 16);
-  if (!Y || !B1 || !B2 || !ipiv || !dinfo || !partial)
-    return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
-  double *dS = partial + 2 * TRB;
-  cudaEventRecord(ev[1], st);
-  rc = bem_zgetrf(ctx, W, n, n, ipiv, dinfo, st);
-  if (rc) return rc;
-  cudaEventRecord(ev[2], st);
-  {
-    ProfScope ps(ctx, BEMGPU_K_SOLVE_GEMM, st, 0.0, 16.0 * n * nt2);
-    identity_cols_kernel<<<dim3((n + 255) / 256, nt2), 256, 0, st>>>(Y, n, n, ns2, nt2);
-    ctx->launches++;
-  }
-  rc = bem_zgetrs(ctx, W, n, n, ipiv, Y, n, nt2, st);
-  if (rc) return rc;
-  cudaEventRecord(ev[3], st);
-  {
-    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 2.0 * ((double)ns2 * ns2 + (double)nt2 * nt2),
-                 32.0 * ((double)ns2 * ns2 + (double)nt2 * nt2));
-    sym_kernel<<<dim3((ns2 + 255) / 256, ns2), 256, 0, st>>>(G1, ns2, ns2);
-    ctx->launches++;
-    sym_kernel<<<dim3((nt2 + 255) / 256, nt2), 256, 0, st>>>(G2, nt2, nt2);
-    ctx->launches++;
-  }
-  const double zero_c[2] = {0.0, 0.0};
-  rc = bem_zgemm(ctx, BEMGPU_K_TRACE, 'N', ns2, nt2, ns2, one_c, G1, ns2, Y, n, zero_c, B1, ns2, st);
-  if (!rc) rc = bem_zgemm(ctx, BEMGPU_K_TRACE, 'N', ns2, nt2, nt2, one_c, Y, n, G2, nt2, zero_c, B2, ns2, st);
-  if (rc) return rc;
-  {
-    ProfScope ps(ctx, BEMGPU_K_TRACE, st, 8.0 * ns2 * nt2, 32.0 * ns2 * nt2);
-    trace_partial_kernel<<<TRB, TR_THREADS, 0, st>>>(B1, B2, ns2, ns2, nt2, partial);
-    ctx->launches++;
-    trace_final_kernel<<<1, 32, 0, st>>>(partial, TRB, dS);
-    ctx->launches++;
-  }
-  cudaEventRecord(ev[4], st);
   double S[2];
-  int hinfo = 0;
-  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(S, dS, sizeof S, cudaMemcpyDeviceToHost, st));
-  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
-  BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-  if (bem_tc_error(ctx, true))
-    return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "heat_transfer: a grid-barrier or pipeline wait ran out");
-  if (hinfo != 0) return bem_fail(ctx, BEMGPU_ERR_SINGULAR, "heat_transfer: zero pivot at column %d", hinfo);
+  cudaEventRecord(ev[1], st);
+  rc = fp64_path_solve(ctx, W, n, ns2, G1, G2, st, S, ev);
+  if (rc) return rc;
   *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
   if (info) {
     memset(info, 0, sizeof *info);

@@ -261,6 +261,7 @@ namespace {
 // blocked solve, then the same refinement and trace as the complex64 path with
 // FP64 corrections.  Used when the complex64 factorization is not accurate
 // enough for the refinement to converge (ill-conditioned W), or on request.
+// W is factored in place; its residuals use b.opW, sliced before.
 int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cudaStream_t st, double S[2],
                  int &iters, double &err) {
   const int nt2 = n - ns2;
@@ -436,11 +437,26 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   int solver = 1;
   if (ctx->solver == 0 && !(err <= ctx->escalate_tol)) {
     // the complex64 factors are not accurate enough for this W (refinement
-    // diverged or stalled above the tolerance, or a zero pivot): factor W in
-    // FP64-class arithmetic on the tensor cores and refine with that
-    rc = fp64lu_solve(ctx, W, n, ns2, b, st, S, iters, err);
+    // diverged or stalled above the tolerance, or a zero pivot): factor a
+    // copy of W in FP64-class arithmetic on the tensor cores and refine with
+    // that.  W stays as filled for the last step: when even this refinement
+    // stalls above the fallback tolerance (its residual's ~2^-40 accuracy
+    // times the condition of W), the caller solves W on the FP64 path.
+    double *Wlu = (double *)bem_workspace(ctx, "m_Wlu", 16 * nn);
+    if (!Wlu) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: FP64-class copy of W (n=%d)", n);
+    BEM_CUDA_TRY(ctx, cudaMemcpyAsync(Wlu, W, 16 * nn, cudaMemcpyDeviceToDevice, st));
+    rc = fp64lu_solve(ctx, Wlu, n, ns2, b, st, S, iters, err);
     if (rc) return rc;
     solver = 2;
+    if (!(err <= ctx->fallback_tol)) {
+      BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (info) {
+        info->err_est = err;
+        info->refine_iters = iters;
+        info->solver = 2;
+      }
+      return BEM_SOLVE_ON_FP64_PATH;
+    }
   }
   cudaEventRecord(ev[5], st);
   BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));

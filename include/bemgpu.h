@@ -80,7 +80,8 @@ typedef struct {
   int refine_iters;
   int64_t pairs_near, pairs_far_fp64, pairs_far_fp32;
   double ms_queued, ms_latency; /* farm requests: submit -> start and submit -> done, host clock */
-  int solver;                   /* mixed path: 1 complex64 LU, 2 FP64-class tensor-core LU */
+  int solver;                   /* mixed path: 1 complex64 LU, 2 FP64-class tensor-core LU, 3 the plain
+                                   FP64 LU after the FP64-class refinement stalled (err_est then 0) */
 } bemgpu_solve_info_t;
 
 /* ---- context ---- */
@@ -120,6 +121,11 @@ int bemgpu_ctx_set_solver(bemgpu_ctx_t ctx, int mode);
 /* Error estimate of the complex64 refinement above which mode 0 escalates to
  * the FP64-class factorization (default 1e-6, the mixed path's bound). */
 int bemgpu_ctx_set_escalation_tol(bemgpu_ctx_t ctx, double tol);
+/* Error estimate of the FP64-class refinement above which mode 0 solves the
+ * same W again on the plain FP64 path (default 1e-6): the refinement's
+ * residual is exact to ~2^-40, so for W conditioned worse than ~1e6 its
+ * estimate stalls above the bound while the FP64 LU still meets it. */
+int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
 /* Failure-path self-test: one kernel polls a flag that nothing sets, gives up
  * after `spins` polls (or about a second), and records a timeout exactly as the
  * library's bounded waits do; returns BEMGPU_ERR_TIMEOUT and leaves the context

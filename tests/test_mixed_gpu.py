@@ -134,3 +134,32 @@ def test_escalation_to_fp64_class_lu():
     info = {}
     api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
     assert info["solver"] == 1
+
+
+def test_fallback_to_the_fp64_path():
+    """When the FP64-class refinement stays above the fallback tolerance, mode 0
+    solves the same (double-float-filled) W on the plain FP64 path: forced here
+    with both tolerances at 0, the result is the FP64 path's to the fill's
+    accuracy, err_est is 0 and info reports solver 3."""
+    v, t = mesh.icosphere(1.0, 1, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    b1 = b2.translated(mesh.gap_translation(v, v, 0.05))
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    ctx = api.Context(0)
+    top, s, tt = api.parseShapes(b1, b2, d, d, ctx)
+    L = _lib.load()
+    P64 = api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, tt, precision=_lib.PREC_FP64)
+    assert L.bemgpu_ctx_set_escalation_tol(ctx.handle, 0.0) == 0
+    assert L.bemgpu_ctx_set_fp64_fallback_tol(ctx.handle, 0.0) == 0
+    info = {}
+    P = api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+    assert info["solver"] == 3 and info["err_est"] == 0.0
+    assert abs(P / P64 - 1) < 1e-10, (P, P64)
+    # the same request again gives the same bits (W is kept as filled)
+    assert api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA) == P
+    assert L.bemgpu_ctx_set_fp64_fallback_tol(ctx.handle, -1.0) == _lib.ERR_ARG
+    assert L.bemgpu_ctx_set_fp64_fallback_tol(ctx.handle, 1e-6) == 0
+    assert L.bemgpu_ctx_set_escalation_tol(ctx.handle, 1e-6) == 0
+    info = {}
+    api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+    assert info["solver"] == 1
