@@ -198,6 +198,97 @@ __global__ void laswp_kernel(T *A, int64_t lda, int c0, int c1, int k1, int k2, 
   }
 }
 
+// The same interchanges for a panel of at most LASWP_MAXW rows, as one
+// permutation: warp 0 of each CTA replays the swaps on row labels in shared
+// memory (the panel's rows and the pivot rows below it), which gives for
+// every touched row the row its final content comes from; then one warp per
+// column gathers those entries into registers and writes them back (all
+// loads of a column before its stores).  Same result as the swaps in order;
+// each entry moves once instead of once per swap that touches it.
+constexpr int LASWP_MAXW = 128;
+constexpr int LASWP_WARPS = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * LASWP_WARPS)
+    laswp_perm_kernel(T *A, int64_t lda, int c0, int c1, int k1, int k2, const int *ipiv) {
+  __shared__ int row[2 * LASWP_MAXW], from[2 * LASWP_MAXW];
+  __shared__ int nslot, nmove;
+  __shared__ int mdst[2 * LASWP_MAXW], msrc[2 * LASWP_MAXW];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, m = k2 - k1;
+  if (warp == 0) {
+    for (int s = lane; s < m; s += 32) {
+      row[s] = k1 + s;
+      from[s] = k1 + s;
+    }
+    if (lane == 0) nslot = m;
+    __syncwarp();
+    for (int k = k1; k < k2; k++) {
+      const int p = ipiv[k];
+      if (p == k) continue;
+      int sp;
+      if (p < k2) {
+        sp = p - k1;
+      } else {
+        // the slot of pivot row p among the rows below the panel (appended
+        // on first use)
+        const int ns = nslot;
+        int found = -1;
+        for (int s0 = m; s0 < ns; s0 += 32) {
+          const int s = s0 + lane;
+          const unsigned hit = __ballot_sync(0xffffffffu, s < ns && row[s] == p);
+          if (hit) {
+            found = s0 + __ffs(hit) - 1;
+            break;
+          }
+        }
+        if (found < 0) {
+          found = ns;
+          if (lane == 0) {
+            row[ns] = p;
+            from[ns] = p;
+            nslot = ns + 1;
+          }
+        }
+        __syncwarp();
+        sp = found;
+      }
+      if (lane == 0) {
+        const int t = from[k - k1];
+        from[k - k1] = from[sp];
+        from[sp] = t;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) {
+      int c = 0;
+      for (int s = 0; s < nslot; s++)
+        if (from[s] != row[s]) {
+          mdst[c] = row[s];
+          msrc[c] = from[s];
+          c++;
+        }
+      nmove = c;
+    }
+  }
+  __syncthreads();
+  const int nm = nmove;
+  constexpr int PER = 2 * LASWP_MAXW / 32;
+  for (int c = c0 + blockIdx.x * LASWP_WARPS + warp; c < c1; c += gridDim.x * LASWP_WARPS) {
+    const int64_t col = (int64_t)c * lda;
+    cx<T> v[PER];
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int i = lane + 32 * j;
+      if (i < nm) v[j] = cld(A, msrc[i] + col);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < PER; j++) {
+      const int i = lane + 32 * j;
+      if (i < nm) cst(A, mdst[i] + col, v[j]);
+    }
+  }
+}
 
 // ---------------- cooperative panel factorization ----------------
 // The whole panel [k0, k0 + w) in one cooperative launch: CTA g keeps rows
@@ -850,9 +941,11 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
     }
     BEM_CUDA_TRY(ctx, cudaGetLastError());
     // interchanges to the left and right of the panel
+    static_assert(NBL <= LASWP_MAXW, "panel wider than the interchange kernel's permutation");
     if (k0 > 0) {
       ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * k0);
-      laswp_kernel<T><<<(k0 + 127) / 128, 128, 0, stream>>>(A, lda, 0, k0, k0, k0 + w, d_ipiv);
+      const int g = std::min((k0 + LASWP_WARPS - 1) / LASWP_WARPS, 2 * ctx->num_sms);
+      laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, 0, k0, k0, k0 + w, d_ipiv);
       ctx->launches++;
     }
     if (k0 + w < n) {
@@ -864,7 +957,8 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
       const int tb = std::min((nr + 7) / 8, NBL > 64 ? ctx->num_sms : ctx->num_sms * 4);
       {
         ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * nr);
-        laswp_kernel<T><<<(nr + 127) / 128, 128, 0, stream>>>(A, lda, k0 + w, n, k0, k0 + w, d_ipiv);
+        const int g = std::min((nr + LASWP_WARPS - 1) / LASWP_WARPS, 2 * ctx->num_sms);
+        laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, k0 + w, n, k0, k0 + w, d_ipiv);
         ctx->launches++;
       }
       {
