@@ -133,6 +133,10 @@ size_t bem_workspace_bytes(const bemgpu_ctx_s *ctx);
 
 // Sets ctx->last_error and returns code.
 int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...);
+// One line to stderr when the environment variable BEMGPU_TRACE is set to a
+// non-empty value other than "0" (the solver's decisions: refinement steps,
+// escalations); nothing otherwise.
+void bem_trace(const char *fmt, ...);
 // Returns a device buffer of at least `bytes` for `name` (grown on demand).
 void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes);
 // Near pairs of (t, s) built on the host (no device memory touched).

@@ -9,6 +9,7 @@
 #include <complex>
 #include <cstdarg>
 #include <cstring>
+#include <cstdlib>
 #include <algorithm>
 #include <unordered_map>
 
@@ -48,6 +49,20 @@ int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...) {
   va_end(ap);
   if (ctx) ctx->last_error = buf;
   return code;
+}
+
+void bem_trace(const char *fmt, ...) {
+  static const bool on = [] {
+    const char *v = getenv("BEMGPU_TRACE");
+    return v && v[0] && strcmp(v, "0") != 0;
+  }();
+  if (!on) return;
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  fprintf(stderr, "bemgpu: %s\n", buf);
 }
 
 void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes) {

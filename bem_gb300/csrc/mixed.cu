@@ -281,7 +281,11 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
   if (rc) return rc;
   err = 1.0;
   double err_prev = 1.0;
-  for (iters = 1; iters <= 3; iters++) {
+  // up to 6 steps: near its floor (cond(W) x ~1e-12) this refinement can
+  // contract by only ~0.5 per step, and a step costs a fraction of the FP64
+  // path it would otherwise fall back to; it stops when a step gains less
+  // than 20 %
+  for (iters = 1; iters <= 6; iters++) {
     ExactOperand opY;
     if (iters == 1) {
       rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, MIXED_SLICES, opY, st);
@@ -305,7 +309,8 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
       return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "FP64-class solve: a tensor-core pipeline wait ran out");
     err_prev = err;
     err = fabs(S[0] - Sprev[0]) / fmax(fabs(S[0]), 1e-300);
-    if (err < 3e-7 || err > 0.5 * err_prev) break;
+    bem_trace("n=%d FP64-class refinement step %d: err_est %.3e", n, iters, err);
+    if (err < 3e-7 || err > 0.8 * err_prev) break;
   }
   return BEMGPU_OK;
 }
@@ -399,7 +404,9 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   double Sprev[2] = {0, 0}, S[2] = {0, 0};
   int iters = 0;
   double err = hinfo ? 1e300 : 1.0, err_prev = 1.0;
-  const int max_iters = hinfo ? 0 : 4;
+  // up to 6 steps while each gains at least a factor 2 (slowly contracting
+  // refinements still finish well before an escalation would)
+  const int max_iters = hinfo ? 0 : 6;
   while (iters < max_iters) {
     // R = E_t - W Y: R64 holds -W Y; the first step forms it from Y, later
     // steps add -W dY of the last correction (3-slice product)
@@ -431,6 +438,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     if (iters == 1) continue;  // the spectral power of the unrefined solve is not needed
     err_prev = err;
     err = fabs(S[0] - Sprev[0]) / fmax(fabs(S[0]), 1e-300);
+    bem_trace("n=%d complex64 refinement step %d: err_est %.3e", n, iters, err);
     // converged, or stalled at the accuracy floor of the residual
     if (err < 3e-7 || err > 0.5 * err_prev) break;
   }
@@ -442,6 +450,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     // that.  W stays as filled for the last step: when even this refinement
     // stalls above the fallback tolerance (its residual's ~2^-40 accuracy
     // times the condition of W), the caller solves W on the FP64 path.
+    bem_trace("n=%d escalating to the FP64-class LU (complex64 err_est %.3e, pivot info %d)", n, err, hinfo);
     double *Wlu = (double *)bem_workspace(ctx, "m_Wlu", 16 * nn);
     if (!Wlu) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: FP64-class copy of W (n=%d)", n);
     BEM_CUDA_TRY(ctx, cudaMemcpyAsync(Wlu, W, 16 * nn, cudaMemcpyDeviceToDevice, st));
@@ -449,6 +458,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     if (rc) return rc;
     solver = 2;
     if (!(err <= ctx->fallback_tol)) {
+      bem_trace("n=%d FP64-class err_est %.3e above %.1e: solving on the FP64 path", n, err, ctx->fallback_tol);
       BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (info) {
         info->err_est = err;

@@ -126,6 +126,8 @@ int bemgpu_ctx_set_escalation_tol(bemgpu_ctx_t ctx, double tol);
  * residual is exact to ~2^-40, so for W conditioned worse than ~1e6 its
  * estimate stalls above the bound while the FP64 LU still meets it. */
 int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
+/* Tracing: with BEMGPU_TRACE set (not "0") in the environment, the library
+ * prints one line per refinement step and escalation decision to stderr. */
 /* Failure-path self-test: one kernel polls a flag that nothing sets, gives up
  * after `spins` polls (or about a second), and records a timeout exactly as the
  * library's bounded waits do; returns BEMGPU_ERR_TIMEOUT and leaves the context
