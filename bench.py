@@ -223,6 +223,13 @@ def peaks():
 # Nominal GB300 FP64 rate (vector and tensor): MEASURED_PEAKS.json carries HBM and
 # bf16 only, so FP64-bound kernels are compared with this nominal figure.
 FP64_NOMINAL_TFLOPS = 1.25
+# FP32 lanes of the GPU (152 SMs x 128): the issue rate of the double-float fill.
+FP32_LANES = 152 * 128
+# FP32-pipe thread instructions per algorithmic FP64-class flop of the
+# double-float fill kernels, from ncu's instruction counts on the ico2
+# workload: near pairs 7.06 (2.84e9 warp instructions, 8200 pairs x 1.57
+# Mflop), far pairs 6.85 (6.44e8 warp instructions, 401400 pairs x 7506 flop).
+DF_INSTR_PER_FLOP = 7.0
 
 
 def shard_steps(grid, rank, world):
@@ -404,7 +411,7 @@ def run_ours(args, rank, world):
     fill_s = sum(i["ms_fill"] for i in prof_infos) / 1e3
     pk, pk_kind = peaks()
     roof = roofline(stats, args.precision, pk, pk_kind,
-                    fp64class=all(i.get("solver") == 2 for i in prof_infos))
+                    fp64class=all(i.get("solver") == 2 for i in prof_infos), sm_mhz=clk.summary()["sm_mhz"])
     out = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -449,7 +456,7 @@ GROUPS = {
 }
 
 
-def roofline(stats, precision, pk, pk_kind, fp64class=False):
+def roofline(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None):
     """Roofline of the dominant kernel group of the timed region: algorithmic
     flops (or bytes) per CUDA-event second against the measured peak."""
     groups = dict(GROUPS)
@@ -468,13 +475,16 @@ def roofline(stats, precision, pk, pk_kind, fp64class=False):
             ach = fl / (ms / 1e3) / 1e12
             return dict(base, bound="fp64", achieved=ach, peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s",
                         frac=ach / FP64_NOMINAL_TFLOPS, peak_source="nominal GB300 FP64 (not in MEASURED_PEAKS.json)")
-        ach = fl / (ms / 1e3) / 1e12
-        return dict(base, bound="fp32 pipe (double-float)", achieved=ach, peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s",
-                    frac=ach / FP64_NOMINAL_TFLOPS,
-                    peak_source="FP64-class work in double-float; compared with the nominal FP64 rate it replaces",
-                    note="algorithmic FP64-class flops of the fill (frozen count) per CUDA-event second; the FP32 "
-                         "pipes run the double-float arithmetic at ~55 % of their issue rate (ncu, near-pair "
-                         "kernel), so frac > 1 means faster than the FP64 pipe could be, not above a roofline")
+        alg = fl / (ms / 1e3) / 1e12
+        ach = alg * DF_INSTR_PER_FLOP
+        peak = FP32_LANES * (sm_mhz or 2070.0) * 1e6 / 1e12
+        return dict(base, bound="fp32 issue (double-float)", achieved=ach, peak=peak,
+                    unit="T thread-instructions/s", frac=ach / peak,
+                    peak_source="nominal FP32 issue rate: 152 SMs x 128 lanes x the sampled SM clock",
+                    alg_fp64class_tflops=alg, instr_per_alg_flop=DF_INSTR_PER_FLOP,
+                    note="the fill is FP64-class arithmetic in double-float on the FP32 pipes: its algorithmic "
+                         "FP64-class flops (frozen count, live) per CUDA-event second times the FP32-pipe "
+                         "thread instructions per algorithmic flop that ncu counted on the two fill kernels")
     if bound == "tensor":
         ach = fl / (ms / 1e3) / 1e12
         peak = pk.get("bf16_tflops_sustained", 1700.0)
