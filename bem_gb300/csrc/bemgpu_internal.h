@@ -8,6 +8,7 @@
 #include <vector>
 #include <map>
 #include <mutex>
+#include <initializer_list>
 
 #include "../../include/bemgpu.h"
 
@@ -271,5 +272,6 @@ int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const 
 // FP64-class solve stays above ctx->fallback_tol: the caller then solves W
 // on the plain FP64 path.
 constexpr int BEM_SOLVE_ON_FP64_PATH = 100;
+void bem_release_if_short(bemgpu_ctx_s *ctx, size_t need, std::initializer_list<const char *> names);
 int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
                     cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info);

@@ -467,7 +467,7 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
   if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
                           : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
-  const int64_t kp = ((2 * (int64_t)k + 127) / 128) * 128;  // whole drain steps (4 x 32)
+  const int64_t kp = ((2 * (int64_t)k + 127) / 128) * 128;  // whole exponent blocks (drain steps)
   if ((is_a ? rp / 2 : rp) > 65535) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d rows too many", rows);
   const std::string base = std::string("ex_") + name;
   op.S = bem_workspace(ctx, base, sizeof(__nv_bfloat16) * (size_t)slices * rp * kp);

@@ -96,10 +96,12 @@ namespace {
 // Device bytes of the solve-phase buffers (everything allocated after the
 // fill and gather), mirroring the allocation sites in mixed.cu, dense.cu,
 // gemm_tc.cu and gemm_exact.cu (mixed path) or below (FP64 path).
-// `solver` is the context's mixed-path mode (bemgpu_ctx_set_solver): with 2
-// (FP64-class only) the complex64 factors, inverses and their bf16x3 slice
-// planes are never allocated, and the FP64-class LU's inverted diagonal
-// blocks are; with 0 (escalation) both sets can be live in one solve.
+// `solver` is the context's mixed-path mode (bemgpu_ctx_set_solver): with 1
+// only the complex64 factors, inverses and their bf16x3 slice planes; with 2
+// only the FP64-class LU's blocks and operands; with 0 the larger of the two
+// stages, because an escalating solve gives the complex64 buffers back before
+// it allocates the FP64-class ones (a copy of W, the FP64 fallback's Y, B1,
+// B2) when free memory is short (bem_mixed_solve, heat_transfer below).
 size_t solve_phase_bytes(int Ns, int Nt, int precision, int solver) {
   const size_t N = (size_t)Ns + Nt, n = 2 * N, ns2 = 2 * (size_t)Ns, nt2 = 2 * (size_t)Nt;
   const size_t nn = n * n, nm = n * nt2, st2 = ns2 * nt2;
@@ -112,30 +114,25 @@ size_t solve_phase_bytes(int Ns, int Nt, int precision, int solver) {
   b += bem_exact_operand_bytes(true, (int)n, (int)n, 5) + bem_exact_operand_bytes(true, (int)ns2, (int)ns2, 5) +
        bem_exact_operand_bytes(true, (int)nt2, (int)nt2, 5) + bem_exact_operand_bytes(false, (int)nt2, (int)n, 5) +
        bem_exact_operand_bytes(false, (int)nt2, (int)ns2, 5) + bem_exact_operand_bytes(false, (int)ns2, (int)nt2, 5);
-  if (solver != 2) {
-    // complex64 W, L^-1, U^-1, and two n x nt2 complex64 right-hand sides
-    b += 3 * 8 * nn + 2 * 8 * nm;
-    // bf16x3 slice planes: the largest product is the application of L^-1 /
-    // U^-1 to the n x nt2 right-hand sides; the triangular inverses' halves
-    // are smaller
+  // complex64 stage: W, L^-1, U^-1, two n x nt2 right-hand sides, and the
+  // bf16x3 slice planes (the largest product is the application of L^-1 /
+  // U^-1 to the n x nt2 right-hand sides; the triangular inverses' halves are
+  // smaller) with the triangular-inverse scratch
+  size_t c64 = 3 * 8 * nn + 2 * 8 * nm;
+  {
     size_t a1, b1, a2, b2;
     bem_cgemm_tc_bytes((int)n, (int)nt2, (int)n, a1, b1);
     bem_cgemm_tc_bytes((int)(n / 2 + 64), (int)(n / 2 + 64), (int)(n / 2 + 64), a2, b2);
-    b += std::max(a1, a2) + std::max(b1, b2);
-    b += 8 * (n / 2 + 64) * (n / 2 + 64);  // triangular-inverse scratch
+    c64 += std::max(a1, a2) + std::max(b1, b2) + 8 * (n / 2 + 64) * (n / 2 + 64);
   }
-  if (solver != 1) {
-    // FP64-class LU: the inverted 512 x 512 diagonal blocks of L and U, and
-    // the sliced operands of its K = 512 exact updates (an n x 512 panel, a
-    // 512 x n row block)
-    b += 2 * 16 * n * 512 + bem_exact_operand_bytes(true, (int)n, 512, 5) +
-         bem_exact_operand_bytes(false, (int)n, 512, 5);
-  }
-  if (solver == 0) {
-    // escalation keeps W as filled: the FP64-class LU factors a copy, and the
-    // FP64-path fallback needs its own Y, B1, B2
-    b += 16 * nn + 16 * nm + 2 * 16 * st2;
-  }
+  // FP64-class stage: the inverted 512 x 512 diagonal blocks of L and U and
+  // the sliced operands of its K = 512 exact updates (an n x 512 panel, a
+  // 512 x n row block); escalating from complex64 it also factors a copy of
+  // W and keeps room for the FP64 fallback's Y, B1, B2
+  size_t f64 = 2 * 16 * n * 512 + bem_exact_operand_bytes(true, (int)n, 512, 5) +
+               bem_exact_operand_bytes(false, (int)n, 512, 5);
+  if (solver == 0) f64 += 16 * nn + 16 * nm + 2 * 16 * st2;
+  b += solver == 1 ? c64 : solver == 2 ? f64 : std::max(c64, f64);
   b += scratch;
   return b;
 }
@@ -288,7 +285,11 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     rc = bem_mixed_solve(ctx, W, n, ns2, G1, G2, st, S, &mi);
     if (rc == BEM_SOLVE_ON_FP64_PATH) {
       // the FP64-class refinement stalled above the fallback tolerance: W is
-      // as filled, solve it on the plain FP64 path (FP64 LU, no refinement)
+      // as filled, solve it on the plain FP64 path (FP64 LU, no refinement);
+      // the mixed stages' buffers go back first if its Y, B1, B2 would not fit
+      bem_release_if_short(ctx, 16 * (size_t)n * nt2 + 2 * 16 * (size_t)ns2 * nt2,
+                           {"m_Wlu", "m_W32", "m_R32", "m_Linv", "m_Uinv", "m_T32", "tc_A", "tc_B", "tri_tmp",
+                            "ex_W", "ex_Y", "ex_X", "ex_XH", "ex_xm_A", "ex_xm_B"});
       cudaEventRecord(ev[1], st);
       rc = fp64_path_solve(ctx, W, n, ns2, G1, G2, st, S, ev);
       if (rc) return rc;

@@ -27,6 +27,7 @@
 
 #include <cmath>
 #include <algorithm>
+#include <initializer_list>
 
 namespace {
 
@@ -317,6 +318,16 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
 
 }  // namespace
 
+// Gives back named workspace buffers that a later stage no longer needs
+// when free device memory would not hold `need` more bytes beside them (the
+// largest solves); otherwise keeps them for the next request.
+void bem_release_if_short(bemgpu_ctx_s *ctx, size_t need, std::initializer_list<const char *> names) {
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  if ((double)fr >= 1.05 * (double)need + (double)(1u << 30)) return;
+  for (const char *nm : names) bem_workspace_release(ctx, nm);
+}
+
 int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
                     cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info) {
   if (!bem_exact_available())
@@ -451,13 +462,24 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     // stalls above the fallback tolerance (its residual's ~2^-40 accuracy
     // times the condition of W), the caller solves W on the FP64 path.
     bem_trace("n=%d escalating to the FP64-class LU (complex64 err_est %.3e, pivot info %d)", n, err, hinfo);
+    // the complex64 stage is done: its buffers go back first if the copy of W
+    // and the FP64-class blocks would not fit beside them
+    bem_release_if_short(ctx, 16 * nn + 2 * 16 * (size_t)n * 512 + bem_exact_operand_bytes(true, n, 512, 5) +
+                                  bem_exact_operand_bytes(false, n, 512, 5),
+                         {"m_W32", "m_R32", "m_Linv", "m_Uinv", "m_T32", "tc_A", "tc_B", "tri_tmp"});
     double *Wlu = (double *)bem_workspace(ctx, "m_Wlu", 16 * nn);
-    if (!Wlu) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: FP64-class copy of W (n=%d)", n);
-    BEM_CUDA_TRY(ctx, cudaMemcpyAsync(Wlu, W, 16 * nn, cudaMemcpyDeviceToDevice, st));
+    const bool keep_w = Wlu != nullptr;
+    if (keep_w) {
+      BEM_CUDA_TRY(ctx, cudaMemcpyAsync(Wlu, W, 16 * nn, cudaMemcpyDeviceToDevice, st));
+    } else {
+      // no room for the copy: factor W itself (no FP64 fallback afterwards)
+      bem_trace("n=%d no memory for a copy of W: factoring it in place", n);
+      Wlu = W;
+    }
     rc = fp64lu_solve(ctx, Wlu, n, ns2, b, st, S, iters, err);
     if (rc) return rc;
     solver = 2;
-    if (!(err <= ctx->fallback_tol)) {
+    if (keep_w && !(err <= ctx->fallback_tol)) {
       bem_trace("n=%d FP64-class err_est %.3e above %.1e: solving on the FP64 path", n, err, ctx->fallback_tol);
       BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (info) {
