@@ -119,3 +119,18 @@ def test_native_rwg_table_matches_python(lib):
     bad[0, 0] = v.shape[0]
     with pytest.raises(ValueError):
         mesh.build_rwgs_native(bad, v.shape[0])
+
+
+def test_solve_footprint_is_monotone_and_fits_the_slab_pair(lib):
+    """bemgpu_solve_footprint (host only): grows with the bodies, the mixed
+    path holds more than the FP64 path, and the largest workload (two
+    8190-RWG slabs, N = 32760) stays below one GB300's 284,208 MiB with the
+    default escalating solver (its complex64 and FP64-class stages are not
+    held together)."""
+    fp = lambda ns, nt, prec: lib.bemgpu_solve_footprint(ns, nt, prec)
+    for prec in (0, 2):
+        sizes = [fp(n, n, prec) for n in (288, 480, 1920, 4000, 8190)]
+        assert all(a < b for a, b in zip(sizes, sizes[1:])), sizes
+    assert fp(1920, 1920, 2) > fp(1920, 1920, 0)
+    assert fp(8190, 8190, 2) < 284208 * 2 ** 20
+    assert fp(0, 10, 2) == -1 and fp(10, -1, 0) == -1
