@@ -74,3 +74,28 @@ def test_reference_arm_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["config"]["N"] == 1152
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+
+
+def test_roofline_block_of_each_group():
+    """The roofline block names the dominant kernel group with the contract's
+    keys; the double-float fill is measured against the FP32 issue rate and
+    the exact product against the bf16 peak, with the library's count of
+    executed slice products."""
+    pk = {"hbm_gbs": 7000.0, "bf16_tflops_sustained": 1715.7}
+    fill = {"fill_near": dict(ms=38.0, flops=1.0e11, bytes=0.0, launches=3, tensor=0.0),
+            "fill_far": dict(ms=17.8, flops=7.7e10, bytes=0.0, launches=3, tensor=0.0),
+            "refine_gemm": dict(ms=33.0, flops=3.6e12, bytes=0.0, launches=10, tensor=3.1e13),
+            "trace": dict(ms=17.0, flops=1.7e12, bytes=0.0, launches=10, tensor=1.5e13)}
+    r = bench.roofline(fill, "mixed", pk, "measured", sm_mhz=2070.0)
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
+        assert k in r, k
+    assert r["kernel"] == "fill" and r["bound"].startswith("fp32 issue")
+    assert r["peak"] == pytest.approx(152 * 128 * 2070e6 / 1e12)
+    assert r["frac"] == pytest.approx(r["achieved"] / r["peak"]) and 0 < r["frac"] < 1
+    tensor = dict(fill)
+    tensor["fill_near"] = dict(fill["fill_near"], ms=1.0)
+    tensor["fill_far"] = dict(fill["fill_far"], ms=1.0)
+    r = bench.roofline(tensor, "mixed", pk, "measured", sm_mhz=2070.0)
+    assert r["kernel"] == "ex_gemm" and r["bound"] == "tensor" and r["peak"] == 1715.7
+    assert r["executed_bf16_tflops"] == pytest.approx(4.6e13 / 0.050 / 1e12)
+    assert r["slice_products_per_mac"] == pytest.approx(4.6e13 / 5.3e12)
