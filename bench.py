@@ -596,9 +596,9 @@ def run_reference_sample(wl_name, threads=None, frac=None):
 
 
 def run_reference(args, rank, world):
-    wl = WORKLOADS[args.workload]
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    """The reference arm: K bounded samples of the CPU path (the oracle port)
+    on this host's cores; the median sample is the step time.  The CPU path
+    has no caches or compilation to warm, so warm-up steps are not run."""
     samples = []
     for k in range(max(1, args.steps)):
         samples.append(run_reference_sample(args.workload))
