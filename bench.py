@@ -10,6 +10,8 @@ Synthetic meshes from bem_gb300.mesh (seeded), no dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--precision fp64|mixed] [--workload ico3|ico2|cube4|tip|slab|mix] [--lanes L]
+                  [--solver escalate|c64|fp64class] [--serve-requests R] [--sweep F]
+                  [--e2e-steps K2] [--prof-steps K3] [--no-cpu-baseline]
 
 Other workloads: cube4 (two 1 um cubes, 4x4 squares per face, N = 1152, gap
 100 nm, 20 f); tip (a cone tip over a plate, uneven N per request); slab (two
