@@ -16,6 +16,11 @@
 #define BEM_ONETHIRD 0.33333333333333333333333333333333
 #define BEM_ONEOVER4PI 0.079577471545947667884441881686257
 
+// Devices a process may use with this library: per-device state (quadrature
+// tables loaded, the allocation-free fill's scratch address) lives in arrays
+// of this size, and bemgpu_ctx_create rejects a higher device index.
+#define BEM_MAX_DEVICES 64
+
 // Device-resident per-triangle record of one RWG tree (FP64).  The frame
 // (p0, p1, p2 and derived vectors) is that of the triangle's first half-RWG in
 // the tree's RWG order: Zts integrates the outer rule over t[0] and the inner

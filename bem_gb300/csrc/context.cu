@@ -243,7 +243,8 @@ int bemgpu_ctx_create(int device, bemgpu_ctx_t *out) {
   if (!out) return BEMGPU_ERR_ARG;
   *out = nullptr;
   int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+  if (device < 0 || device >= BEM_MAX_DEVICES) return BEMGPU_ERR_ARG;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device >= ndev) {
     cudaGetLastError();
     return BEMGPU_ERR_CUDA;
   }

@@ -1365,12 +1365,14 @@ GreenDev to_dev(const bemgpu_green_t *g) {
 
 ZDev to_zdev(const bemgpu_green_t *g) { return {g->Zeps[0], g->Zeps[1], g->Zmu[0], g->Zmu[1]}; }
 
-bool g_tables_loaded[64] = {false};
+bool g_tables_loaded[BEM_MAX_DEVICES] = {false};
 
 std::mutex g_tables_mu;
 
 int load_tables(bemgpu_ctx_s *ctx) {
   // once per device; contexts on several host threads (farm lanes) may race here
+  if (ctx->device < 0 || ctx->device >= BEM_MAX_DEVICES)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "device %d outside 0..%d", ctx->device, BEM_MAX_DEVICES - 1);
   std::lock_guard<std::mutex> lk(g_tables_mu);
   if (g_tables_loaded[ctx->device]) return BEMGPU_OK;
   BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rule6, bemgpu_tri_rule6, sizeof(bemgpu_tri_rule6)));
@@ -1543,13 +1545,23 @@ extern "C" int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t 
 
 // ---------------- Zts without device allocation ----------------
 //
-// For callers that cannot allocate device memory while they run: code inside
-// a CUDA graph capture or a callback, a real-time loop that must not block on
-// the allocator, or an embedding host whose memory pool owns the device.
-// bemgpu_zts_noalloc does the same fill as bemgpu_zts into the caller's
-// buffer, but keeps its scratch (the half-pair blocks and the near-pair list)
-// in one file-scope device array of fixed size, allocated when the library
-// is loaded on a GPU and held until the process exits.
+// For callers that must not allocate device memory while they run: a solver
+// loop with a latency budget that cannot stall in cudaMalloc (which may
+// synchronise the device), or a host application whose own memory pool has
+// claimed the device memory, so that a library allocation would fail or
+// break its accounting.  bemgpu_zts_noalloc does the same FP64 fill as
+// bemgpu_zts into the caller's buffer, but keeps its scratch (the half-pair
+// blocks and the near-pair list) in one file-scope device array of fixed
+// size, created when the library's module is loaded on a GPU and held until
+// the process exits.
+//
+// What each call still does on the host: it builds the near-pair list of
+// (t, s) in host memory (a std::vector), copies it into the scratch with
+// cudaMemcpyAsync on the caller's stream and synchronises that stream before
+// returning, since the host copy belongs to the call.  The first call on a
+// device also does that device's set-up: cudaGetSymbolAddress of the scratch
+// and, if no other fill ran there yet, the upload of the quadrature tables
+// (cudaMemcpyToSymbol); make that first call before any stream capture.
 namespace {
 
 constexpr size_t NOALLOC_SCRATCH_BYTES = 32u << 20;   // 32 MiB
@@ -1558,7 +1570,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH
 
 std::mutex g_noalloc_mu;
 std::mutex g_noalloc_run_mu;  // one call at a time uses the shared scratch
-void *g_noalloc_addr[64] = {nullptr};
+void *g_noalloc_addr[BEM_MAX_DEVICES] = {nullptr};
 
 }  // namespace
 
@@ -1567,6 +1579,8 @@ extern "C" int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree
   if (!ctx || !t || !s || !g || !dZ) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: null argument");
   if (t->geom != s->geom) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: t and s must share one geometry");
   if (ldz < 2 * (int64_t)t->nrwg) return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: ldz < 2*size(t)");
+  if (ctx->device < 0 || ctx->device >= BEM_MAX_DEVICES)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "zts_noalloc: device %d outside 0..%d", ctx->device, BEM_MAX_DEVICES - 1);
   const size_t hbytes = sizeof(HalfPairBlock) * (size_t)t->nrwg * (size_t)s->nrwg;
   if (hbytes > NOALLOC_SCRATCH_BYTES - NOALLOC_NEAR_BYTES)
     return bem_fail(ctx, BEMGPU_ERR_ARG,

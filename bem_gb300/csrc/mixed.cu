@@ -32,8 +32,9 @@
 namespace {
 
 constexpr int MIXED_SLICES = 5;  // block fixed-point slices of the refinement and trace products
-constexpr int DELTA_SLICES = 3;  // slices of a correction (~1e-4 of the iterate): its products carry
-                                 // 2^-24 of their own size, far below 2^-41 of the whole
+constexpr int DELTA_SLICES = 3;  // slices of a correction: each correction is quantized to them in
+                                 // place before it is added to the iterate, so the residual's
+                                 // incremental products stay exact (to 2^-40 of |W||Y|)
 constexpr int TRACE_SLICES = 4;  // slices of X in the full trace products H1 X, H2 X^H (10 products):
                                  // ~2^-33 of |H||X| per entry; the trace of a product of two
                                  // absorption (semi-definite) operators does not cancel, so S keeps
@@ -286,19 +287,28 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
   // contract by only ~0.5 per step, and a step costs a fraction of the FP64
   // path it would otherwise fall back to; it stops when a step gains less
   // than 20 %
+  ExactOperand opDY;  // the last correction, quantized: R64 and Y move by the same values
+  unsigned eb_y = 0;   // FP64 exponent fields of the largest |Y| and |dY| entries
   for (iters = 1; iters <= 6; iters++) {
-    ExactOperand opY;
     if (iters == 1) {
+      ExactOperand opY;
       rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, MIXED_SLICES, opY, st);
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
+      if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
-      rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opY, st);
-      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 1, st);
+      // as in the complex64 refinement: every slice product while the
+      // correction is above 2^-16 of the iterate, levels 0..2 below
+      unsigned eb_dy = 0;
+      BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_dy, opDY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+      BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      opDY.exact = (int)eb_dy - (int)eb_y > -16;
+      rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opDY, b.R64, n, 1, st);
     }
     if (rc) return rc;
     residual_fp64_kernel<<<gm, 256, 0, st>>>(b.R64, b.dY, n, n, ns2);
     ctx->launches++;
     rc = bem_zgetrs_exact(ctx, W, n, n, b.ipiv, b.dY, n, nt2, st);
+    if (!rc) rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opDY, st, b.dY);
     if (rc) return rc;
     add_fp64_kernel<<<gm, 256, 0, st>>>(b.Y, b.dY, n, n);
     ctx->launches++;
@@ -418,26 +428,44 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   // up to 6 steps while each gains at least a factor 2 (slowly contracting
   // refinements still finish well before an escalation would)
   const int max_iters = hinfo ? 0 : 6;
+  ExactOperand opDY;  // the last correction, quantized: R64 and Y move by the same values
+  unsigned eb_y = 0;   // FP64 exponent fields of the largest |Y| and |dY| entries
   while (iters < max_iters) {
     // R = E_t - W Y: R64 holds -W Y; the first step forms it from Y, later
     // steps add -W dY of the last correction (3-slice product)
-    ExactOperand opY;
     if (iters == 0) {
       // the first iterate (complex64 accuracy) is quantized to 3 slices in
       // place; W's 5 slices times those 3 then need 12 slice products, not 15,
       // for the same 2^-40 residual
+      ExactOperand opY;
       rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, DELTA_SLICES, opY, st, b.Y);
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
+      if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
-      rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opY, st);
-      if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 1, st);
+      // -W dY to 2^-40 of |W||Y|: all 12 slice products of W's 5 slices and
+      // the correction's 3 exact ones while |dY| > 2^-16 |Y| (a slowly
+      // contracting refinement); below that, the 6 products of levels 0..2
+      // (error 2^-24 of |W||dY|) are as accurate at half the cost
+      unsigned eb_dy = 0;
+      BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_dy, opDY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+      BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      opDY.exact = (int)eb_dy - (int)eb_y > -16;
+      rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opDY, b.R64, n, 1, st);
     }
     if (rc) return rc;
     residual_finish_kernel<<<gm, 256, 0, st>>>(b.R64, b.R32, n, n, ns2);
     ctx->launches++;
     rc = bem_capply_inverse(ctx, b.Linv, b.Uinv, n, b.ipiv, b.R32, n, nt2, b.T32, st);
     if (rc) return rc;
-    update_kernel<<<gm, 256, 0, st>>>(b.Y, b.R32, n, n, 1, b.dY);
+    // dY = widen(correction), quantized in place to the 3 slices the next
+    // residual multiplies, then Y += dY: -W Y in R64 stays exact to the
+    // product's 2^-40 however large the correction is (a slowly contracting
+    // refinement's corrections are not small)
+    update_kernel<<<gm, 256, 0, st>>>(b.dY, b.R32, n, n, 0, nullptr);
+    ctx->launches++;
+    rc = bem_exact_prep(ctx, "Y", false, b.dY, n, nt2, n, 1.0, DELTA_SLICES, opDY, st, b.dY);
+    if (rc) return rc;
+    add_fp64_kernel<<<gm, 256, 0, st>>>(b.Y, b.dY, n, n);
     ctx->launches++;
     iters++;
     Sprev[0] = S[0];

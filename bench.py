@@ -354,6 +354,72 @@ def run_ours(args, rank, world):
     # geometry and trees from host arrays inside the timed region, submits the
     # request to the farm and reads the spectral power back.
     from bem_gb300 import mesh as _mesh
+    e2e = None
+    if not args.lite:
+        e2e = _e2e_segment(args, order, bodies, diels, ctx, farm, prec, _mesh, api, torch, a)
+
+    # The plain FP64 path on the first timed requests, through the same farm
+    # (its rate is the north-star's denominator) and, request by request, the
+    # measured error of the timed mixed-precision results against it.
+    fp64_arm, accuracy = None, None
+    n64 = min(args.fp64_steps, args.steps)
+    if n64 > 0 and args.precision != "fp64":
+        jobs64 = [job(args.warmup + k) for k in range(n64)]
+        torch.cuda.synchronize()
+        f_ev0 = torch.cuda.Event(enable_timing=True)
+        f_ev1 = torch.cuda.Event(enable_timing=True)
+        f_ev0.record()
+        P64 = farm.map(jobs64, precision=_lib.PREC_FP64)
+        torch.cuda.synchronize()
+        f_ev1.record()
+        torch.cuda.synchronize()
+        ms64 = f_ev0.elapsed_time(f_ev1)
+        errs = [abs(Ps[k] / P64[k] - 1) for k in range(n64)]
+        fp64_arm = {"value": n64 / (ms64 / 1e3), "unit": "solves/s", "steps": n64, "ms_per_step": ms64 / n64,
+                    "lanes": args.lanes, "note": "the plain FP64 path (complex128 fill, FP64 LU on the FMA pipes) "
+                                                 "on the first timed requests, through the same farm"}
+        accuracy = {"err_vs_fp64_max": max(errs), "err_vs_fp64": errs,
+                    "err_est_same_solves": [infos[k]["err_est"] for k in range(n64)], "solves_checked": n64,
+                    "note": "relative error of the timed mixed-precision spectral power against the FP64 path "
+                            "on the same requests"}
+    farm.close()
+
+    n_all = sorted({2 * sy[0].rwgs for sy in systems})
+    n_unknowns = n_all[0] if len(n_all) == 1 else f"{n_all[0]}-{n_all[-1]}"
+    value = args.steps * world / (ms / 1e3)
+    out = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
+        "data": "synthetic (seeded generated meshes; no dataset)",
+        "config": workload_config(args, n_unknowns, world),
+        "err_est": [i["err_est"] for i in infos], "refine_iters": [i["refine_iters"] for i in infos],
+        "factorization": {"complex64": sum(i["solver"] == 1 for i in infos),
+                          "fp64class": sum(i["solver"] == 2 for i in infos),
+                          "fp64_fallback": sum(i["solver"] == 3 for i in infos)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "serving": serving,
+        "P_sample": Ps[:2],
+    }
+    if fp64_arm:
+        out["fp64_path"] = fp64_arm
+        out["mixed_over_fp64"] = value / fp64_arm["value"]
+        out["accuracy"] = accuracy
+    if args.lite:
+        out["stage_ms"] = {k: sum(i[k] for i in infos) / len(infos)
+                           for k in ("ms_fill", "ms_lu", "ms_solve", "ms_trace", "ms_refine")}
+        out["stage_ms_note"] = "per-solve stage times inside the timed region (lanes overlapping)"
+        return out
+    out["e2e"] = e2e
+    out.update(_kernel_segment(args, job, prec, ctx, clk, L, api, torch, _lib, ctypes))
+    return out
+
+
+def _e2e_segment(args, order, bodies, diels, ctx, farm, prec, _mesh, api, torch, a):
+    """e2e through the public API from host buffers: each step uploads its
+    geometry and trees from host arrays inside the timed region, submits the
+    request to the farm and reads the spectral power back."""
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_ev0 = torch.cuda.Event(enable_timing=True)
@@ -378,12 +444,15 @@ def run_ours(args, rank, world):
     e2e_ms = e2e_ev0.elapsed_time(e2e_ev1)
     e2e_wall = (time.perf_counter() - t0) * 1e3
     e2e_ms = max(e2e_ms, e2e_wall)
-    farm.close()
+    return {"value": e2e_steps / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
+            "d2h_bytes_per_step": 8 + 16 + 4}
 
-    # Per-kernel times for the roofline: overlapped lanes inflate each other's
-    # event-timed kernel durations, so the kernels are timed (CUDA events on
-    # the launching stream, per kernel class) over solves run one at a time,
-    # the same requests as the first timed steps.
+
+def _kernel_segment(args, job, prec, ctx, clk, L, api, torch, _lib, ctypes):
+    """Per-kernel times for the roofline: overlapped lanes inflate each
+    other's event-timed kernel durations, so the kernels are timed (CUDA
+    events on the launching stream, per kernel class) over solves run one at
+    a time, the same requests as the first timed steps."""
     n_prof = args.prof_steps or min(args.steps, 4)
     prof_jobs = [job(args.warmup + k) for k in range(n_prof)]
     api.CalcHeatTransfer(*job(0), precision=prec, strict=False)  # workspace of this context
@@ -407,39 +476,21 @@ def run_ours(args, rank, world):
         n, ns2, nt2 = 2 * j[4].rwgs, 2 * j[5].rwgs, 2 * j[6].rwgs
         return n ** 2 + ns2 ** 2 + nt2 ** 2
 
-    n_all = sorted({2 * sy[0].rwgs for sy in systems})
-    n_unknowns = n_all[0] if len(n_all) == 1 else f"{n_all[0]}-{n_all[-1]}"
-    value = args.steps * world / (ms / 1e3)
     fill_s = sum(i["ms_fill"] for i in prof_infos) / 1e3
     pk, pk_kind = peaks()
     roof = roofline(stats, args.precision, pk, pk_kind,
                     fp64class=all(i.get("solver") == 2 for i in prof_infos), sm_mhz=clk.summary()["sm_mhz"])
-    out = {
-        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
-        "data": "synthetic (seeded generated meshes; no dataset)",
-        "config": workload_config(args, n_unknowns, world),
+    return {
         "fill_gentries_per_s": sum(entries(j) for j in prof_jobs) / fill_s / 1e9,
         # the three Zts outputs written as complex128 (16 B per entry)
         "fill_write_gbs": 16 * sum(entries(j) for j in prof_jobs) / fill_s / 1e9,
         "stage_ms": {k: sum(i[k] for i in prof_infos) / len(prof_infos)
                      for k in ("ms_fill", "ms_lu", "ms_solve", "ms_trace", "ms_refine")},
-        "err_est": [i["err_est"] for i in infos], "refine_iters": [i["refine_iters"] for i in infos],
-        "factorization": {"complex64": sum(i["solver"] == 1 for i in infos),
-                          "fp64class": sum(i["solver"] == 2 for i in infos)},
         "kernel_ms_per_step": {k: v["ms"] / n_prof for k, v in stats.items()},
         "kernel_ms_note": f"stage and kernel-class times (and the fill rate) over {n_prof} solves run one at "
                           f"a time, without lane overlap",
         "roofline": roof,
-        "gpu_launches": int(launches),
-        "e2e": {"value": e2e_steps / (e2e_ms / 1e3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / e2e_steps),
-                "d2h_bytes_per_step": 8 + 16 + 4},
-        "clocks": clk.summary(),
-        "serving": serving,
-        "P_sample": Ps[:2],
     }
-    return out
 
 
 # Kernel groups of the per-kind breakdown and the resource that bounds each.
@@ -531,88 +582,202 @@ def workload_config(args, n_unknowns, world):
             "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_max ** 2 * 16 / 1e6)}
 
 
-LA_FULL_MAX = 8192
+# CPU baseline: the reference path's CPU implementation (the oracle port,
+# pinned to the reference binary) in the reference's throughput mode, the MPI
+# task farm of src/transfer-mpi.cpp:91-190: one single-threaded process per
+# host core (OPENBLAS_NUM_THREADS=1; the reference's fill has no threading,
+# src/Impedance.cpp:388-413), all running at once.  Each process times a
+# bounded sample of one solve and extrapolates it to the whole solve:
+#   fill: the three Zts calls over CPU_FILL_UNITS far-pair equivalents of
+#         test triangles (a near pair counts as CPU_NEAR_UNITS), x the
+#         triangles / sampled triangles (the same fraction of each call);
+#   algebra: zgetrf + zgetri (src/util/DenseMatrix.cpp:65-77), the two
+#         products and B2^H B1 (src/HeatTransfer.cpp:36-52) at
+#         n_la = min(n, CPU_LA_MAX) with the bodies' proportions, x (n/n_la)^3.
+CPU_FILL_UNITS = 4.0e5
+CPU_NEAR_UNITS = 150.0
+NEAR_PER_TRIANGLE = 13.0
+CPU_LA_MAX = 2048
+# sample steps of the cpu_baseline block of the GPU arm's line
+CPU_BASELINE_STEPS = 3
+
+_CPU_SYSTEMS = {}
 
 
-def _reference_solve_time(b1, b2, cfg, f, threads, frac=None):
-    """Seconds of one solve of the oracle port: the three fills over a
-    fraction of the test triangles (scaled up by the triangle count) and the
-    dense algebra (inverse and the two products of the trace) at full size,
-    or at n = 4096 scaled by (n / 4096)^3 above n = LA_FULL_MAX."""
-    from bem_gb300 import mesh
+def _cpu_system(wl_name, gi):
+    key = (wl_name, gi)
+    if key not in _CPU_SYSTEMS:
+        from bem_gb300 import mesh
+        b1, b2, cfg = make_bodies(WORKLOADS[wl_name])[gi]
+        xyz, tris, rwg, ns = mesh.two_body(b1, b2)
+        _CPU_SYSTEMS[key] = (xyz, tris, rwg, ns, b1.nt, b2.nt, cfg)
+    return _CPU_SYSTEMS[key]
+
+
+def _cpu_solve_sample(task):
+    """One process's bounded, single-threaded sample of one solve of the
+    oracle port (see CPU_FILL_UNITS); returns its extrapolated seconds."""
+    wl_name, gi, f, offset = task
+    import scipy.linalg.lapack as lapack
     from oracle import oracle
-    xyz, tris, rwg, ns = mesh.two_body(b1, b2)
-    ntri = b1.nt + b2.nt
-    frac = frac or (1.0 if ntri <= 500 else 64.0 / ntri)
+    xyz, tris, rwg, ns, nt1, nt2, cfg = _cpu_system(wl_name, gi)
+    ntri = nt1 + nt2
+    units = (ntri + NEAR_PER_TRIANGLE * CPU_NEAR_UNITS) * ntri
+    units += sum((m + NEAR_PER_TRIANGLE * CPU_NEAR_UNITS) * m for m in (nt1, nt2))
+    frac = min(1.0, CPU_FILL_UNITS / units)
     om = oracle.dimensionless_omega(1e-6, f)
     eps = oracle.lorentz_eps(f, *cfg)
-    t0 = time.perf_counter()
-    k = max(1, int(round(frac * ntri)))
-    oracle.zts(xyz, tris, rwg, rwg, 1 + 0j, 1 + 0j, om, tri_range=(0, k), nthreads=threads)
-    k1 = max(1, int(round(frac * b1.nt)))
-    oracle.zts(xyz, tris, rwg[:ns], rwg[:ns], eps, 1 + 0j, om, tri_range=(0, k1), nthreads=threads)
-    k2 = max(1, int(round(frac * b2.nt)))
-    oracle.zts(xyz, tris, rwg[ns:], rwg[ns:], eps, 1 + 0j, om, tri_range=(0, k2), nthreads=threads)
-    # each call's time scales with its own test-triangle count; the sample
-    # keeps the three in proportion, so one factor scales the sum
-    t_fill = (time.perf_counter() - t0) * (ntri / k)
+    t_fill = 0.0
+    for rows, m, e in ((rwg, ntri, 1 + 0j), (rwg[:ns], nt1, eps), (rwg[ns:], nt2, eps)):
+        k = max(1, int(round(frac * m)))
+        lo = (offset * k) % m
+        hi = min(m, lo + k)
+        t0 = time.perf_counter()
+        oracle.zts(xyz, tris, rows, rows, e, 1 + 0j, om, tri_range=(lo, hi), nthreads=1, timing_only=True)
+        t_fill += (time.perf_counter() - t0) * m / (hi - lo)
     n = 2 * rwg.shape[0]
-    n_la = n if n <= LA_FULL_MAX else 4096
-    ns2 = min(2 * ns, n_la - 2) if n_la < n else 2 * ns
-    rng = np.random.default_rng(0)
-    W = rng.standard_normal((n_la, n_la)) + 1j * rng.standard_normal((n_la, n_la)) + n_la * np.eye(n_la)
+    n_la = min(n, CPU_LA_MAX)
+    ns2 = 2 * max(1, int(round(ns * n_la / n)))
+    rng = np.random.default_rng(offset)
+    W = np.asfortranarray(rng.standard_normal((n_la, n_la)) + 1j * rng.standard_normal((n_la, n_la))
+                          + n_la * np.eye(n_la))
+    G1 = rng.standard_normal((ns2, ns2)) + 1j * rng.standard_normal((ns2, ns2))
+    G2 = rng.standard_normal((n_la - ns2,) * 2) + 1j * rng.standard_normal((n_la - ns2,) * 2)
     t0 = time.perf_counter()
-    Wi = np.linalg.inv(W)
-    G = W[:ns2, :ns2]
-    B1 = (G @ Wi[:ns2, :])[:, ns2:]
-    B2 = (Wi[:, ns2:] @ W[ns2:, ns2:])[:ns2, :]
+    lu, piv, info = lapack.zgetrf(W, overwrite_a=True)
+    Wi, info = lapack.zgetri(lu, piv, overwrite_lu=True)
+    B1 = ((G1 + G1.conj().T) @ Wi[:ns2, :])[:, ns2:]
+    B2 = (Wi[:, ns2:] @ (G2 + G2.conj().T))[:ns2, :]
     _ = np.trace(B2.conj().T @ B1)
     t_la = (time.perf_counter() - t0) * (n / n_la) ** 3
-    note = f"fills over {k}/{ntri} test triangles (x{ntri / k:.1f}) + inverse/products at n={n_la}"
-    if n_la < n:
-        note += f" scaled by (n/{n_la})^3"
-    return t_fill + t_la, t_fill, t_la, n, note
+    return {"solve_s": t_fill + t_la, "fill_s": t_fill, "la_s": t_la, "n": n, "n_la": n_la,
+            "fill_scale": 1.0 / frac, "la_scale": (n / n_la) ** 3}
 
 
-def run_reference_sample(wl_name, threads=None, frac=None):
-    """Times the oracle port (the reference path restated on the CPU) on a
-    bounded sample of the workload's solves: one solve for the fixed-geometry
-    workloads, the mean over the first four requests for the mix."""
-    wl = WORKLOADS[wl_name]
-    threads = threads or os.cpu_count() or 1
-    bodies = make_bodies(wl)
-    grid = step_grid(wl)
-    picks = range(min(4, len(bodies))) if wl["kind"] == "mix" else [0]
-    times, notes, ns = [], [], []
-    for gi in picks:
-        f = next(ff for (g, ff, _) in grid if g == gi)
-        b1, b2, cfg = bodies[gi]
-        tot, t_fill, t_la, n, note = _reference_solve_time(b1, b2, cfg, f, threads, frac)
-        times.append((tot, t_fill, t_la))
-        notes.append(note)
-        ns.append(n)
-    m = [float(np.mean([t[i] for t in times])) for i in range(3)]
-    sample = "; ".join(notes) + (f" (mean of {len(picks)} requests)" if len(picks) > 1 else ", one frequency")
-    return {"solve_s": m[0], "fill_s": m[1], "la_s": m[2], "threads": threads,
-            "n": ns[0] if len(set(ns)) == 1 else f"{min(ns)}-{max(ns)}", "sample": sample}
+def _cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+class CpuFarm:
+    """The throughput-mode CPU baseline: `procs` spawned single-threaded
+    worker processes (spawned, so that they are safe after GPU work)."""
+
+    def __init__(self, wl_name, procs=None):
+        import multiprocessing as mp
+        self.wl_name = wl_name
+        self.procs = procs or _cpu_cores()
+        self.grid = step_grid(WORKLOADS[wl_name])
+        saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")}
+        for k in saved:
+            os.environ[k] = "1"
+        try:
+            self.pool = mp.get_context("spawn").Pool(self.procs)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+
+    def step(self, k):
+        """One sample step: every process times its own solve sample at
+        once; returns (solves/s of the farm, wall seconds, samples)."""
+        tasks = []
+        for p in range(self.procs):
+            gi, f, _ = self.grid[(k * self.procs + p) % len(self.grid)]
+            tasks.append((self.wl_name, gi, f, k * self.procs + p))
+        t0 = time.perf_counter()
+        res = self.pool.map(_cpu_solve_sample, tasks, chunksize=1)
+        wall = time.perf_counter() - t0
+        return sum(1.0 / r["solve_s"] for r in res), wall, res
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def cpu_baseline_run(wl_name, steps, procs=None):
+    farm = CpuFarm(wl_name, procs)
+    try:
+        vals, walls, res = [], [], []
+        for k in range(steps):
+            v, w, r = farm.step(k)
+            vals.append(v)
+            walls.append(w)
+            res.extend(r)
+    finally:
+        farm.close()
+    fs = sorted(r["fill_scale"] for r in res)
+    ls = sorted(r["la_scale"] for r in res)
+    n_all = sorted({r["n"] for r in res})
+    sample = (f"throughput mode: {farm.procs} single-threaded processes at once (OPENBLAS_NUM_THREADS=1), "
+              f"each timing one solve of the oracle port per step: the three fills over sampled test triangles "
+              f"(extrapolation x{fs[0]:.0f}-x{fs[-1]:.0f}) + zgetrf/zgetri and the trace products at "
+              f"n_la={min(r['n_la'] for r in res)} (x{ls[0]:.1f}-x{ls[-1]:.1f} by (n/n_la)^3); "
+              f"value = sum over processes of 1/(extrapolated solve time), median over {steps} steps")
+    return {"value": statistics.median(vals), "spread": {"min": min(vals), "median": statistics.median(vals),
+                                                        "max": max(vals), "steps": steps},
+            "ms_per_step": 1e3 * statistics.median(walls), "cores": farm.procs,
+            "n": n_all[0] if len(n_all) == 1 else f"{n_all[0]}-{n_all[-1]}", "sample": sample,
+            "fill_s_per_solve": statistics.median(r["fill_s"] for r in res),
+            "la_s_per_solve": statistics.median(r["la_s"] for r in res)}
 
 
 def run_reference(args, rank, world):
-    """The reference arm: K bounded samples of the CPU path (the oracle port)
-    on this host's cores; the median sample is the step time.  The CPU path
-    has no caches or compilation to warm, so warm-up steps are not run."""
-    samples = []
-    for k in range(max(1, args.steps)):
-        samples.append(run_reference_sample(args.workload))
-    s = statistics.median(x["solve_s"] for x in samples)
-    v = 1.0 / s
-    return {"metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": s * 1e3, "higher_is_better": True, "scaling": "weak",
+    """The reference arm: the reference path's CPU implementation in its
+    throughput mode (CpuFarm) on this host's cores, one bounded sample step
+    per timed step (no warm-up: nothing is cached or compiled).  value is
+    the median step's extrapolated solves/s; ms_per_step is a sample step's
+    wall time."""
+    r = cpu_baseline_run(args.workload, max(1, args.steps))
+    return {"metric": METRIC, "value": r["value"], "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded meshes; no dataset)",
-            "config": workload_config(args, samples[0]["n"], world), "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": samples[0]["threads"], "kind": "port",
-                             "sample": samples[0]["sample"]},
-            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": workload_config(args, r["n"], world), "impl": "reference",
+            "cpu_baseline": {"value": r["value"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"], "spread": r["spread"],
+                             "fill_s_per_solve": r["fill_s_per_solve"], "la_s_per_solve": r["la_s_per_solve"]},
+            "e2e": {"value": r["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# Sub-results of the default line: the other synthetic workloads, each run as
+# its own bench process (its own GPU memory) after the main measurement, and
+# summarised in the main line.  slab: the large single solve (N = 32760, one
+# FP64-class solve after one warm-up solve of the same size); mix: the
+# serving mix (64 requests: closed-loop rate of one frequency per request,
+# then 64 Poisson-arrival sweeps of SUB_MIX_SWEEP frequencies).
+SUB_MIX_SWEEP = 8
+SUBS = {
+    "slab": ["--workload", "slab", "--solver", "fp64class", "--steps", "1", "--warmup", "1", "--lanes", "1",
+             "--serve-requests", "0", "--fp64-steps", "0", "--lite"],
+    "mix": ["--workload", "mix", "--steps", "64", "--warmup", "4", "--serve-requests", "64",
+            "--sweep", str(SUB_MIX_SWEEP), "--lite"],
+    "tip": ["--workload", "tip", "--steps", "64", "--warmup", "4", "--serve-requests", "0", "--lite"],
+}
+SUB_KEYS = ("value", "unit", "ms_per_step", "steps", "config", "err_est", "factorization", "serving", "stage_ms",
+            "fp64_path", "accuracy", "mixed_over_fp64", "clocks", "gpu_launches", "fill_gentries_per_s")
+
+
+def run_subs(names):
+    out = {}
+    for nm in names:
+        cmd = [sys.executable, os.path.abspath(__file__), *SUBS[nm], "--no-cpu-baseline", "--subs", "none"]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        wall = time.perf_counter() - t0
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            out[nm] = {"failed": f"rc={r.returncode}", "stderr_tail": r.stderr[-600:]}
+            continue
+        d = json.loads(lines[-1])
+        sub = {k: d[k] for k in SUB_KEYS if k in d}
+        sub["cmd"] = "python bench.py " + " ".join(SUBS[nm])
+        sub["wall_s"] = wall
+        out[nm] = sub
+    return out
 
 
 def main():
@@ -625,7 +790,7 @@ def main():
     ap.add_argument("--workload", default="ico3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=4, help="farm lanes: solves in flight at once on the GPU")
-    ap.add_argument("--serve-requests", type=int, default=16,
+    ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests of the Poisson-arrival serving measurement (0: skip)")
     ap.add_argument("--solver", default="escalate", choices=["escalate", "c64", "fp64class"],
                     help="mixed-path factorization: complex64 LU escalating to the FP64-class LU when the "
@@ -635,6 +800,13 @@ def main():
                     help="solves run one at a time for the kernel statistics (default: min(--steps, 4))")
     ap.add_argument("--sweep", type=int, default=0,
                     help="frequencies per serving request of the mix workload (default: the workload's 32)")
+    ap.add_argument("--fp64-steps", type=int, default=4,
+                    help="timed requests solved again on the plain FP64 path (rate and measured error; 0: skip)")
+    ap.add_argument("--subs", default="default",
+                    help="comma-separated sub-workloads summarised in the line (slab, mix, tip), 'none', or "
+                         "'default' (slab,mix for the default ico3 workload, none otherwise)")
+    ap.add_argument("--lite", action="store_true",
+                    help="skip the end-to-end and per-kernel segments (sub-workload runs)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     if world > 1 and args.impl == "ours":
@@ -645,11 +817,15 @@ def main():
             print(json.dumps(run_reference(args, rank, world)))
         return
     out = run_ours(args, rank, world)
+    subs = (["slab", "mix"] if args.workload == "ico3" else []) if args.subs == "default" else \
+        [x for x in args.subs.split(",") if x and x != "none"]
+    if rank == 0 and subs and world == 1:
+        out["subs"] = run_subs(subs)
     if rank == 0:
         if not args.no_cpu_baseline and world == 1:
-            r = run_reference_sample(args.workload)
-            out["cpu_baseline"] = {"value": 1.0 / r["solve_s"], "unit": "solves/s", "cores": r["threads"],
-                                   "kind": "port", "sample": r["sample"]}
+            r = cpu_baseline_run(args.workload, CPU_BASELINE_STEPS)
+            out["cpu_baseline"] = {"value": r["value"], "unit": "solves/s", "cores": r["cores"], "kind": "port",
+                                   "sample": r["sample"], "spread": r["spread"]}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

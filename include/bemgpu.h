@@ -201,17 +201,20 @@ int bemgpu_zts_host(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const be
                     const bemgpu_options_t *opt, int precision, double *Z, int64_t ldz);
 
 /* Zts(t, s, g) in FP64 into the caller's device buffer dZ without allocating
- * device memory (no counterpart in the reference).  For callers that cannot
- * allocate while they run: code inside a CUDA graph capture or a stream
- * callback, a real-time loop that must not block on the allocator, or a host
- * application whose own pool owns the device memory.  The scratch is one
- * file-scope device array of 32 MiB that every GPU loading the library holds
- * until the process exits; it bounds size(t) * size(s) to 245760 RWG pairs
- * (and the near-pair list to 131072 pairs), larger requests return
- * BEMGPU_ERR_ARG.  The first call on a device looks up that array's device
- * address (make it before any stream capture).  All calls share the array:
- * calls that overlap on the GPU race, so serialize them (one stream, or wait
- * for the previous call).  Synchronous: returns once dZ is written. */
+ * device memory (no counterpart in the reference).  For callers that must not
+ * allocate while they run: a solver loop with a latency budget that cannot
+ * stall in cudaMalloc, or a host application whose own memory pool has
+ * claimed the device memory.  The scratch is one file-scope device array of
+ * 32 MiB that every GPU loading the library holds until the process exits; it
+ * bounds size(t) * size(s) to 245760 RWG pairs (and the near-pair list to
+ * 131072 pairs), larger requests return BEMGPU_ERR_ARG.  The first call on a
+ * device does that device's set-up (the array's device address, and the
+ * quadrature tables if no fill ran there yet): make it before any stream
+ * capture.  Each call builds the near-pair list in host memory, copies it to
+ * the scratch on `stream` and synchronises `stream` before it returns (dZ is
+ * then written).  All calls share the array: calls from one process take
+ * turns, but calls that overlap on the GPU (other processes' are separate)
+ * would race, so serialise them. */
 int bemgpu_zts_noalloc(bemgpu_ctx_t ctx, bemgpu_tree_t t, bemgpu_tree_t s, const bemgpu_green_t *g,
                        const bemgpu_options_t *opt, void *dZ, int64_t ldz, void *stream);
 

@@ -458,7 +458,11 @@ typedef struct {
   int tid, nthreads;
   int tbeg, tend;
   int64_t counts[8];
+  cplx sink[4]; /* timing mode (no output matrix): the scattered values are summed here */
 } job_t;
+
+/* Sum of the timing mode's sinks, so that the integration it times is kept. */
+volatile double oracle_timing_checksum;
 
 static int kind_slot(int kind) {
   switch (kind) { case 0: return 0; case 1: return 1; case 6: return 2; case 10: return 3;
@@ -488,6 +492,14 @@ static void *zts_worker(void *arg) {
           double c = ONEOVER4PI * hi->elen * hj->elen;
           if (hi->positive != hj->positive) c = -c;
           cplx Lij = c * L[ij], Kij = c * K[ij];
+          if (!Z) {
+            J->sink[0] += J->g->Zeps * Lij;
+            J->sink[1] += Kij;
+            J->sink[2] -= Kij;
+            J->sink[3] += J->g->Zmu * Lij;
+            ij++;
+            continue;
+          }
           Z[ii + J->ld * jj] += J->g->Zeps * Lij;
           Z[ii + J->ld * (jj + 1)] += Kij;
           Z[ii + 1 + J->ld * jj] -= Kij;
@@ -522,7 +534,10 @@ static int build_halves(const geom_t *G, const int *rwg, int nrwg, tri_halves_t 
  * from (eps, mu, omega) as GreensFunction::init does.  farThresh = Options'
  * farThresh6/10/15/21 (src/Options.cpp:23-26).  Only test triangles at
  * positions [tri_begin, tri_end) of t's triangle list are integrated (a
- * bounded sample for CPU timing; pass 0, -1 for all).  Writes the number of
+ * bounded sample for CPU timing; pass 0, -1 for all).  With Zout NULL
+ * (timing mode) the same pairs are integrated and scaled, but the values are
+ * summed into a per-thread sink instead of a matrix, so that a sample of a
+ * large fill needs no n x n buffer.  Writes the number of
  * pairs integrated by each branch into counts[7] (same, neighbour, rule 6, 10,
  * 15, 21, 36) when counts is non-null.  Returns 0 or a negative error.
  */
@@ -543,22 +558,31 @@ int oracle_zts(const double *xyz, int nv, const int *tri, int nt, const int *rwg
   if (tri_end < 0 || tri_end > ntl) tri_end = ntl;
   if (tri_begin < 0) tri_begin = 0;
   int64_t rows = 2 * (int64_t)nrwg_t, cols = 2 * (int64_t)nrwg_s;
-  cplx *Z = (cplx *)Zout;
-  for (int64_t j = 0; j < cols; j++) memset(Z + ld * j, 0, sizeof(cplx) * rows);
-  cplx *Zneg = (cplx *)calloc((size_t)(ld * cols), sizeof(cplx));
-  if (!Zneg) { free(th); free(sh); free(tl); free(sl); return -2; }
+  cplx *Z = (cplx *)Zout, *Zneg = NULL;
+  if (Z) {
+    for (int64_t j = 0; j < cols; j++) memset(Z + ld * j, 0, sizeof(cplx) * rows);
+    Zneg = (cplx *)calloc((size_t)(ld * cols), sizeof(cplx));
+    if (!Zneg) { free(th); free(sh); free(tl); free(sl); return -2; }
+  }
   if (nthreads < 1) nthreads = 1;
   job_t *jobs = (job_t *)calloc(nthreads, sizeof(job_t));
   pthread_t *tids = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
   for (int k = 0; k < nthreads; k++) {
-    job_t J = {&G, &g, farThresh, th, sh, tl, sl, ntl, nsl, Z, Zneg, ld, k, nthreads, tri_begin, tri_end, {0}};
+    job_t J = {&G, &g, farThresh, th, sh, tl, sl, ntl, nsl, Z, Zneg, ld, k, nthreads, tri_begin, tri_end, {0}, {0}};
     jobs[k] = J;
   }
   for (int k = 1; k < nthreads; k++) pthread_create(&tids[k], NULL, zts_worker, &jobs[k]);
   zts_worker(&jobs[0]);
   for (int k = 1; k < nthreads; k++) pthread_join(tids[k], NULL);
-  for (int64_t j = 0; j < cols; j++)
-    for (int64_t i = 0; i < rows; i++) Z[i + ld * j] += Zneg[i + ld * j];
+  if (Z) {
+    for (int64_t j = 0; j < cols; j++)
+      for (int64_t i = 0; i < rows; i++) Z[i + ld * j] += Zneg[i + ld * j];
+  } else {
+    double sum = 0.0;
+    for (int k = 0; k < nthreads; k++)
+      for (int c = 0; c < 4; c++) sum += creal(jobs[k].sink[c]) + cimag(jobs[k].sink[c]);
+    oracle_timing_checksum = sum;
+  }
   if (counts) {
     for (int c = 0; c < 7; c++) {
       counts[c] = 0;

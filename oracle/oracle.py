@@ -86,15 +86,17 @@ def green_constants(eps: complex, mu: complex, omega: complex) -> dict:
 
 
 def zts(xyz, tris, rwg_t, rwg_s, eps: complex, mu: complex, omega: complex, far=FAR_THRESH,
-        tri_range=(0, -1), nthreads: int | None = None, counts: bool = False):
+        tri_range=(0, -1), nthreads: int | None = None, counts: bool = False, timing_only: bool = False):
     """Zts(t, s, g) (src/Impedance.cpp:388-413) on one shared geometry.
-    Returns the (2*Nt x 2*Ns) complex128 matrix in column-major (Fortran) order."""
+    Returns the (2*Nt x 2*Ns) complex128 matrix in column-major (Fortran) order.
+    timing_only: integrate the same pairs without an output matrix (a CPU
+    timing sample of a fill too large to hold per process); returns None."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     tris = np.ascontiguousarray(tris, dtype=np.int32)
     rwg_t = np.ascontiguousarray(rwg_t, dtype=np.int32)
     rwg_s = np.ascontiguousarray(rwg_s, dtype=np.int32)
     nt_rwg, ns_rwg = rwg_t.shape[0], rwg_s.shape[0]
-    Z = np.zeros((2 * nt_rwg, 2 * ns_rwg), dtype=np.complex128, order="F")
+    Z = None if timing_only else np.zeros((2 * nt_rwg, 2 * ns_rwg), dtype=np.complex128, order="F")
     emo = np.array([eps.real, eps.imag, mu.real, mu.imag, complex(omega).real, complex(omega).imag])
     far = np.asarray(far, dtype=np.float64)
     cnt = np.zeros(7, dtype=np.int64)
@@ -102,7 +104,8 @@ def zts(xyz, tris, rwg_t, rwg_s, eps: complex, mu: complex, omega: complex, far=
         nthreads = os.cpu_count() or 1
     rc = lib().oracle_zts(xyz.ctypes.data, xyz.shape[0], tris.ctypes.data, tris.shape[0],
                           rwg_t.ctypes.data, nt_rwg, rwg_s.ctypes.data, ns_rwg, emo.ctypes.data,
-                          far.ctypes.data, Z.ctypes.data, 2 * nt_rwg, int(tri_range[0]), int(tri_range[1]),
+                          far.ctypes.data, None if Z is None else Z.ctypes.data, 2 * nt_rwg,
+                          int(tri_range[0]), int(tri_range[1]),
                           int(nthreads), cnt.ctypes.data)
     if rc != 0:
         raise RuntimeError(f"oracle_zts failed: {rc}")

@@ -12,7 +12,7 @@ does not reproduce with its current code), so these fixtures are the pin.
 
 Usage (where the reference checkout is present):
     make -f oracle/Makefile.ref -j8
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case names]   # all cases, or only the named ones
 """
 from __future__ import annotations
 
@@ -91,7 +91,31 @@ def main():
     v, t = mesh.cube(1.0, 2)
     run_case("cube2_alumina_gap50nm", v, t, v, t, mesh.gap_translation(v, v, 0.05), [0.09, 0.1, 0.12], ALUMINA,
              ALUMINA)
+    # 5. jittered icospheres L2 (N = 1920) at 50 nm, below, at and above SiC's surface-phonon resonance
+    v, t = mesh.icosphere(1.0, 2, jitter=0.02, seed=12345)
+    run_case("ico2_gap50nm", v, t, v, t, mesh.gap_translation(v, v, 0.05), [0.0983, 0.116, 0.125], SIC, SIC)
+    # 6. the precision-form workload itself: jittered icospheres L3 (N = 7680) at its smallest gap, 20 nm,
+    #    at omega_TO and in the surface-phonon band
+    v, t = mesh.icosphere(1.0, 3, jitter=0.02, seed=12345)
+    run_case("ico3_gap20nm", v, t, v, t, mesh.gap_translation(v, v, 0.02), [0.0983, 0.116], SIC, SIC)
+
+
+def main_only(names):
+    """Regenerates the named cases only (each case is independent)."""
+    saved = globals()["run_case"]
+
+    def pick(name, *a, **k):
+        if name in names:
+            saved(name, *a, **k)
+    globals()["run_case"] = pick
+    try:
+        main()
+    finally:
+        globals()["run_case"] = saved
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1:
+        main_only(set(sys.argv[1:]))
+    else:
+        main()

@@ -73,6 +73,9 @@ def test_reference_arm_line():
         assert k in d, k
     assert d["impl"] == "reference" and d["value"] > 0 and d["config"]["N"] == 1152
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    sp = d["cpu_baseline"]["spread"]
+    assert sp["min"] <= d["value"] <= sp["max"] and sp["steps"] == 1
+    assert "throughput mode" in d["cpu_baseline"]["sample"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
 
 

@@ -51,7 +51,8 @@ def test_fill_matches_reference_samples(golden, case):
         assert np.allclose(np.abs(M).sum(1), rec[key + "_rowabs"], rtol=1e-11, atol=0)
 
 
-@pytest.mark.parametrize("case", ["cube4_gap100nm", "ico1_gap20nm", "cube2_alumina_gap50nm"])
+@pytest.mark.parametrize("case", ["cube4_gap100nm", "ico1_gap20nm", "cube2_alumina_gap50nm", "ico2_gap50nm",
+                                  "ico3_gap20nm"])
 def test_fill_matches_oracle_entrywise(golden, case):
     rec = golden(case)
     b1, b2, top, s, t = _trees(rec)

@@ -19,7 +19,8 @@ def _system(rec):
     return b1, b2, api.parseShapes(b1, b2, d1, d2)
 
 
-@pytest.mark.parametrize("case", ["cube1_gap100nm", "cube4_gap100nm", "ico1_gap20nm", "cube2_alumina_gap50nm"])
+@pytest.mark.parametrize("case", ["cube1_gap100nm", "cube4_gap100nm", "ico1_gap20nm", "cube2_alumina_gap50nm",
+                                  "ico2_gap50nm", "ico3_gap20nm"])
 def test_spectral_power_matches_reference(golden, case):
     rec = golden(case)
     _, _, (top, s, t) = _system(rec)

@@ -82,6 +82,21 @@ def test_mixed_matches_reference_cube_workload(golden):
         assert abs(P / Pref - 1) < TOL_P, (f, P, Pref)
 
 
+@pytest.mark.parametrize("case", ["ico2_gap50nm", "ico3_gap20nm"])
+def test_mixed_matches_reference_icospheres(golden, case):
+    """The mixed path against the reference binary's own spectral power on
+    the precision-form icospheres (L3, N = 7680, 20 nm) and on L2."""
+    rec = golden(case)
+    b1, b2 = golden_geometry(rec)
+    d = api.FixedLorentz(*[float(x) for x in rec["lorentz1"]])
+    top, s, t = api.parseShapes(b1, b2, d, d)
+    for f, Pref in zip(rec["freqs"], rec["P"]):
+        info = {}
+        P = api.CalcHeatTransfer(rec["a"], float(f), rec["T1"], rec["T2"], top, s, t, precision=_lib.PREC_MIXED_LA,
+                                 info=info)
+        assert abs(P / Pref - 1) < TOL_P, (case, f, P, Pref, info["err_est"], info["solver"])
+
+
 def test_mixed_same_result_twice():
     top, s, t = _pair(1, 0.1)
     a = api.CalcHeatTransfer(1e-6, 0.11, 300.0, 0.0, top, s, t, precision=_lib.PREC_MIXED_LA)

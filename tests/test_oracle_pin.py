@@ -29,7 +29,7 @@ def test_cube1_matrices_match_reference(golden):
     assert row_scaled_err(G2, rec["G2"]) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["cube4_gap100nm", "ico1_gap20nm"])
+@pytest.mark.parametrize("case", ["cube4_gap100nm", "ico1_gap20nm", "ico2_gap50nm"])
 def test_sampled_matrices_match_reference(golden, case):
     rec = golden(case)
     Z, G1, G2 = _fills(rec, float(rec["z_eV"]))
@@ -43,7 +43,7 @@ def test_sampled_matrices_match_reference(golden, case):
 
 
 @pytest.mark.parametrize("case,stride", [("cube1_gap100nm", 1), ("cube4_gap100nm", 4), ("ico1_gap20nm", 1),
-                                         ("cube2_alumina_gap50nm", 1)])
+                                         ("cube2_alumina_gap50nm", 1), ("ico2_gap50nm", 1)])
 def test_spectral_power_matches_reference(golden, case, stride):
     rec = golden(case)
     b1, b2 = golden_geometry(rec)
