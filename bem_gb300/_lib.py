@@ -38,7 +38,7 @@ EXPORTED = [
     "bemgpu_farm_poll", "bemgpu_farm_cancel", "bemgpu_farm_last_error", "bemgpu_farm_set_budget",
     "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint", "bemgpu_ctx_solve_footprint",
     "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol", "bemgpu_ctx_set_fp64_fallback_tol",
-    "bemgpu_zgemm_exact_quantized",
+    "bemgpu_zgemm_exact_quantized", "bemgpu_tree_create_body_device", "bemgpu_tree_concat", "bemgpu_tree_rwgs",
 ]
 
 
@@ -96,6 +96,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_tree_create": (i32, [vp, dp, i32, P(vp)]),
         "bemgpu_tree_destroy": (i32, [vp]),
         "bemgpu_tree_size": (i32, [vp]),
+        "bemgpu_tree_create_body_device": (i32, [vp, i32, i32, P(vp)]),
+        "bemgpu_tree_concat": (i32, [vp, vp, P(vp)]),
+        "bemgpu_tree_rwgs": (i32, [vp, dp, i32]),
         "bemgpu_mesh_rwgs": (i32, [dp, i32, i32, dp, i32, P(i32)]),
         "bemgpu_green_init": (i32, [dp, dp, dp, i32, P(Green)]),
         "bemgpu_options_default": (None, [P(Options)]),

@@ -197,6 +197,19 @@ class RWGTree:
         _check(_lib.load().bemgpu_tree_create(geom.handle, self.rwg.ctypes.data, self.rwgs, ctypes.byref(h)), geom.ctx)
         self.handle = h
 
+    @classmethod
+    def _adopt(cls, geom: Geometry, handle: ctypes.c_void_p, diel=None) -> "RWGTree":
+        """A tree the library built (device set-up); its table read back."""
+        L = _lib.load()
+        n = L.bemgpu_tree_size(handle)
+        rwg = np.empty((n, 4), dtype=np.int32)
+        L.bemgpu_tree_rwgs(handle, rwg.ctypes.data, n)
+        self = cls.__new__(cls)
+        self.geom, self.rwg, self.rwgs, self.diel = geom, rwg, n, diel
+        self.g = GreensFunction(1.0, 1.0, 0.0, False)
+        self.handle = handle
+        return self
+
     def __del__(self):
         try:
             if self.handle:
@@ -205,13 +218,30 @@ class RWGTree:
             pass
 
 
-def parseShapes(body1: Body, body2: Body, diel1, diel2, ctx: Context | None = None):
+def parseShapes(body1: Body, body2: Body, diel1, diel2, ctx: Context | None = None, setup: str = "host"):
     """Builds the two-body tree and the one-body trees over one geometry.
     ``body1`` is expected already translated by the gap vector (as
     parseShapes translates body 1, src/HeatTransfer.cpp:67-69).
-    Returns (top, s, t)."""
+    Returns (top, s, t).
+
+    setup="host": the trees take the bodies' own RWG tables.  setup="device":
+    only the vertices and triangles are uploaded; each body's RWG table (the
+    reference's edge-creation order, ShapeMesh.cpp:857-928) and half-RWG
+    frames are built by kernels (bemgpu_tree_create_body_device), and the
+    two-body tree is their concatenation (bemgpu_tree_concat)."""
     xyz, tris, rwg, ns = two_body(body1, body2)
     geom = Geometry(xyz, tris, ctx)
+    if setup == "device":
+        L = _lib.load()
+        hs, ht, htop = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _check(L.bemgpu_tree_create_body_device(geom.handle, 0, body1.nt, ctypes.byref(hs)), geom.ctx)
+        s = RWGTree._adopt(geom, hs, diel1)
+        _check(L.bemgpu_tree_create_body_device(geom.handle, body1.nt, body2.nt, ctypes.byref(ht)), geom.ctx)
+        t = RWGTree._adopt(geom, ht, diel2)
+        _check(L.bemgpu_tree_concat(hs, ht, ctypes.byref(htop)), geom.ctx)
+        return RWGTree._adopt(geom, htop), s, t
+    if setup != "host":
+        raise ValueError(f"setup must be 'host' or 'device', not {setup!r}")
     top = RWGTree(geom, rwg)
     s = RWGTree(geom, rwg[:ns], diel1)
     t = RWGTree(geom, rwg[ns:], diel2)

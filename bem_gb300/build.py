@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbemgpu.so")
 
-SOURCES = ["context.cu", "fill.cu", "dense.cu", "gemm_tc.cu", "gemm_exact.cu", "mixed.cu", "heat_transfer.cu", "farm.cu"]
+SOURCES = ["context.cu", "fill.cu", "dense.cu", "gemm_tc.cu", "gemm_exact.cu", "mixed.cu", "heat_transfer.cu", "farm.cu",
+           "mesh_device.cu"]
 HEADERS = ["bemgpu_internal.h", "quadrature_tables.h", "tc_common.cuh", "df64.cuh", "df_constants.h", os.path.join("..", "..", "include", "bemgpu.h")]
 
 NVCC_FLAGS = [

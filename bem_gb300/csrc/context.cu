@@ -501,6 +501,13 @@ int bemgpu_tree_destroy(bemgpu_tree_t t) {
 
 int bemgpu_tree_size(bemgpu_tree_t t) { return t ? t->nrwg : BEMGPU_ERR_ARG; }
 
+int bemgpu_tree_rwgs(bemgpu_tree_t t, int *rwg, int cap) {
+  if (!t || cap < 0 || (cap > 0 && !rwg)) return BEMGPU_ERR_ARG;
+  const int n = std::min(cap, t->nrwg);
+  std::copy(t->rwg.begin(), t->rwg.begin() + 4 * (size_t)n, rwg);
+  return t->nrwg;
+}
+
 // Edge creation of ShapeMesh::ShapeMesh (src/ShapeMesh.cpp:857-928): the
 // triangles are visited in order, and each edge (v0,v1), (v1,v2), (v2,v0) of
 // the current triangle whose other triangle has not been visited yet becomes

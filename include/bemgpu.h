@@ -179,6 +179,23 @@ int bemgpu_tree_size(bemgpu_tree_t t);
  * edge does not have exactly two triangles.  Host only (no context). */
 int bemgpu_mesh_rwgs(const int *tri, int nt, int nv, int *rwg, int cap, int *nrwg);
 
+/* The same RWG table built on the device, with the tree's half-RWG frames:
+ * the closed body formed by the geometry's triangles [tri0, tri0 + ntri),
+ * its RWGs in the reference's edge-creation order (ShapeMesh::ShapeMesh,
+ * src/ShapeMesh.cpp:857-928; rows as bemgpu_mesh_rwgs writes them, with
+ * geometry triangle ids) and the records of HalfRWG::HalfRWG
+ * (src/RWG.cpp:7-39), computed by kernels from the resident geometry
+ * (mesh set-up for new geometries without the host builder).  BEMGPU_ERR_MESH
+ * when the body is not a closed 2-manifold.  Synchronous. */
+int bemgpu_tree_create_body_device(bemgpu_geom_t g, int tri0, int ntri, bemgpu_tree_t *out);
+/* The two-body tree (RWGTree over both bodies, src/RWGTree.cpp:602-722 with
+ * the bodies' RWGs one after the other): a's RWGs, then b's; the trees share
+ * one geometry and no triangle.  The records are concatenated on the device. */
+int bemgpu_tree_concat(bemgpu_tree_t a, bemgpu_tree_t b, bemgpu_tree_t *out);
+/* A tree's RWG table (4 ints per RWG, as bemgpu_tree_create takes it): writes
+ * min(cap, size) rows; returns the size. */
+int bemgpu_tree_rwgs(bemgpu_tree_t t, int *rwg, int cap);
+
 /* ---- Green's function / constants ---- */
 /* GreensFunction::init(eps, mu, omega) (src/GreensFunction.cpp:17-30). */
 int bemgpu_green_init(const double eps[2], const double mu[2], const double omega[2], int external,

@@ -19,7 +19,9 @@
 //   5. writes the RWG order chosen by the reference (RWGTree + unshuffle,
 //      src/RWGTree.cpp:602-761) and, on request, the three Zts matrices of
 //      CalcHeatTransfer (src/HeatTransfer.cpp:20-29) as raw complex128;
-//   6. prints CalcHeatTransfer (src/HeatTransfer.cpp:8-59) for each frequency.
+//   6. prints CalcHeatTransfer (src/HeatTransfer.cpp:8-59) for each frequency;
+//   7. on request (--edges), writes each body's edges in the order ShapeMesh
+//      created them (src/ShapeMesh.cpp:857-928), before any partition.
 #include "HeatTransfer.h"
 #include "ShapeParser.h"
 #include "RWGTree.h"
@@ -34,14 +36,8 @@
 #include <vector>
 #include <chrono>
 
-// The reference's parseShapes (src/HeatTransfer.cpp) names these; the harness
-// never parses XML, so the definitions only satisfy the linker.
-ShapeParser::ShapeParser() { parser = NULL; }
-ShapeParser::~ShapeParser() {}
-void ShapeParser::parse(char *, Shape &, Dielectric **) {
-  fprintf(stderr, "ref_harness: XML parsing is not built into the oracle harness\n");
-  abort();
-}
+// X3D files are read by the reference's own ShapeParser (src/ShapeParser.cpp,
+// built over the small Xerces stand-in in oracle/shim/) in --x3d mode only.
 
 // Lorentz oscillator with SiC::eps's functional form (src/util/SiC.cpp:16-19),
 // parameters fixed (no temperature dependence) and given in eV.
@@ -102,9 +98,49 @@ static std::vector<double> parseList(const char *s) {
   return v;
 }
 
+// --x3d FILE --shape-out OUT: the reference's parse of one X3D file
+// (ShapeParser::parse, src/ShapeParser.cpp:83-153 with its Transform stack):
+// "nv nt", the transformed coordinates, the faces' four FaceIndex integers,
+// and the Dielectric's eps at 0.1 eV ("none" without one).
+static int dumpX3d(const char *file, const char *out) {
+  ShapeParser parser;
+  Shape shape;
+  Dielectric *diel = NULL;
+  parser.parse((char *)file, shape, &diel);
+  FILE *f = fopen(out, "w");
+  if (!f) { perror(out); return 2; }
+  fprintf(f, "%d %d\n", (int)shape.coord.size(), (int)shape.faceIndex.size());
+  for (size_t i = 0; i < shape.coord.size(); i++)
+    fprintf(f, "%.17g %.17g %.17g\n", shape.coord[i].x, shape.coord[i].y, shape.coord[i].z);
+  for (size_t i = 0; i < shape.faceIndex.size(); i++)
+    fprintf(f, "%d %d %d %d\n", shape.faceIndex[i].i[0], shape.faceIndex[i].i[1], shape.faceIndex[i].i[2],
+            shape.faceIndex[i].i[3]);
+  // ShapeParserHandler leaves its dielectric pointer unset when the file has
+  // no Dielectric element, so it is read only when the file names one
+  bool named = false;
+  if (FILE *x = fopen(file, "rb")) {
+    std::string doc;
+    char buf[65536];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof buf, x)) > 0) doc.append(buf, n);
+    fclose(x);
+    named = doc.find("<Dielectric") != std::string::npos;
+  }
+  if (named && diel) {
+    Complex e = diel->eps(0.1);
+    fprintf(f, "eps %.17g %.17g\n", real(e), imag(e));
+  } else {
+    fprintf(f, "none\n");
+  }
+  fclose(f);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   initReferenceCountingPointerLock();
-  const char *mesh1 = NULL, *mesh2 = NULL, *orderOut = NULL, *zPrefix = NULL;
+  if (argc == 5 && std::string(argv[1]) == "--x3d" && std::string(argv[3]) == "--shape-out")
+    return dumpX3d(argv[2], argv[4]);
+  const char *mesh1 = NULL, *mesh2 = NULL, *orderOut = NULL, *zPrefix = NULL, *edgesOut = NULL;
   Vector3 gap(0., 0., 0.);
   Real a = 1e-6, T1 = 300., T2 = 0.;
   std::vector<double> l1, l2, freqs;
@@ -122,12 +158,14 @@ int main(int argc, char **argv) {
     else if (k == "--freqs") freqs = parseList(argv[++i]);
     else if (k == "--order") orderOut = argv[++i];
     else if (k == "--dumpz") zPrefix = argv[++i];
+    else if (k == "--edges") edgesOut = argv[++i];
     else if (k == "--time") timing = true;
     else { fprintf(stderr, "unknown argument %s\n", argv[i]); return 2; }
   }
   if (!mesh1 || !mesh2 || l1.size() != 4 || l2.size() != 4) {
     fprintf(stderr, "usage: ref_harness --mesh1 f --mesh2 f --gap x,y,z --a m --T1 K --T2 K "
-                    "--lorentz1 einf,wTO,wLO,gamma --lorentz2 ... --freqs f1,f2 [--order out] [--dumpz prefix] [--time]\n");
+                    "--lorentz1 einf,wTO,wLO,gamma --lorentz2 ... --freqs f1,f2 [--order out] [--dumpz prefix] [--edges out] "
+                    "[--time]\n");
     return 2;
   }
 
@@ -155,6 +193,23 @@ int main(int argc, char **argv) {
   RWGTree *top = new RWGTree(meshDiel, *eap, options.minSegmentSize, 0.0);
   RWGTree *s = top->sub[0];
   RWGTree *t = top->sub[1];
+
+  if (edgesOut) {
+    // One line per edge of each body's first mesh level, in creation order:
+    // body, first triangle (t1, positive), second triangle (t2), p1, p2
+    // (ids local to the body's mesh file).
+    FILE *f = fopen(edgesOut, "w");
+    ShapeMesh *mb[2] = {m1, m2};
+    for (int b = 0; b < 2; b++) {
+      Array<Edge> &E = *mb[b]->refinedEdge[0];
+      Point *P0 = mb[b]->refinedPoint[0]->p;
+      Triangle *T0 = mb[b]->refinedTriangle[0]->p;
+      for (int i = 0; i < E.n; i++)
+        fprintf(f, "%d %ld %ld %ld %ld\n", b, (long)(E[i].t1 - T0), (long)(E[i].t2 - T0), (long)(E[i].p1 - P0),
+                (long)(E[i].p2 - P0));
+    }
+    fclose(f);
+  }
 
   if (orderOut) {
     // One line per RWG in top->rwg order: body, edge p1, edge p2, pos tri, neg tri

@@ -1,8 +1,2 @@
-// Minimal declaration standing in for Xerces-C's SAXParser (see HandlerBase.hpp).
-#ifndef ORACLE_SHIM_SAXPARSER_HPP
-#define ORACLE_SHIM_SAXPARSER_HPP
-class SAXParser {
- public:
-  enum ValSchemes { Val_Never, Val_Always, Val_Auto };
-};
-#endif
+// Stand-in for Xerces-C's xercesc/parsers/SAXParser.hpp: see oracle/shim/xercesc/shim_core.hpp.
+#include "../shim_core.hpp"

@@ -70,3 +70,39 @@ def test_non_manifold_rejected():
     v, t = mesh.cube(1.0, 1)
     with pytest.raises(ValueError):
         mesh.build_rwgs(t[:-1])
+
+
+def _reference_edges(v1, t1, v2, t2):
+    """Each body's edges in the order the reference's ShapeMesh created them
+    (src/ShapeMesh.cpp:857-928), from the reference's own code via the oracle
+    harness: rows (first triangle, second triangle, p1, p2), local ids."""
+    import os
+    import subprocess
+    import tempfile
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    harness = os.path.join(root, "oracle", "_ref", "ref_harness")
+    if not os.path.exists(harness):
+        pytest.skip("the reference harness is built only where the reference checkout is present")
+    with tempfile.TemporaryDirectory() as td:
+        m1, m2, out = (os.path.join(td, x) for x in ("m1.txt", "m2.txt", "edges.txt"))
+        mesh.write_mesh_txt(m1, v1, t1)
+        mesh.write_mesh_txt(m2, v2, t2)
+        subprocess.run([harness, "--mesh1", m1, "--mesh2", m2, "--gap", "5,0,0", "--lorentz1", "6.7,0.0983,0.12,0.00059",
+                        "--lorentz2", "6.7,0.0983,0.12,0.00059", "--edges", out], check=True, capture_output=True)
+        e = np.loadtxt(out, dtype=np.int64).reshape(-1, 5)
+    return [e[e[:, 0] == b][:, 1:] for b in (0, 1)]
+
+
+@pytest.mark.parametrize("make", [lambda: mesh.cube(1.0, 4), lambda: mesh.icosphere(1.0, 2, jitter=0.02, seed=12345),
+                                  lambda: mesh.box(0.5, 10.0, 10.0, 2, 12, 12),
+                                  lambda: mesh.cone_tip(0.5, 1.0, 0.1, n_around=14, n_side=6, n_cap=3, n_base=3)])
+def test_rwg_tables_follow_the_reference_edge_creation_order(make):
+    """bemgpu_mesh_rwgs (the C-ABI host builder) and mesh.build_rwgs give each
+    body's RWGs in exactly the reference's ShapeMesh edge order: same rows,
+    same positive / negative triangles, same edge vertex order."""
+    v, t = make()
+    v2, t2 = mesh.icosphere(1.0, 1)
+    ref, _ = _reference_edges(v, t, v2, t2)
+    native = mesh.build_rwgs_native(t, v.shape[0])
+    assert np.array_equal(native, ref)
+    assert np.array_equal(mesh.build_rwgs(t), ref)
