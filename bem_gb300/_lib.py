@@ -18,6 +18,7 @@ ERR_CANCELLED = -8
 PENDING = 1
 K_NAMES = ["fill_far", "fill_near", "gather", "lu_panel", "lu_gemm", "trsm", "solve_gemm", "trace", "refine_gemm",
            "near_spmm", "slice"]
+TUNE_NEAR_MINB, TUNE_FAR_ROWS, TUNE_RASTER = 0, 1, 2
 PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_LA = 2
@@ -39,6 +40,7 @@ EXPORTED = [
     "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint", "bemgpu_ctx_solve_footprint",
     "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol", "bemgpu_ctx_set_fp64_fallback_tol",
     "bemgpu_zgemm_exact_quantized", "bemgpu_tree_create_body_device", "bemgpu_tree_concat", "bemgpu_tree_rwgs",
+    "bemgpu_ctx_set_tuning", "bemgpu_ctx_get_tuning",
 ]
 
 
@@ -127,6 +129,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_solve_footprint": (i64, [i32, i32, i32]),
         "bemgpu_ctx_solve_footprint": (i64, [vp, i32, i32, i32]),
         "bemgpu_ctx_set_solver": (i32, [vp, i32]),
+        "bemgpu_ctx_set_tuning": (i32, [vp, i32, i32]),
+        "bemgpu_ctx_get_tuning": (i32, [vp, i32, P(i32)]),
         "bemgpu_ctx_wait_selftest": (i32, [vp, i64]),
         "bemgpu_ctx_set_escalation_tol": (i32, [vp, ctypes.c_double]),
         "bemgpu_ctx_set_fp64_fallback_tol": (i32, [vp, ctypes.c_double]),

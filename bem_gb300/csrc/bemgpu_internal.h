@@ -101,6 +101,13 @@ struct bemgpu_ctx_s {
   int gemm_engine = 0;   // complex64 LU/solve GEMMs: 0 tensor cores where possible, 2 FMA pipes only
   int acc_engine = 0;    // residual/trace GEMMs with FP64 output: same choices
   int solver = 0;        // mixed path: 0 complex64 with FP64-class escalation, 1 complex64, 2 FP64-class
+  // launch shapes chosen by the autotuner (bemgpu_ctx_set_tuning); the
+  // defaults are the measured best on the N = 7680 icosphere workload
+  struct Tuning {
+    int near_minb = 3;   // CTAs per SM of the near-pair moment kernel's register budget (2, 3, 4)
+    int far_rows = 4;    // warps per CTA of the far-pair kernel (1, 2, 4, 8)
+    int raster = 8;      // M-tiles per rasterization band of the tensor-core products (1..64)
+  } tune;
   double escalate_tol = 1e-6;  // complex64 refinement error estimate above which the solve escalates
   double fallback_tol = 1e-6;  // FP64-class error estimate above which mode 0 re-solves on the FP64 path
   // live kernel statistics

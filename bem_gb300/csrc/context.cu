@@ -499,6 +499,38 @@ int bemgpu_tree_destroy(bemgpu_tree_t t) {
   return BEMGPU_OK;
 }
 
+int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value) {
+  if (!ctx) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  switch (knob) {
+    case BEMGPU_TUNE_NEAR_MINB:
+      if (value < 2 || value > 4) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: near_minb %d not in 2..4", value);
+      ctx->tune.near_minb = value;
+      return BEMGPU_OK;
+    case BEMGPU_TUNE_FAR_ROWS:
+      if (value != 1 && value != 2 && value != 4 && value != 8)
+        return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: far_rows %d not 1, 2, 4 or 8", value);
+      ctx->tune.far_rows = value;
+      return BEMGPU_OK;
+    case BEMGPU_TUNE_RASTER:
+      if (value < 1 || value > 64) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: raster %d not in 1..64", value);
+      ctx->tune.raster = value;
+      return BEMGPU_OK;
+    default:
+      return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
+  }
+}
+
+int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value) {
+  if (!ctx || !value) return BEMGPU_ERR_ARG;
+  switch (knob) {
+    case BEMGPU_TUNE_NEAR_MINB: *value = ctx->tune.near_minb; return BEMGPU_OK;
+    case BEMGPU_TUNE_FAR_ROWS: *value = ctx->tune.far_rows; return BEMGPU_OK;
+    case BEMGPU_TUNE_RASTER: *value = ctx->tune.raster; return BEMGPU_OK;
+    default: return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
+  }
+}
+
 int bemgpu_tree_size(bemgpu_tree_t t) { return t ? t->nrwg : BEMGPU_ERR_ARG; }
 
 int bemgpu_tree_rwgs(bemgpu_tree_t t, int *rwg, int cap) {

@@ -554,7 +554,7 @@ __device__ __noinline__ void far_pair_fp32(const TriRec &T, const TriRec &S, con
 
 // mixed != 0: pairs whose centroid distance exceeds 3 edge lengths (the longer
 // of the two triangles' longest edges) are integrated in FP32.
-__global__ void __launch_bounds__(128) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
+__global__ void __launch_bounds__(256) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
                                                         const TriRec *__restrict__ Sr, int ntS, GreenDev g,
                                                         FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mode,
                                                         const TriDF *__restrict__ TDr, const TriDF *__restrict__ SDr) {
@@ -677,6 +677,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 constexpr int NEAR_WARPS = 4;
+constexpr int NEAR_MOM_FLOATS = 32;          // one outer node's smooth inner moments (InnerMomDF)
+constexpr int64_t NEAR_MOM_CHUNK = 8192;     // near pairs per moments launch: 8192 x 105 x 128 B = 110 MB
 
 // Moments of the smooth inner rule at one outer node (complex df):
 // I0 = sum w g~, A = sum w g~ l, Q0 = sum w q~, Q1 = sum w q~ l.
@@ -1076,6 +1078,134 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_df_kernel(
   }
 }
 
+// The same near pairs in two kernels, so that the inner rule (nine tenths of
+// the arithmetic) runs with the registers it needs rather than those of the
+// closed forms and contraction: near_moments_df_kernel writes the smooth inner
+// moments of every (pair, outer node) of a chunk of pairs to a scratch array
+// (structure of arrays, NEAR_MOM_FLOATS planes), near_outer_df_kernel reads
+// them back and finishes the pairs exactly as near_pairs_df_kernel does.  The
+// arithmetic and its order are unchanged, so the matrices are bit-identical.
+static_assert(sizeof(InnerMomDF) == NEAR_MOM_FLOATS * sizeof(float), "moment layout");
+
+__device__ __forceinline__ void mom_store(float *mom, int64_t stride, int64_t j, const InnerMomDF &m) {
+  const float *f = reinterpret_cast<const float *>(&m);
+#pragma unroll
+  for (int c = 0; c < NEAR_MOM_FLOATS; c++) mom[c * stride + j] = f[c];
+}
+
+__device__ __forceinline__ void mom_load(const float *__restrict__ mom, int64_t stride, int64_t j, InnerMomDF &m) {
+  float *f = reinterpret_cast<float *>(&m);
+#pragma unroll
+  for (int c = 0; c < NEAR_MOM_FLOATS; c++) f[c] = __ldcs(mom + c * stride + j);
+}
+
+// Pairs [0, npairs) of `list` (a chunk), two per warp as near_pairs_df_kernel
+// takes them; the moments of pair p, outer node q go to index p * 105 + q of
+// each plane (stride = npairs * 105).  MINB: CTAs per SM the register
+// allocation must allow (2: 224 registers, no spills; 3: 168; 4: 128, with
+// some spilled to local memory); the context's tuning picks one.
+template <int MINB>
+__global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_moments_df_kernel(
+    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
+    GreenDev g, float *__restrict__ mom) {
+  __shared__ __align__(16) float s_nodes[NEAR_WARPS][2][BEMGPU_TRI_RULE91_N][8];
+  __shared__ float s_outer[BEMGPU_TRI_RULE105_N][6];
+  __shared__ df3 s_frame[NEAR_WARPS][2][3];  // the test triangle's v01, v02 and P_s - P_t
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  const int64_t stride = npairs * BEMGPU_TRI_RULE105_N;
+  for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
+    for (int c = 0; c < 3; c++) {
+      const df v = df_make(c_rule105[u][c]);
+      s_outer[u][2 * c] = v.hi;
+      s_outer[u][2 * c + 1] = v.lo;
+    }
+  __syncthreads();
+  const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
+  for (int64_t p0 = 2 * ((int64_t)blockIdx.x * NEAR_WARPS + wid); p0 < npairs; p0 += 2 * nw) {
+    const int np2 = p0 + 1 < npairs ? 2 : 1;
+    NearPair npr[2];
+    npr[0] = list[p0];
+    npr[1] = list[np2 == 2 ? p0 + 1 : p0];
+    for (int it = lane; it < np2 * BEMGPU_TRI_RULE91_N; it += 32) {
+      const int k = it >= BEMGPU_TRI_RULE91_N ? 1 : 0, u = it - k * BEMGPU_TRI_RULE91_N;
+      const TriRec &S = Sr[npr[k].s];
+      const d3 l = c_rule91[u][0] * ld3(S.v01) + c_rule91[u][1] * ld3(S.v02);
+      const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const df v = df_make(vals[c]);
+        s_nodes[wid][k][u][2 * c] = v.hi;
+        s_nodes[wid][k][u][2 * c + 1] = v.lo;
+      }
+    }
+    if (lane < np2) {
+      const TriRec &T = Tr[npr[lane].t], &S = Sr[npr[lane].s];
+      s_frame[wid][lane][0] = df3_make(ld3(T.v01));
+      s_frame[wid][lane][1] = df3_make(ld3(T.v02));
+      s_frame[wid][lane][2] = df3_make(ld3(S.p0) - ld3(T.p0));
+    }
+    __syncwarp();
+    for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
+      const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
+      const float *o = s_outer[q];
+      const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]};
+      const df3 rt1 = df3_add(df3_scale(xi1, s_frame[wid][k][0]), df3_scale(xi2, s_frame[wid][k][1]));
+      const df3 rs = df3_sub(rt1, s_frame[wid][k][2]);
+      InnerMomDF m;
+      near_inner_df<1>(s_nodes[wid][k], &rs, g, &m);
+      mom_store(mom, stride, (p0 + k) * BEMGPU_TRI_RULE105_N + q, m);
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_outer_df_kernel(
+    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
+    GreenDev g, const float *__restrict__ mom, HalfPairBlock *__restrict__ H, int ntr) {
+  __shared__ float s_outer[BEMGPU_TRI_RULE105_N][6];
+  __shared__ NearPairDF s_pc[NEAR_WARPS][2];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  const int64_t stride = npairs * BEMGPU_TRI_RULE105_N;
+  for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
+    for (int c = 0; c < 3; c++) {
+      const df v = df_make(c_rule105[u][c]);
+      s_outer[u][2 * c] = v.hi;
+      s_outer[u][2 * c + 1] = v.lo;
+    }
+  __syncthreads();
+  const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
+  for (int64_t p0 = 2 * ((int64_t)blockIdx.x * NEAR_WARPS + wid); p0 < npairs; p0 += 2 * nw) {
+    const int np2 = p0 + 1 < npairs ? 2 : 1;
+    NearPair npr[2];
+    npr[0] = list[p0];
+    npr[1] = list[np2 == 2 ? p0 + 1 : p0];
+    if (lane < np2) near_pair_df_setup(Tr[npr[lane].t], Sr[npr[lane].s], g, s_pc[wid][lane]);
+    __syncwarp();
+    NearAccDF acc[2];
+    const df z = {0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      acc[0].L[k] = {z, z}; acc[0].K[k] = {z, z};
+      acc[1].L[k] = {z, z}; acc[1].K[k] = {z, z};
+    }
+    for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
+      const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
+      const NearPairDF &pc = s_pc[wid][k];
+      const float *o = s_outer[q];
+      const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
+      const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
+      InnerMomDF m;
+      mom_load(mom, stride, (p0 + k) * BEMGPU_TRI_RULE105_N + q, m);
+      near_outer_df(m, pc, Tr[npr[k].t].nh, Sr[npr[k].s].nh, rt1, wq, acc[k]);
+    }
+    for (int k = 0; k < np2; k++)
+      near_finish_df(Tr[npr[k].t], Sr[npr[k].s], npr[k].same, s_pc[wid][k], acc[k], H, ntr);
+    __syncwarp();
+  }
+}
+
 // Near pairs in FP64 (the plain path), one pair per warp: lanes take the
 // outer nodes, each runs the 91-node smooth inner rule, the analytic singular
 // terms and the close-pair contraction; the warp sums, adds the neighbour-edge
@@ -1423,8 +1553,9 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
   GreenDev gd = to_dev(g);
   FarOpts fo = {opt->farThresh6, opt->farThresh10, opt->farThresh15, opt->farThresh21};
   const int mode = precision == BEMGPU_PREC_MIXED ? FILL_FP32_FAR : precision == BEMGPU_PREC_MIXED_LA ? FILL_DF : FILL_FP64;
-  dim3 blk(32, 4);
-  dim3 grd((s->ntri + 31) / 32, (t->ntri + 3) / 4);
+  const int fr = ctx->tune.far_rows;
+  dim3 blk(32, fr);
+  dim3 grd((s->ntri + 31) / 32, (t->ntri + fr - 1) / fr);
   double far_flops = 0, far_bytes = 0, near_flops = 0, near_bytes = 0;
   if (ctx->prof) {
     const int64_t *fc = bem_far_rule_counts(ctx, t, s, opt);
@@ -1457,11 +1588,30 @@ int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_
     int64_t blocks = (nl->n + per_block - 1) / per_block;
     int nb = (int)std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 16);
     ProfScope ps(ctx, BEMGPU_K_FILL_NEAR, stream, near_flops, near_bytes);
-    if (mode == FILL_DF)
-      near_pairs_df_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
-    else
+    if (mode == FILL_DF) {
+      // chunks of pairs: inner moments into the scratch, then the outer part
+      const int64_t chunk = std::min<int64_t>(nl->n, NEAR_MOM_CHUNK);
+      float *mom = (float *)bem_workspace(ctx, "fill_near_mom",
+                                          sizeof(float) * NEAR_MOM_FLOATS * (size_t)chunk * BEMGPU_TRI_RULE105_N);
+      if (!mom) return bem_fail(ctx, BEMGPU_ERR_OOM, "fill: near-pair moment scratch");
+      for (int64_t c0 = 0; c0 < nl->n; c0 += chunk) {
+        const int64_t nc = std::min<int64_t>(chunk, nl->n - c0);
+        const int nbc = (int)std::min<int64_t>((nc + per_block - 1) / per_block, (int64_t)ctx->num_sms * 16);
+        const NearPair *lc = nl->d + c0;
+        if (ctx->tune.near_minb == 4)
+          near_moments_df_kernel<4><<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, lc, nc, gd, mom);
+        else if (ctx->tune.near_minb == 2)
+          near_moments_df_kernel<2><<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, lc, nc, gd, mom);
+        else
+          near_moments_df_kernel<3><<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, lc, nc, gd, mom);
+        near_outer_df_kernel<<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d + c0, nc, gd, mom, H,
+                                                                   t->nrwg);
+        ctx->launches += 2;
+      }
+    } else {
       near_pairs_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
-    ctx->launches++;
+      ctx->launches++;
+    }
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   if (n_near) *n_near = nl->n;

@@ -112,7 +112,7 @@ struct ExMaps {
 template <int SA, int SB>
 __global__ void __launch_bounds__(EX_THREADS, 1)
     ex_gemm_kernel(const __grid_constant__ ExMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf, int mvalid,
-                   int nvalid, int accumulate, const int *__restrict__ shifts, int *err) {
+                   int nvalid, int accumulate, const int *__restrict__ shifts, int raster, int *err) {
   typedef ExProducts<SA, SB> PR;
   typedef ExCfg<SA, SB> CF;
   constexpr int NP = PR::count();
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int mt, nt;
-  grouped_tile(TC_RASTER_GROUP, mt, nt);
+  grouped_tile(raster, mt, nt);
   const int m0 = mt * EX_BM, n0 = nt * EX_BN;
 
   if (threadIdx.x == 0) {
@@ -565,16 +565,16 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   const int ktiles = (int)(a.kp / bk);
   if (SA == 5 && SB == 3)
     ex_gemm_kernel<5, 3><<<grid, EX_THREADS, ex_smem_bytes<5, 3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
-                                                                          accumulate, shifts, err);
+                                                                          accumulate, shifts, ctx->tune.raster, err);
   else if (SA == 5)
     ex_gemm_kernel<5, 5><<<grid, EX_THREADS, ex_smem_bytes<5, 5>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
-                                                                          accumulate, shifts, err);
+                                                                          accumulate, shifts, ctx->tune.raster, err);
   else if (SA == 4)
     ex_gemm_kernel<4, 4><<<grid, EX_THREADS, ex_smem_bytes<4, 4>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
-                                                                          accumulate, shifts, err);
+                                                                          accumulate, shifts, ctx->tune.raster, err);
   else
     ex_gemm_kernel<3, 3><<<grid, EX_THREADS, ex_smem_bytes<3, 3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
-                                                                          accumulate, shifts, err);
+                                                                          accumulate, shifts, ctx->tune.raster, err);
   ctx->launches++;
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   return BEMGPU_OK;

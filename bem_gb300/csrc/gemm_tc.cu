@@ -59,7 +59,7 @@ namespace {
 template <typename TOUT>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ TcMaps maps, int ktiles, TOUT *__restrict__ C, int64_t ldcf, int mvalid,
-                   int nvalid, int accumulate, int tri, int *err) {
+                   int nvalid, int accumulate, int tri, int raster, int *err) {
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) &
                                                           ~(uintptr_t)1023);
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accum_bar + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int mt, nt;
-  grouped_tile(TC_RASTER_GROUP, mt, nt);
+  grouped_tile(raster, mt, nt);
   const int m0 = mt * TC_BM, n0 = nt * TC_BN;
 
   if (threadIdx.x == 0) {
@@ -202,7 +202,7 @@ constexpr int TCC_THREADS = 64 + 32 * TCC_EPI_WARPS;
 // C (FP64) = hi + lo [+ C] at C[rho + ldcf c].
 __global__ void __launch_bounds__(TCC_THREADS, 1)
     tc_gemm_comp_kernel(const __grid_constant__ TcMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf,
-                        int mvalid, int nvalid, int accumulate, int *err) {
+                        int mvalid, int nvalid, int accumulate, int raster, int *err) {
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 1023) &
                                                           ~(uintptr_t)1023);
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(TCC_THREADS, 1)
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int mt, nt;
-  grouped_tile(TC_RASTER_GROUP, mt, nt);
+  grouped_tile(raster, mt, nt);
   const int m0 = mt * TC_BM, n0 = nt * TCC_BN;
 
   if (threadIdx.x == 0) {
@@ -526,13 +526,13 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
     const int kt = (int)(Kp / TC_BK);
     if (out == TC_OUT_F64_COMP)
       tc_gemm_comp_kernel<<<grid, TCC_THREADS, TCC_SMEM_BYTES, st>>>(maps, kt, (double *)C, 2 * ldc, 2 * m, n,
-                                                                    accumulate, err);
+                                                                    accumulate, ctx->tune.raster, err);
     else if (out == TC_OUT_F64)
       tc_gemm_kernel<double><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(maps, kt, (double *)C, 2 * ldc, 2 * m, n,
-                                                                      accumulate, tri, err);
+                                                                      accumulate, tri, ctx->tune.raster, err);
     else
       tc_gemm_kernel<float><<<grid, TC_THREADS, TC_SMEM_BYTES, st>>>(maps, kt, (float *)C, 2 * ldc, 2 * m, n,
-                                                                     accumulate, tri, err);
+                                                                     accumulate, tri, ctx->tune.raster, err);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());

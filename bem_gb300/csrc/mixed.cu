@@ -297,11 +297,11 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
       if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
       // as in the complex64 refinement: every slice product while the
-      // correction is above 2^-16 of the iterate, levels 0..2 below
+      // correction is above 2^-12 of the iterate, levels 0..2 below
       unsigned eb_dy = 0;
       BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_dy, opDY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
       BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      opDY.exact = (int)eb_dy - (int)eb_y > -16;
+      opDY.exact = (int)eb_dy - (int)eb_y > -12;
       rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opDY, b.R64, n, 1, st);
     }
     if (rc) return rc;
@@ -442,14 +442,14 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
       if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
-      // -W dY to 2^-40 of |W||Y|: all 12 slice products of W's 5 slices and
-      // the correction's 3 exact ones while |dY| > 2^-16 |Y| (a slowly
-      // contracting refinement); below that, the 6 products of levels 0..2
-      // (error 2^-24 of |W||dY|) are as accurate at half the cost
+      // -W dY: all 12 slice products of W's 5 slices and the correction's 3
+      // exact ones (2^-40 of |W||dY|) while |dY| > 2^-12 |Y| (a slowly
+      // contracting refinement); below that, the 6 products of levels 0..2,
+      // whose error 2^-24 |W||dY| stays under 2^-36 |W||Y|, at half the cost
       unsigned eb_dy = 0;
       BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_dy, opDY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
       BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      opDY.exact = (int)eb_dy - (int)eb_y > -16;
+      opDY.exact = (int)eb_dy - (int)eb_y > -12;
       rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opDY, b.R64, n, 1, st);
     }
     if (rc) return rc;

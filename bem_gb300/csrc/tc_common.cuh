@@ -145,7 +145,8 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
 // Grouped rasterization of a (gridDim.x M-tiles) x (gridDim.y N-tiles) grid:
 // CTAs launched consecutively (linear id, x fastest) cover a band of `group`
 // M-tiles across the N-tiles, so the band's A tiles are re-read from L2, not
-// HBM, by every N-tile passing them.
+// HBM, by every N-tile passing them.  `group` is the context's tuning
+// (BEMGPU_TUNE_RASTER, default 8).
 __device__ __forceinline__ void grouped_tile(int group, int &mt, int &nt) {
   const int nM = gridDim.x, nN = gridDim.y;
   const int L = blockIdx.y * nM + blockIdx.x;
@@ -156,7 +157,6 @@ __device__ __forceinline__ void grouped_tile(int group, int &mt, int &nt) {
   mt = first + local % gm;
   nt = local / gm;
 }
-constexpr int TC_RASTER_GROUP = 8;
 
 // hi + lo += p (Knuth's TwoSum: the rounding error of hi + p goes to lo).
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float p) {

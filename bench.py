@@ -289,6 +289,18 @@ def run_ours(args, rank, world):
         top, s, t = (sysset or systems)[gi]
         return (a, f, T1, 0.0, top, s, t)
 
+    # launch shapes from the project's autotuner (bem_gb300.tuning): cached per
+    # GPU and size class, tuned on this workload's first request when missing
+    tiles = None
+    if args.tune != "off":
+        from bem_gb300 import tuning
+        t0t = time.perf_counter()
+        params, source = tuning.tuned(lambda: api.CalcHeatTransfer(*job(0), precision=prec, strict=False),
+                                      ctx.handle, 2 * systems[order[0][0]][0].rwgs, dev,
+                                      retune=args.tune == "retune")
+        for c in lane_ctx:
+            tuning.apply(c, params)
+        tiles = dict(params, source=source, seconds=time.perf_counter() - t0t)
     farm.map([job(k) for k in range(args.warmup)], precision=prec, strict=False)
     if world > 1:
         import torch.distributed as dist
@@ -398,6 +410,7 @@ def run_ours(args, rank, world):
                           "fp64class": sum(i["solver"] == 2 for i in infos),
                           "fp64_fallback": sum(i["solver"] == 3 for i in infos)},
         "gpu_launches": int(launches),
+        "tiles": tiles,
         "clocks": clk.summary(),
         "serving": serving,
         "P_sample": Ps[:2],
@@ -758,7 +771,7 @@ SUBS = {
     "tip": ["--workload", "tip", "--steps", "64", "--warmup", "4", "--serve-requests", "0", "--lite"],
 }
 SUB_KEYS = ("value", "unit", "ms_per_step", "steps", "config", "err_est", "factorization", "serving", "stage_ms",
-            "fp64_path", "accuracy", "mixed_over_fp64", "clocks", "gpu_launches", "fill_gentries_per_s")
+            "fp64_path", "accuracy", "mixed_over_fp64", "clocks", "gpu_launches", "fill_gentries_per_s", "tiles")
 
 
 def run_subs(names):
@@ -805,6 +818,9 @@ def main():
     ap.add_argument("--subs", default="default",
                     help="comma-separated sub-workloads summarised in the line (slab, mix, tip), 'none', or "
                          "'default' (slab,mix for the default ico3 workload, none otherwise)")
+    ap.add_argument("--tune", default="cache", choices=["cache", "retune", "off"],
+                    help="launch shapes from the autotuner's cache (tuned first when missing), re-tuned, or the "
+                         "library defaults")
     ap.add_argument("--lite", action="store_true",
                     help="skip the end-to-end and per-kernel segments (sub-workload runs)")
     args = ap.parse_args()

@@ -126,6 +126,21 @@ int bemgpu_ctx_set_escalation_tol(bemgpu_ctx_t ctx, double tol);
  * residual is exact to ~2^-40, so for W conditioned worse than ~1e6 its
  * estimate stalls above the bound while the FP64 LU still meets it. */
 int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
+/* Launch-shape knobs of this context (no reference counterpart), set by the
+ * project's autotuner (bem_gb300/tuning.py: it times each candidate on the
+ * caller's workload and caches the best per GPU and size class).
+ *   BEMGPU_TUNE_NEAR_MINB  CTAs per SM that the near-pair inner-moment kernel's
+ *                          register budget allows: 2 (224 registers), 3 (168,
+ *                          default) or 4 (128, some spilled);
+ *   BEMGPU_TUNE_FAR_ROWS   warps per CTA of the far-pair kernel: 1, 2, 4 (default), 8;
+ *   BEMGPU_TUNE_RASTER     M-tiles per rasterization band of the tensor-core
+ *                          products: 1..64 (default 8).
+ * BEMGPU_ERR_ARG for an unknown knob or value.  Results do not depend on them. */
+#define BEMGPU_TUNE_NEAR_MINB 0
+#define BEMGPU_TUNE_FAR_ROWS 1
+#define BEMGPU_TUNE_RASTER 2
+int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value);
+int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value);
 /* Tracing: with BEMGPU_TRACE set (not "0") in the environment, the library
  * prints one line per refinement step and escalation decision to stderr. */
 /* Failure-path self-test: one kernel polls a flag that nothing sets, gives up

@@ -1,0 +1,54 @@
+"""The autotuner's cache and size classes (CPU), and on the GPU: the launch
+shapes it chooses between leave every result bit for bit unchanged, and a
+tuning run returns valid settings and caches them."""
+import json
+
+import pytest
+
+from bem_gb300 import tuning
+
+
+def test_size_classes_and_cache_roundtrip(tmp_path):
+    assert tuning.size_class(1152) == "n2048" and tuning.size_class(7680) == "n8192"
+    assert tuning.size_class(8192) == "n8192" and tuning.size_class(8193) == "n16384"
+    path = str(tmp_path / "t.json")
+    tuning.store("GB300|n8192", {"near_minb": 4, "far_rows": 2, "raster": 16}, path)
+    tuning.store("GB300|n2048", {"near_minb": 2, "far_rows": 8, "raster": 4}, path)
+    data = json.load(open(path))
+    assert data["GB300|n8192"]["raster"] == 16 and data["GB300|n2048"]["far_rows"] == 8
+    assert tuning.load_cache(str(tmp_path / "missing.json")) == {}
+    assert set(tuning.DEFAULTS) == set(tuning.KNOBS)
+
+
+@pytest.mark.gpu
+def test_results_do_not_depend_on_the_launch_shapes(tmp_path):
+    from bem_gb300 import api, mesh, _lib
+    v, t = mesh.icosphere(1.0, 2, jitter=0.02, seed=12345)
+    b2 = mesh.Body.from_mesh(v, t)
+    b1 = b2.translated(mesh.gap_translation(v, v, 0.05))
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    ctx = api.Context(0)
+    top, s, tt = api.parseShapes(b1, b2, d, d, ctx)
+    g = api.GreensFunction(1.0, 1.0, 0.55, True)
+
+    def run():
+        return (api.CalcHeatTransfer(1e-6, 0.116, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA),
+                api.Zts(top, top, g, precision=_lib.PREC_MIXED_LA).tobytes())
+
+    base = run()
+    for name, (_, cands, _) in tuning.KNOBS.items():
+        for v in cands:
+            tuning.apply(ctx.handle, dict(tuning.DEFAULTS, **{name: v}))
+            assert run() == base, (name, v)
+    params, timings = tuning.tune(lambda: api.CalcHeatTransfer(1e-6, 0.116, 300.0, 0.0, top, s, tt,
+                                                               precision=_lib.PREC_MIXED_LA), ctx.handle, reps=1)
+    assert all(params[k] in tuning.KNOBS[k][1] for k in tuning.KNOBS)
+    assert tuning.current(ctx.handle) == params
+    assert all(ms > 0 for ms in timings["near_minb"].values())
+    path = str(tmp_path / "cache.json")
+    tuning.store(tuning.cache_key(2 * top.rwgs), params, path)
+    p3, src = tuning.tuned(lambda: None, ctx.handle, 2 * top.rwgs, path=path)
+    assert src == "cache" and p3 == params
+    L = _lib.load()
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_NEAR_MINB, 5) == _lib.ERR_ARG
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, 99, 1) == _lib.ERR_ARG
