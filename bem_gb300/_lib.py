@@ -40,7 +40,8 @@ EXPORTED = [
     "bemgpu_farm_budget", "bemgpu_ctx_workspace_bytes", "bemgpu_ctx_trim", "bemgpu_solve_footprint", "bemgpu_ctx_solve_footprint",
     "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol", "bemgpu_ctx_set_fp64_fallback_tol",
     "bemgpu_zgemm_exact_quantized", "bemgpu_tree_create_body_device", "bemgpu_tree_concat", "bemgpu_tree_rwgs",
-    "bemgpu_ctx_set_tuning", "bemgpu_ctx_get_tuning",
+    "bemgpu_ctx_set_tuning", "bemgpu_ctx_get_tuning", "bemgpu_heat_transfer_batch", "bemgpu_batch_footprint",
+    "bemgpu_farm_set_batch",
 ]
 
 
@@ -114,9 +115,13 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_zgemm_exact": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32, i32]),
         "bemgpu_zgemm_exact_quantized": (i32, [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64, i32]),
         "bemgpu_heat_transfer": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(ctypes.c_double), P(SolveInfo)]),
+        "bemgpu_heat_transfer_batch": (i32, [vp, i32, P(vp), P(vp), P(vp), P(SolveReq), P(Options), i32,
+                                             P(ctypes.c_double), P(SolveInfo), P(i32)]),
+        "bemgpu_batch_footprint": (i64, [i32, i32, i32, i32]),
         "bemgpu_farm_create": (i32, [i32, i32, P(vp)]),
         "bemgpu_farm_destroy": (i32, [vp]),
         "bemgpu_farm_lanes": (i32, [vp]),
+        "bemgpu_farm_set_batch": (i32, [vp, i32]),
         "bemgpu_farm_lane_ctx": (i32, [vp, i32, P(vp)]),
         "bemgpu_farm_submit": (i32, [vp, vp, vp, vp, P(SolveReq), P(Options), i32, P(i64)]),
         "bemgpu_farm_poll": (i32, [vp, i64, ctypes.c_double, P(ctypes.c_double), P(SolveInfo)]),

@@ -302,6 +302,35 @@ def CalcHeatTransfer(a: float, eV: float, T1: float, T2: float, top: RWGTree, s:
     return P.value
 
 
+def CalcHeatTransferBatch(jobs, options: Options | None = None, precision: int = _lib.PREC_FP64,
+                          infos: list | None = None, strict: bool = True) -> list:
+    """CalcHeatTransfer for several (a, eV, T1, T2, top, s, t) at once
+    (bemgpu_heat_transfer_batch): one fill launch pair for all of them and,
+    for requests of equal size, one cooperative LU panel launch per block
+    column.  The results equal CalcHeatTransfer's one by one, bit for bit."""
+    options = options or Options()
+    jobs = list(jobs)
+    n = len(jobs)
+    if n == 0:
+        return []
+    ctx = jobs[0][4].geom.ctx
+    reqs = (_lib.SolveReq * n)(*[_solve_req(a, eV, T1, T2, s, t) for (a, eV, T1, T2, top, s, t) in jobs])
+    vp = ctypes.c_void_p * n
+    tops, ss, ts = vp(*[j[4].handle for j in jobs]), vp(*[j[5].handle for j in jobs]), vp(*[j[6].handle for j in jobs])
+    P = (ctypes.c_double * n)()
+    si = (_lib.SolveInfo * n)()
+    st = (ctypes.c_int * n)()
+    _lib.load().bemgpu_heat_transfer_batch(ctx.handle, n, tops, ss, ts, reqs, ctypes.byref(options._c()),
+                                           int(precision), P, si, st)
+    for i in range(n):
+        if not (st[i] == _lib.ERR_NO_CONVERGE and not strict) and st[i] != _lib.OK:
+            _check(st[i], ctx)
+    if infos is not None:
+        for i in range(n):
+            infos.append({k: getattr(si[i], k) for k, _ in _lib.SolveInfo._fields_})
+    return list(P)
+
+
 class FrequencySweep:
     """FrequencySweep(file): one frequency (eV) per line (src/FrequencySweep.cpp:4-16)."""
 
@@ -344,7 +373,7 @@ class Farm:
     CalcHeatTransfer's error behaviour.  The farm keeps the trees of every
     uncollected request alive."""
 
-    def __init__(self, lanes: int = 2, device: int = 0):
+    def __init__(self, lanes: int = 2, device: int = 0, batch: int = 1):
         L = _lib.load()
         h = ctypes.c_void_p()
         rc = L.bemgpu_farm_create(int(device), int(lanes), ctypes.byref(h))
@@ -354,6 +383,15 @@ class Farm:
         self.lanes = lanes
         self.device = device
         self._held = {}
+        self.set_batch(batch)
+
+    def set_batch(self, max_requests: int):
+        """Continuous batching: each lane solves up to ``max_requests`` queued
+        requests of equal sizes together (bemgpu_farm_set_batch)."""
+        rc = _lib.load().bemgpu_farm_set_batch(self.handle, int(max_requests))
+        if rc != _lib.OK:
+            raise _lib.BemGpuError(rc, f"batch size {max_requests} not in 1..64")
+        self.batch = max_requests
 
     def _err(self) -> str:
         return _lib.load().bemgpu_farm_last_error(self.handle).decode()

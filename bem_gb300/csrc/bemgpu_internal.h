@@ -20,6 +20,8 @@
 // tables loaded, the allocation-free fill's scratch address) lives in arrays
 // of this size, and bemgpu_ctx_create rejects a higher device index.
 #define BEM_MAX_DEVICES 64
+// Requests of one bemgpu_heat_transfer_batch call at most.
+#define BEM_MAX_BATCH 64
 
 // Device-resident per-triangle record of one RWG tree (FP64).  The frame
 // (p0, p1, p2 and derived vectors) is that of the triangle's first half-RWG in
@@ -104,7 +106,7 @@ struct bemgpu_ctx_s {
   // launch shapes chosen by the autotuner (bemgpu_ctx_set_tuning); the
   // defaults are the measured best on the N = 7680 icosphere workload
   struct Tuning {
-    int near_minb = 3;   // CTAs per SM of the near-pair moment kernel's register budget (2, 3, 4)
+    int near_minb = 2;   // CTAs per SM of the double-float near-pair kernel's register budget (2, 3, 4)
     int far_rows = 4;    // warps per CTA of the far-pair kernel (1, 2, 4, 8)
     int raster = 8;      // M-tiles per rasterization band of the tensor-core products (1..64)
   } tune;
@@ -186,6 +188,18 @@ struct HalfPairBlock {
 // Computes every triangle pair of (t, s) with one Green's function and writes
 // the per-half-pair products into H (ntr x nsr blocks, index j*ntr+i).
 // precision BEMGPU_PREC_MIXED integrates pairs farther apart than 3 edge lengths in FP32.
+// One Zts fill of a group (bem_fill_group): tree pair, Green's function,
+// half-pair blocks out; near/far pair counts written back.
+struct FillJob {
+  const bemgpu_tree_s *t, *s;
+  bemgpu_green_t g;
+  HalfPairBlock *H;
+  int64_t near, far;
+};
+// Several fills in one far-pair and one near-pair launch (the three Zts of a
+// solve, or of a batch of solves).
+int bem_fill_group(bemgpu_ctx_s *ctx, FillJob *jobs, int njobs, const bemgpu_options_t *opt, int precision,
+                   cudaStream_t stream);
 int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s,
                    const bemgpu_green_t *g, const bemgpu_options_t *opt, int precision, HalfPairBlock *H,
                    cudaStream_t stream, int64_t *n_near, int64_t *n_far);
@@ -214,6 +228,10 @@ int bem_zgetrs_exact(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, con
                      int64_t ldb, int nrhs, cudaStream_t stream);
 // complex64 versions (mixed path).
 int bem_cgetrf(bemgpu_ctx_s *ctx, float *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream);
+// The same for nb matrices A + i strideA (pivots d_ipiv + i n, info d_info + i),
+// their panels factored together in one cooperative launch.
+int bem_cgetrf_batch(bemgpu_ctx_s *ctx, float *A, int64_t strideA, int nb, int64_t lda, int n, int *d_ipiv,
+                     int *d_info, cudaStream_t stream);
 int bem_cgetrs(bemgpu_ctx_s *ctx, const float *A, int64_t lda, int n, const int *d_ipiv, float *B, int64_t ldb,
                int nrhs, cudaStream_t stream);
 // L^{-1} (unit lower) and U^{-1} (upper) of a packed complex64 LU (n x n,
@@ -285,5 +303,12 @@ int bem_zgemm(bemgpu_ctx_s *ctx, int kind, char opA, int m, int n, int k, const 
 // on the plain FP64 path.
 constexpr int BEM_SOLVE_ON_FP64_PATH = 100;
 void bem_release_if_short(bemgpu_ctx_s *ctx, size_t need, std::initializer_list<const char *> names);
+// The complex64 LU of W already done (a batch's bem_cgetrf_batch): the factors
+// in place of fl32(W), the pivots and the zero-pivot info.
+struct MixedLU {
+  float *W32;
+  int *ipiv, *info;
+};
 int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
-                    cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info);
+                    cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info, const MixedLU *pre = nullptr);
+void bem_c128_to_c64(bemgpu_ctx_s *ctx, const double *W, int n, float *W32, cudaStream_t st);

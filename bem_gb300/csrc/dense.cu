@@ -318,9 +318,24 @@ template <typename T>
 __global__ void __launch_bounds__(COOP_THREADS)
     panel_coop_kernel(T *A, int64_t lda, int n, int k0, int w, int chunk, int *ipiv, int *info, T *cval,
                       int *crow, T *cdata_raw, T *drow_raw, unsigned *counter, int *err,
-                      unsigned long long *best) {
+                      unsigned long long *best, int64_t strideA) {
   typedef typename V2<T>::type T2;
   extern __shared__ __align__(16) unsigned char coop_smem[];
+  {
+    // a batch of equal-size matrices (blockIdx.y): its own matrix, pivots,
+    // candidate slots and barrier; the CTAs of different matrices never wait
+    // on one another
+    const int64_t bb = blockIdx.y;
+    A += bb * strideA;
+    ipiv += bb * n;
+    info += bb;
+    cval += bb * 2 * gridDim.x;
+    crow += bb * 2 * gridDim.x;
+    cdata_raw += bb * 2 * 2 * (int64_t)gridDim.x * w;
+    drow_raw += bb * 2 * 2 * (int64_t)w;
+    counter += bb;
+    best += 4 * bb;
+  }
   T2 *P = reinterpret_cast<T2 *>(coop_smem);  // chunk x w, P[i * w + c]
   T2 *prow = P + (int64_t)chunk * w;           // the pivot (U) row of the current column
   T2 *A2 = reinterpret_cast<T2 *>(A);
@@ -859,7 +874,7 @@ constexpr int COOP_MAX_SMEM = 226 * 1024;  // below the 227 KB per-CTA limit, wi
 // (nothing launched) when the panel does not fit the cooperative kernel.
 template <typename T>
 bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int *d_ipiv, int *d_info,
-                cudaStream_t stream, int &rc) {
+                cudaStream_t stream, int &rc, int nb = 1, int64_t strideA = 0) {
   typedef typename V2<T>::type T2;
   rc = BEMGPU_OK;
   const int rows = n - k0;
@@ -880,16 +895,20 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, panel_coop_kernel<T>, COOP_THREADS, smem) !=
           cudaSuccess ||
-      per_sm * ctx->num_sms < G) {
+      per_sm * ctx->num_sms < G * nb) {
     cudaGetLastError();
     return false;
   }
-  T *cval = (T *)bem_workspace(ctx, "coop_cval", sizeof(T) * 2 * 1024);
-  int *crow = (int *)bem_workspace(ctx, "coop_crow", sizeof(int) * 2 * 1024);
-  T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * 1024 * (size_t)NB_MAX);
-  T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)NB_MAX);
-  unsigned *counter = (unsigned *)bem_workspace(ctx, "coop_counter", sizeof(unsigned));
-  unsigned long long *best = (unsigned long long *)bem_workspace(ctx, "coop_best", 4 * sizeof(unsigned long long));
+  // candidate slots and barriers per matrix of the batch (the kernel offsets
+  // them by blockIdx.y: 2 G values, rows and rows of w entries, 2 w for the
+  // diagonal row, one counter, four pivot keys)
+  T *cval = (T *)bem_workspace(ctx, "coop_cval", sizeof(T) * 2 * (size_t)G * nb);
+  int *crow = (int *)bem_workspace(ctx, "coop_crow", sizeof(int) * 2 * (size_t)G * nb);
+  T *cdata = (T *)bem_workspace(ctx, "coop_cdata", sizeof(T2) * 2 * (size_t)G * w * nb);
+  T *drow = (T *)bem_workspace(ctx, "coop_drow", sizeof(T2) * 2 * (size_t)w * nb);
+  unsigned *counter = (unsigned *)bem_workspace(ctx, "coop_counter", sizeof(unsigned) * (size_t)nb);
+  unsigned long long *best =
+      (unsigned long long *)bem_workspace(ctx, "coop_best", 4 * sizeof(unsigned long long) * (size_t)nb);
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
   if (!cval || !crow || !cdata || !drow || !counter || !best || !err || G > 1024 || w > NB_MAX) {
     rc = bem_fail(ctx, BEMGPU_ERR_OOM, "getrf: panel workspace");
@@ -899,15 +918,15 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
     cudaMemsetAsync(err, 0, sizeof(int), stream);
     ctx->tc_err_ready = true;
   }
-  cudaMemsetAsync(counter, 0, sizeof(unsigned), stream);
-  cudaMemsetAsync(best, 0, 4 * sizeof(unsigned long long), stream);
+  cudaMemsetAsync(counter, 0, sizeof(unsigned) * (size_t)nb, stream);
+  cudaMemsetAsync(best, 0, 4 * sizeof(unsigned long long) * (size_t)nb, stream);
   int n_ = n, k0_ = k0, w_ = w, chunk_ = chunk;
   void *args[] = {&A,    &lda,  &n_,    &k0_,  &w_,      &chunk_, &d_ipiv, &d_info,
-                  &cval, &crow, &cdata, &drow, &counter, &err,    &best};
+                  &cval, &crow, &cdata, &drow, &counter, &err,    &best,   &strideA};
   const double cb = 2.0 * sizeof(T);
-  ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 4.0 * (double)rows * w * w, cb * 2.0 * rows * w);
-  const cudaError_t e = cudaLaunchCooperativeKernel((const void *)panel_coop_kernel<T>, dim3(G), dim3(COOP_THREADS),
-                                                    args, smem, stream);
+  ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 4.0 * (double)rows * w * w * nb, cb * 2.0 * rows * w * nb);
+  const cudaError_t e = cudaLaunchCooperativeKernel((const void *)panel_coop_kernel<T>, dim3(G, nb),
+                                                    dim3(COOP_THREADS), args, smem, stream);
   ctx->launches++;
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -916,14 +935,20 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
   return true;
 }
 
+// LU with partial pivoting of nb equal-size matrices A + i strideA (pivots
+// d_ipiv + i n, info d_info + i): every panel of the batch in one cooperative
+// launch (each matrix with its own CTAs and barrier), the interchanges,
+// triangular blocks and trailing updates per matrix.  Each matrix gets the
+// arithmetic of a batch of one.
 template <typename T>
-int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {
+int getrf_impl(bemgpu_ctx_s *ctx, T *A0, int64_t lda, int n, int *d_ipiv0, int *d_info0, cudaStream_t stream,
+               int nb = 1, int64_t strideA = 0) {
   if (int rc0 = set_trsm_attrs<T>(ctx)) return rc0;
   PivCand *cand = (PivCand *)bem_workspace(ctx, "lu_cand", sizeof(PivCand) * 1024);
   unsigned int *counter = (unsigned int *)bem_workspace(ctx, "lu_counter", sizeof(unsigned int));
   if (!cand || !counter) return bem_fail(ctx, BEMGPU_ERR_OOM, "getrf: workspace");
   BEM_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream));
-  BEM_CUDA_TRY(ctx, cudaMemsetAsync(d_info, 0, sizeof(int), stream));
+  BEM_CUDA_TRY(ctx, cudaMemsetAsync(d_info0, 0, sizeof(int) * (size_t)nb, stream));
   const T mone[2] = {T(-1), T(0)}, one[2] = {T(1), T(0)};
   const double cb = 2.0 * sizeof(T);  // bytes per complex element
   constexpr int NBL = LuCfg<T>::NBL;
@@ -932,47 +957,63 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int *d_ipiv, int *d_
     const int rows = n - k0;
     const int blocks = std::max(1, std::min(ctx->num_sms * 2, (rows + PANEL_THREADS - 1) / PANEL_THREADS));
     int prc = BEMGPU_OK;
-    const bool coop = ctx->coop_panel && panel_coop<T>(ctx, A, lda, n, k0, w, d_ipiv, d_info, stream, prc);
+    bool coop = ctx->coop_panel && panel_coop<T>(ctx, A0, lda, n, k0, w, d_ipiv0, d_info0, stream, prc, nb, strideA);
     if (prc) return prc;
-    for (int jj = 0; !coop && jj <= w; jj++) {
-      ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 8.0 * (rows - jj) * (w - jj), cb * 2 * (rows - jj) * (w - jj));
-      panel_step_kernel<T><<<blocks, PANEL_THREADS, 0, stream>>>(A, lda, n, k0, w, jj, d_ipiv, d_info, cand, counter);
-      ctx->launches++;
+    if (!coop && nb > 1 && ctx->coop_panel) {
+      // the batch's panels do not fit at once: one cooperative panel per matrix
+      coop = true;
+      for (int i = 0; i < nb && coop; i++) {
+        coop = panel_coop<T>(ctx, A0 + i * strideA, lda, n, k0, w, d_ipiv0 + (int64_t)i * n, d_info0 + i, stream,
+                             prc);
+        if (prc) return prc;
+      }
+      if (!coop && nb > 1) return bem_fail(ctx, BEMGPU_ERR_ARG, "getrf: batched panel does not fit");
     }
-    BEM_CUDA_TRY(ctx, cudaGetLastError());
-    // interchanges to the left and right of the panel
-    static_assert(NBL <= LASWP_MAXW, "panel wider than the interchange kernel's permutation");
-    if (k0 > 0) {
-      ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * k0);
-      const int g = std::min((k0 + LASWP_WARPS - 1) / LASWP_WARPS, 2 * ctx->num_sms);
-      laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, 0, k0, k0, k0 + w, d_ipiv);
-      ctx->launches++;
-    }
-    if (k0 + w < n) {
-      const int nr = n - k0 - w;
-      T *A11 = A + 2 * (k0 + lda * (int64_t)k0);
-      T *A12 = A + 2 * (k0 + lda * (int64_t)(k0 + w));
-      // one CTA per SM at most: each CTA stages the w x w diagonal block in
-      // shared memory once and walks its share of the columns
-      const int tb = std::min((nr + 7) / 8, NBL > 64 ? ctx->num_sms : ctx->num_sms * 4);
-      {
-        ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * nr);
-        const int g = std::min((nr + LASWP_WARPS - 1) / LASWP_WARPS, 2 * ctx->num_sms);
-        laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, k0 + w, n, k0, k0 + w, d_ipiv);
+    for (int i = 0; i < nb; i++) {
+      T *A = A0 + i * strideA;
+      int *d_ipiv = d_ipiv0 + (int64_t)i * n;
+      int *d_info = d_info0 + i;
+      for (int jj = 0; !coop && jj <= w; jj++) {
+        ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 8.0 * (rows - jj) * (w - jj), cb * 2 * (rows - jj) * (w - jj));
+        panel_step_kernel<T><<<blocks, PANEL_THREADS, 0, stream>>>(A, lda, n, k0, w, jj, d_ipiv, d_info, cand,
+                                                                   counter);
         ctx->launches++;
       }
-      {
-        ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nr, 2.0 * cb * w * nr);
-        trsm_block_kernel<T, false, NBL / 32>
-            <<<tb, 256, trsm_smem_bytes<T, NBL / 32>(), stream>>>(A11, lda, w, A12, lda, nr);
+      BEM_CUDA_TRY(ctx, cudaGetLastError());
+      // interchanges to the left and right of the panel
+      static_assert(NBL <= LASWP_MAXW, "panel wider than the interchange kernel's permutation");
+      if (k0 > 0) {
+        ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * k0);
+        const int g = std::min((k0 + LASWP_WARPS - 1) / LASWP_WARPS, 2 * ctx->num_sms);
+        laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, 0, k0, k0, k0 + w, d_ipiv);
         ctx->launches++;
       }
-      T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
-      T *A22 = A + 2 * (k0 + w + lda * (int64_t)(k0 + w));
-      int rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
-      if (rc) return rc;
+      if (k0 + w < n) {
+        const int nr = n - k0 - w;
+        T *A11 = A + 2 * (k0 + lda * (int64_t)k0);
+        T *A12 = A + 2 * (k0 + lda * (int64_t)(k0 + w));
+        // one CTA per SM at most: each CTA stages the w x w diagonal block in
+        // shared memory once and walks its share of the columns
+        const int tb = std::min((nr + 7) / 8, NBL > 64 ? ctx->num_sms : ctx->num_sms * 4);
+        {
+          ProfScope ps(ctx, BEMGPU_K_LU_PANEL, stream, 0.0, 4.0 * cb * w * nr);
+          const int g = std::min((nr + LASWP_WARPS - 1) / LASWP_WARPS, 2 * ctx->num_sms);
+          laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, k0 + w, n, k0, k0 + w, d_ipiv);
+          ctx->launches++;
+        }
+        {
+          ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nr, 2.0 * cb * w * nr);
+          trsm_block_kernel<T, false, NBL / 32>
+              <<<tb, 256, trsm_smem_bytes<T, NBL / 32>(), stream>>>(A11, lda, w, A12, lda, nr);
+          ctx->launches++;
+        }
+        T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
+        T *A22 = A + 2 * (k0 + w + lda * (int64_t)(k0 + w));
+        int rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
+        if (rc) return rc;
+      }
+      BEM_CUDA_TRY(ctx, cudaGetLastError());
     }
-    BEM_CUDA_TRY(ctx, cudaGetLastError());
   }
   return BEMGPU_OK;
 }
@@ -1223,6 +1264,12 @@ int bem_zgetrs_exact(bemgpu_ctx_s *ctx, const double *A, int64_t lda, int n, con
   }
   if (!rc) BEM_CUDA_TRY(ctx, cudaGetLastError());
   return rc;
+}
+
+int bem_cgetrf_batch(bemgpu_ctx_s *ctx, float *A, int64_t strideA, int nb, int64_t lda, int n, int *d_ipiv,
+                     int *d_info, cudaStream_t stream) {
+  if (nb < 1) return BEMGPU_OK;
+  return getrf_impl<float>(ctx, A, lda, n, d_ipiv, d_info, stream, nb, strideA);
 }
 
 int bem_cgetrf(bemgpu_ctx_s *ctx, float *A, int64_t lda, int n, int *d_ipiv, int *d_info, cudaStream_t stream) {

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstring>
 #include <condition_variable>
 #include <deque>
 #include <string>
@@ -73,6 +74,7 @@ struct bemgpu_farm_s {
   std::vector<size_t> held, reserved;  // workspace held; reserved while running
   std::deque<int64_t> waiters;         // tickets waiting for memory, in order
   std::condition_variable cv_mem;
+  int batch = 1;                       // requests a lane solves together at most
 };
 
 namespace {
@@ -127,52 +129,99 @@ bool admit(bemgpu_farm_s *f, int me, int64_t ticket, size_t need, std::unique_lo
   return true;
 }
 
+bool same_kind(const FarmJob &a, const FarmJob &b) {
+  return a.precision == b.precision && a.s->nrwg == b.s->nrwg && a.t->nrwg == b.t->nrwg &&
+         memcmp(&a.opt, &b.opt, sizeof a.opt) == 0;
+}
+
 void lane_main(bemgpu_farm_s *f, int lane) {
   bemgpu_ctx_t ctx = f->lanes[lane];
   for (;;) {
-    FarmJob job;
+    std::vector<FarmJob> jobs;
     bool ok;
     {
       std::unique_lock<std::mutex> lk(f->mu);
       f->cv_job.wait(lk, [f, lane] { return (f->stop || !f->queue.empty()) && f->state[lane] != TRIMMING; });
       if (f->queue.empty()) return;  // stopping, nothing left
-      job = f->queue.front();
+      jobs.push_back(f->queue.front());
       f->queue.pop_front();
+      // continuous batching: queued requests of the same sizes, precision and
+      // options join this one (in queue order), up to the farm's batch size
+      for (auto it = f->queue.begin(); it != f->queue.end() && (int)jobs.size() < f->batch;) {
+        if (same_kind(*it, jobs[0])) {
+          jobs.push_back(*it);
+          it = f->queue.erase(it);
+        } else {
+          ++it;
+        }
+      }
+      const FarmJob &job = jobs[0];
       f->state[lane] = WAITING;
-      const int64_t need = bemgpu_ctx_solve_footprint(ctx, job.s->nrwg, job.t->nrwg, job.precision);
+      int64_t need = jobs.size() == 1 ? bemgpu_ctx_solve_footprint(ctx, job.s->nrwg, job.t->nrwg, job.precision)
+                                      : bemgpu_batch_footprint((int)jobs.size(), job.s->nrwg, job.t->nrwg,
+                                                               job.precision);
+      if (jobs.size() > 1 && (size_t)need > f->budget) {
+        // the batch does not fit the budget: the others go back to the front
+        for (size_t k = jobs.size() - 1; k >= 1; k--) f->queue.push_front(jobs[k]);
+        jobs.resize(1);
+        need = bemgpu_ctx_solve_footprint(ctx, job.s->nrwg, job.t->nrwg, job.precision);
+      }
       ok = admit(f, lane, job.ticket, (size_t)need, lk);
       f->state[lane] = ok ? BUSY : IDLE;
-      FarmResult &r = f->results[job.ticket];
-      r.state = RUNNING;
-      r.t_start = Clock::now();
-      if (!ok) {
-        r.state = DONE;
-        r.status = BEMGPU_ERR_OOM;
-        char buf[160];
-        snprintf(buf, sizeof buf, "farm: the request needs %.2f GB, more than the farm's budget of %.2f GB",
-                 need / 1e9, f->budget / 1e9);
-        r.error = buf;
+      const Clock::time_point now = Clock::now();
+      for (const FarmJob &j : jobs) {
+        FarmResult &r = f->results[j.ticket];
+        r.state = RUNNING;
+        r.t_start = now;
+        if (!ok) {
+          r.state = DONE;
+          r.status = BEMGPU_ERR_OOM;
+          char buf[160];
+          snprintf(buf, sizeof buf, "farm: the request needs %.2f GB, more than the farm's budget of %.2f GB",
+                   need / 1e9, f->budget / 1e9);
+          r.error = buf;
+        }
       }
     }
     if (!ok) {
       f->cv_done.notify_all();
       continue;
     }
-    double P = 0.0;
-    bemgpu_solve_info_t info{};
-    const int rc = bemgpu_heat_transfer(ctx, job.top, job.s, job.t, &job.req, &job.opt, job.precision, &P, &info);
+    const int nb = (int)jobs.size();
+    std::vector<double> P(nb, 0.0);
+    std::vector<bemgpu_solve_info_t> info(nb);
+    std::vector<int> rcs(nb, BEMGPU_OK);
+    if (nb == 1) {
+      const FarmJob &job = jobs[0];
+      rcs[0] = bemgpu_heat_transfer(ctx, job.top, job.s, job.t, &job.req, &job.opt, job.precision, &P[0], &info[0]);
+    } else {
+      std::vector<bemgpu_tree_t> tops(nb), ss(nb), ts(nb);
+      std::vector<bemgpu_solve_req_t> reqs(nb);
+      for (int k = 0; k < nb; k++) {
+        tops[k] = jobs[k].top;
+        ss[k] = jobs[k].s;
+        ts[k] = jobs[k].t;
+        reqs[k] = jobs[k].req;
+      }
+      const int rc = bemgpu_heat_transfer_batch(ctx, nb, tops.data(), ss.data(), ts.data(), reqs.data(), &jobs[0].opt,
+                                                jobs[0].precision, P.data(), info.data(), rcs.data());
+      if (rc == BEMGPU_ERR_ARG || rc == BEMGPU_ERR_OOM)  // the batch as a whole did not start
+        for (int k = 0; k < nb; k++) rcs[k] = rc;
+    }
     const size_t held = (size_t)std::max<int64_t>(0, bemgpu_ctx_workspace_bytes(ctx));
     {
       std::unique_lock<std::mutex> lk(f->mu);
-      FarmResult &r = f->results[job.ticket];
-      r.state = DONE;
-      r.status = rc;
-      r.P = P;
-      r.info = info;
       const Clock::time_point now = Clock::now();
-      r.info.ms_queued = ms_between(r.t_submit, r.t_start);
-      r.info.ms_latency = ms_between(r.t_submit, now);
-      if (rc != BEMGPU_OK) r.error = bemgpu_ctx_last_error(ctx);
+      for (int k = 0; k < nb; k++) {
+        FarmResult &r = f->results[jobs[k].ticket];
+        r.state = DONE;
+        r.status = rcs[k];
+        r.P = P[k];
+        r.info = info[k];
+        r.info.ms_queued = ms_between(r.t_submit, r.t_start);
+        r.info.ms_latency = ms_between(r.t_submit, now);
+        if (rcs[k] != BEMGPU_OK) r.error = bemgpu_ctx_last_error(ctx);
+      }
       f->held[lane] = held;
       f->reserved[lane] = 0;
       f->state[lane] = IDLE;
@@ -236,6 +285,13 @@ int bemgpu_farm_destroy(bemgpu_farm_t f) {
 }
 
 int bemgpu_farm_lanes(bemgpu_farm_t f) { return f ? (int)f->lanes.size() : BEMGPU_ERR_ARG; }
+
+int bemgpu_farm_set_batch(bemgpu_farm_t f, int max_requests) {
+  if (!f || max_requests < 1 || max_requests > BEM_MAX_BATCH) return BEMGPU_ERR_ARG;
+  std::lock_guard<std::mutex> lk(f->mu);
+  f->batch = max_requests;
+  return BEMGPU_OK;
+}
 
 int bemgpu_farm_set_budget(bemgpu_farm_t f, int64_t bytes) {
   if (!f || bytes <= 0) return BEMGPU_ERR_ARG;

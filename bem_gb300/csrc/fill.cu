@@ -552,14 +552,39 @@ __device__ __noinline__ void far_pair_fp32(const TriRec &T, const TriRec &S, con
   }
 }
 
+// One fill of a group launch: Zts(t, s, g) into the half-pair blocks H, with
+// its share of the group's far tiles and near work units (prefix offsets).
+struct FillTask {
+  const TriRec *T, *S;       // test and source trees' records
+  const TriDF *TD, *SD;      // their double-float records (double-float mode), else null
+  const NearPair *near;      // the near-pair list of (t, s)
+  HalfPairBlock *H;          // this fill's half-pair blocks
+  int64_t nnear;             // near pairs
+  int64_t near0;             // first near work unit of the group that is this task's
+  int64_t far0;              // first far tile of the group that is this task's
+  int ntT, ntS, ntr, far_tx; // triangles of t and s, RWGs of t, far tiles along s
+  GreenDev g;
+};
+
+__device__ __forceinline__ int task_of_far(const FillTask *tk, int n, int64_t u) {
+  int i = n - 1;
+  while (i > 0 && u < tk[i].far0) i--;
+  return i;
+}
+
+__device__ __forceinline__ int task_of_near(const FillTask *tk, int n, int64_t u) {
+  int i = n - 1;
+  while (i > 0 && u < tk[i].near0) i--;
+  return i;
+}
+
 // mixed != 0: pairs whose centroid distance exceeds 3 edge lengths (the longer
 // of the two triangles' longest edges) are integrated in FP32.
-__global__ void __launch_bounds__(256) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
-                                                        const TriRec *__restrict__ Sr, int ntS, GreenDev g,
-                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mode,
-                                                        const TriDF *__restrict__ TDr, const TriDF *__restrict__ SDr) {
-  const int sb = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ta = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void far_pair_at(const TriRec *__restrict__ Tr, int ntT, const TriRec *__restrict__ Sr,
+                                            int ntS, const GreenDev &g, const FarOpts &o,
+                                            HalfPairBlock *__restrict__ H, int ntr, int mode,
+                                            const TriDF *__restrict__ TDr, const TriDF *__restrict__ SDr, int sb,
+                                            int ta) {
   if (sb >= ntS || ta >= ntT) return;
   const TriRec &T = Tr[ta];
   const TriRec &S = Sr[sb];
@@ -592,6 +617,33 @@ __global__ void __launch_bounds__(256) far_pairs_kernel(const TriRec *__restrict
   else if (__dmul_rn(d, o.th15) > emax2) far_pair(T, S, g, c_rule15, 15, H, ntr);
   else if (__dmul_rn(d, o.th21) > emax2) far_pair(T, S, g, c_rule21, 21, H, ntr);
   else far_pair(T, S, g, c_rule36, 36, H, ntr);
+}
+
+// One fill (t, s, g) -> H: thread (x, y) of the 2-D grid takes the source
+// triangle blockIdx.x * 32 + x and the test triangle blockIdx.y * blockDim.y + y.
+__global__ void __launch_bounds__(256) far_pairs_kernel(const TriRec *__restrict__ Tr, int ntT,
+                                                        const TriRec *__restrict__ Sr, int ntS, GreenDev g,
+                                                        FarOpts o, HalfPairBlock *__restrict__ H, int ntr, int mode,
+                                                        const TriDF *__restrict__ TDr, const TriDF *__restrict__ SDr) {
+  far_pair_at(Tr, ntT, Sr, ntS, g, o, H, ntr, mode, TDr, SDr, blockIdx.x * blockDim.x + threadIdx.x,
+              blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// A group of fills in one launch (the three Zts of a solve, or of several
+// requests): CTA b takes far tile b of the task whose range holds it, a tile
+// being 32 source x blockDim.y test triangles.  The task's Green's function
+// is staged in shared memory (one task per CTA).
+__global__ void __launch_bounds__(256) far_pairs_group_kernel(const FillTask *__restrict__ tasks, int ntask,
+                                                              FarOpts o, int mode) {
+  __shared__ GreenDev s_g;
+  const int i = task_of_far(tasks, ntask, blockIdx.x);
+  const FillTask &tk = tasks[i];
+  if (threadIdx.x == 0 && threadIdx.y == 0) s_g = tk.g;
+  __syncthreads();
+  const int64_t local = (int64_t)blockIdx.x - tk.far0;
+  const int bx = (int)(local % tk.far_tx), by = (int)(local / tk.far_tx);
+  far_pair_at(tk.T, tk.ntT, tk.S, tk.ntS, s_g, o, tk.H, tk.ntr, mode, tk.TD, tk.SD, bx * 32 + threadIdx.x,
+              by * blockDim.y + threadIdx.y);
 }
 
 // ---------------- near pairs ----------------
@@ -677,8 +729,6 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 constexpr int NEAR_WARPS = 4;
-constexpr int NEAR_MOM_FLOATS = 32;          // one outer node's smooth inner moments (InnerMomDF)
-constexpr int64_t NEAR_MOM_CHUNK = 8192;     // near pairs per moments launch: 8192 x 105 x 128 B = 110 MB
 
 // Moments of the smooth inner rule at one outer node (complex df):
 // I0 = sum w g~, A = sum w g~ l, Q0 = sum w q~, Q1 = sum w q~ l.
@@ -1018,191 +1068,92 @@ __device__ __noinline__ void near_finish_df(const TriRec &T, const TriRec &S, in
 // lanes busy, against 82 % for 105 nodes in 4 rounds); each lane adds to the
 // sums of the pair its node belongs to, and the warp finishes the pairs one
 // after the other.
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_df_kernel(
-    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
-    GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
-  __shared__ __align__(16) float s_nodes[NEAR_WARPS][2][BEMGPU_TRI_RULE91_N][8];
-  __shared__ float s_outer[BEMGPU_TRI_RULE105_N][6];
-  __shared__ NearPairDF s_pc[NEAR_WARPS][2];
-  const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
+// The pair couple (p0, p0 + 1) of `list` (one pair when p0 + 1 == npairs),
+// worked by one warp; nodes, pc: the warp's shared staging, outer: the outer
+// rule in double-float.
+__device__ __forceinline__ void near_couple_df(const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr,
+                                               const NearPair *__restrict__ list, int64_t npairs, int64_t p0,
+                                               const GreenDev &g, HalfPairBlock *__restrict__ H, int ntr,
+                                               float (*nodes)[BEMGPU_TRI_RULE91_N][8], const float (*outer)[6],
+                                               NearPairDF *pcs, int lane) {
+  const int np2 = p0 + 1 < npairs ? 2 : 1;
+  NearPair npr[2];
+  npr[0] = list[p0];
+  npr[1] = list[np2 == 2 ? p0 + 1 : p0];
+  // inner nodes l = r_s - P_s and weights of both pairs, then their records
+  for (int it = lane; it < np2 * BEMGPU_TRI_RULE91_N; it += 32) {
+    const int k = it >= BEMGPU_TRI_RULE91_N ? 1 : 0, u = it - k * BEMGPU_TRI_RULE91_N;
+    const TriRec &S = Sr[npr[k].s];
+    const d3 l = c_rule91[u][0] * ld3(S.v01) + c_rule91[u][1] * ld3(S.v02);
+    const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      const df v = df_make(vals[c]);
+      nodes[k][u][2 * c] = v.hi;
+      nodes[k][u][2 * c + 1] = v.lo;
+    }
+  }
+  if (lane < np2) near_pair_df_setup(Tr[npr[lane].t], Sr[npr[lane].s], g, pcs[lane]);
+  __syncwarp();
+  NearAccDF acc[2];
+  const df z = {0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    acc[0].L[k] = {z, z}; acc[0].K[k] = {z, z};
+    acc[1].L[k] = {z, z}; acc[1].K[k] = {z, z};
+  }
+  for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
+    const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
+    const NearPairDF &pc = pcs[k];
+    const float *o = outer[q];
+    const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
+    const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
+    const df3 rs = df3_sub(rt1, pc.sPs);
+    InnerMomDF mom;
+    near_inner_df<1>(nodes[k], &rs, g, &mom);
+    near_outer_df(mom, pc, Tr[npr[k].t].nh, Sr[npr[k].s].nh, rt1, wq, acc[k]);
+  }
+  for (int k = 0; k < np2; k++) near_finish_df(Tr[npr[k].t], Sr[npr[k].s], npr[k].same, pcs[k], acc[k], H, ntr);
+  __syncwarp();
+}
+
+__device__ __forceinline__ void stage_outer_df(float (*outer)[6]) {
   for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
     for (int c = 0; c < 3; c++) {
       const df v = df_make(c_rule105[u][c]);
-      s_outer[u][2 * c] = v.hi;
-      s_outer[u][2 * c + 1] = v.lo;
+      outer[u][2 * c] = v.hi;
+      outer[u][2 * c + 1] = v.lo;
     }
   __syncthreads();
-  const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
-  for (int64_t p0 = 2 * ((int64_t)blockIdx.x * NEAR_WARPS + wid); p0 < npairs; p0 += 2 * nw) {
-    const int np2 = p0 + 1 < npairs ? 2 : 1;
-    NearPair npr[2];
-    npr[0] = list[p0];
-    npr[1] = list[np2 == 2 ? p0 + 1 : p0];
-    // inner nodes l = r_s - P_s and weights of both pairs, then their records
-    for (int it = lane; it < np2 * BEMGPU_TRI_RULE91_N; it += 32) {
-      const int k = it >= BEMGPU_TRI_RULE91_N ? 1 : 0, u = it - k * BEMGPU_TRI_RULE91_N;
-      const TriRec &S = Sr[npr[k].s];
-      const d3 l = c_rule91[u][0] * ld3(S.v01) + c_rule91[u][1] * ld3(S.v02);
-      const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const df v = df_make(vals[c]);
-        s_nodes[wid][k][u][2 * c] = v.hi;
-        s_nodes[wid][k][u][2 * c + 1] = v.lo;
-      }
-    }
-    if (lane < np2) near_pair_df_setup(Tr[npr[lane].t], Sr[npr[lane].s], g, s_pc[wid][lane]);
-    __syncwarp();
-    NearAccDF acc[2];
-    const df z = {0.f, 0.f};
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      acc[0].L[k] = {z, z}; acc[0].K[k] = {z, z};
-      acc[1].L[k] = {z, z}; acc[1].K[k] = {z, z};
-    }
-    for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
-      const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
-      const NearPairDF &pc = s_pc[wid][k];
-      const float *o = s_outer[q];
-      const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
-      const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
-      const df3 rs = df3_sub(rt1, pc.sPs);
-      InnerMomDF mom;
-      near_inner_df<1>(s_nodes[wid][k], &rs, g, &mom);
-      near_outer_df(mom, pc, Tr[npr[k].t].nh, Sr[npr[k].s].nh, rt1, wq, acc[k]);
-    }
-    for (int k = 0; k < np2; k++)
-      near_finish_df(Tr[npr[k].t], Sr[npr[k].s], npr[k].same, s_pc[wid][k], acc[k], H, ntr);
-    __syncwarp();
-  }
 }
 
-// The same near pairs in two kernels, so that the inner rule (nine tenths of
-// the arithmetic) runs with the registers it needs rather than those of the
-// closed forms and contraction: near_moments_df_kernel writes the smooth inner
-// moments of every (pair, outer node) of a chunk of pairs to a scratch array
-// (structure of arrays, NEAR_MOM_FLOATS planes), near_outer_df_kernel reads
-// them back and finishes the pairs exactly as near_pairs_df_kernel does.  The
-// arithmetic and its order are unchanged, so the matrices are bit-identical.
-static_assert(sizeof(InnerMomDF) == NEAR_MOM_FLOATS * sizeof(float), "moment layout");
-
-__device__ __forceinline__ void mom_store(float *mom, int64_t stride, int64_t j, const InnerMomDF &m) {
-  const float *f = reinterpret_cast<const float *>(&m);
-#pragma unroll
-  for (int c = 0; c < NEAR_MOM_FLOATS; c++) mom[c * stride + j] = f[c];
-}
-
-__device__ __forceinline__ void mom_load(const float *__restrict__ mom, int64_t stride, int64_t j, InnerMomDF &m) {
-  float *f = reinterpret_cast<float *>(&m);
-#pragma unroll
-  for (int c = 0; c < NEAR_MOM_FLOATS; c++) f[c] = __ldcs(mom + c * stride + j);
-}
-
-// Pairs [0, npairs) of `list` (a chunk), two per warp as near_pairs_df_kernel
-// takes them; the moments of pair p, outer node q go to index p * 105 + q of
-// each plane (stride = npairs * 105).  MINB: CTAs per SM the register
-// allocation must allow (2: 224 registers, no spills; 3: 168; 4: 128, with
-// some spilled to local memory); the context's tuning picks one.
+// A group of fills: the warps walk the group's pair couples (a task's couples
+// are units [near0, near0 + ceil(nnear / 2)) of the group), each staging its
+// task's Green's function in shared memory.  MINB: CTAs per SM that the
+// register allocation must allow (2: ~250 registers; 3: 168; 4: 128 with
+// spills), chosen by the context's tuning.
 template <int MINB>
-__global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_moments_df_kernel(
-    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
-    GreenDev g, float *__restrict__ mom) {
+__global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_pairs_df_group_kernel(const FillTask *__restrict__ tasks,
+                                                                                    int ntask, int64_t units) {
   __shared__ __align__(16) float s_nodes[NEAR_WARPS][2][BEMGPU_TRI_RULE91_N][8];
   __shared__ float s_outer[BEMGPU_TRI_RULE105_N][6];
-  __shared__ df3 s_frame[NEAR_WARPS][2][3];  // the test triangle's v01, v02 and P_s - P_t
-  const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  const int64_t stride = npairs * BEMGPU_TRI_RULE105_N;
-  for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
-    for (int c = 0; c < 3; c++) {
-      const df v = df_make(c_rule105[u][c]);
-      s_outer[u][2 * c] = v.hi;
-      s_outer[u][2 * c + 1] = v.lo;
-    }
-  __syncthreads();
-  const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
-  for (int64_t p0 = 2 * ((int64_t)blockIdx.x * NEAR_WARPS + wid); p0 < npairs; p0 += 2 * nw) {
-    const int np2 = p0 + 1 < npairs ? 2 : 1;
-    NearPair npr[2];
-    npr[0] = list[p0];
-    npr[1] = list[np2 == 2 ? p0 + 1 : p0];
-    for (int it = lane; it < np2 * BEMGPU_TRI_RULE91_N; it += 32) {
-      const int k = it >= BEMGPU_TRI_RULE91_N ? 1 : 0, u = it - k * BEMGPU_TRI_RULE91_N;
-      const TriRec &S = Sr[npr[k].s];
-      const d3 l = c_rule91[u][0] * ld3(S.v01) + c_rule91[u][1] * ld3(S.v02);
-      const double vals[4] = {l.x, l.y, l.z, c_rule91[u][2]};
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const df v = df_make(vals[c]);
-        s_nodes[wid][k][u][2 * c] = v.hi;
-        s_nodes[wid][k][u][2 * c + 1] = v.lo;
-      }
-    }
-    if (lane < np2) {
-      const TriRec &T = Tr[npr[lane].t], &S = Sr[npr[lane].s];
-      s_frame[wid][lane][0] = df3_make(ld3(T.v01));
-      s_frame[wid][lane][1] = df3_make(ld3(T.v02));
-      s_frame[wid][lane][2] = df3_make(ld3(S.p0) - ld3(T.p0));
-    }
-    __syncwarp();
-    for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
-      const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
-      const float *o = s_outer[q];
-      const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]};
-      const df3 rt1 = df3_add(df3_scale(xi1, s_frame[wid][k][0]), df3_scale(xi2, s_frame[wid][k][1]));
-      const df3 rs = df3_sub(rt1, s_frame[wid][k][2]);
-      InnerMomDF m;
-      near_inner_df<1>(s_nodes[wid][k], &rs, g, &m);
-      mom_store(mom, stride, (p0 + k) * BEMGPU_TRI_RULE105_N + q, m);
-    }
-    __syncwarp();
-  }
-}
-
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_outer_df_kernel(
-    const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
-    GreenDev g, const float *__restrict__ mom, HalfPairBlock *__restrict__ H, int ntr) {
-  __shared__ float s_outer[BEMGPU_TRI_RULE105_N][6];
   __shared__ NearPairDF s_pc[NEAR_WARPS][2];
+  __shared__ GreenDev s_g[NEAR_WARPS];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  const int64_t stride = npairs * BEMGPU_TRI_RULE105_N;
-  for (int u = threadIdx.x; u < BEMGPU_TRI_RULE105_N; u += blockDim.x)
-    for (int c = 0; c < 3; c++) {
-      const df v = df_make(c_rule105[u][c]);
-      s_outer[u][2 * c] = v.hi;
-      s_outer[u][2 * c + 1] = v.lo;
-    }
-  __syncthreads();
+  stage_outer_df(s_outer);
   const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
-  for (int64_t p0 = 2 * ((int64_t)blockIdx.x * NEAR_WARPS + wid); p0 < npairs; p0 += 2 * nw) {
-    const int np2 = p0 + 1 < npairs ? 2 : 1;
-    NearPair npr[2];
-    npr[0] = list[p0];
-    npr[1] = list[np2 == 2 ? p0 + 1 : p0];
-    if (lane < np2) near_pair_df_setup(Tr[npr[lane].t], Sr[npr[lane].s], g, s_pc[wid][lane]);
-    __syncwarp();
-    NearAccDF acc[2];
-    const df z = {0.f, 0.f};
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      acc[0].L[k] = {z, z}; acc[0].K[k] = {z, z};
-      acc[1].L[k] = {z, z}; acc[1].K[k] = {z, z};
+  int cur = -1;
+  for (int64_t u = (int64_t)blockIdx.x * NEAR_WARPS + wid; u < units; u += nw) {
+    const int i = task_of_near(tasks, ntask, u);
+    const FillTask &tk = tasks[i];
+    if (i != cur) {
+      if (lane == 0) s_g[wid] = tk.g;
+      __syncwarp();
+      cur = i;
     }
-    for (int it = lane; it < np2 * BEMGPU_TRI_RULE105_N; it += 32) {
-      const int k = it >= BEMGPU_TRI_RULE105_N ? 1 : 0, q = it - k * BEMGPU_TRI_RULE105_N;
-      const NearPairDF &pc = s_pc[wid][k];
-      const float *o = s_outer[q];
-      const df xi1 = {o[0], o[1]}, xi2 = {o[2], o[3]}, wq = {o[4], o[5]};
-      const df3 rt1 = df3_add(df3_scale(xi1, pc.v01t), df3_scale(xi2, pc.v02t));
-      InnerMomDF m;
-      mom_load(mom, stride, (p0 + k) * BEMGPU_TRI_RULE105_N + q, m);
-      near_outer_df(m, pc, Tr[npr[k].t].nh, Sr[npr[k].s].nh, rt1, wq, acc[k]);
-    }
-    for (int k = 0; k < np2; k++)
-      near_finish_df(Tr[npr[k].t], Sr[npr[k].s], npr[k].same, s_pc[wid][k], acc[k], H, ntr);
-    __syncwarp();
+    near_couple_df(tk.T, tk.S, tk.near, tk.nnear, 2 * (u - tk.near0), s_g[wid], tk.H, tk.ntr, s_nodes[wid],
+                   s_outer, s_pc[wid], lane);
   }
 }
 
@@ -1210,183 +1161,210 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_outer_df_kernel(
 // outer nodes, each runs the 91-node smooth inner rule, the analytic singular
 // terms and the close-pair contraction; the warp sums, adds the neighbour-edge
 // K correction and scatters.
+// Near pair p of `list` in FP64, worked by one warp (nodes: the warp's
+// shared staging of the inner rule).
+__device__ __forceinline__ void near_pair_fp64(const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr,
+                                               const NearPair *__restrict__ list, int64_t p, const GreenDev &g,
+                                               HalfPairBlock *__restrict__ H, int ntr, double (*nodes)[4], int lane) {
+  const z1 ksq = {g.ksqr, g.ksqi};
+  const z1 k2 = {g.k2r, g.k2i};
+  const NearPair np = list[p];
+  const TriRec &T = Tr[np.t];
+  const TriRec &S = Sr[np.s];
+  const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
+  const d3 v01t = ld3(T.v01), v02t = ld3(T.v02);
+  {
+    const d3 v01s = ld3(S.v01), v02s = ld3(S.v02);
+    for (int u = lane; u < BEMGPU_TRI_RULE91_N; u += 32) {
+      const d3 l = c_rule91[u][0] * v01s + c_rule91[u][1] * v02s;
+      nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
+      nodes[u][3] = c_rule91[u][2];
+    }
+  }
+  __syncwarp();
+  const int nht = T.nh, nhs = S.nh;
+  d3 dj[3];
+  for (int j = 0; j < 3; j++) dj[j] = (j < nhs) ? ld3(S.hp0[j]) - Ps : d3{0, 0, 0};
+  z1 L[9], K[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) { L[k] = {0, 0}; K[k] = {0, 0}; }
+  const d3 nS = ld3(S.n);
+  const double Ai2 = 0.5 * S.Ai;
+  for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
+    const double w = c_rule105[q][2];
+    const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
+    const d3 rts = rt - Ps;
+    // LKSmoothInnerIntegrand over s[0] (src/Impedance.cpp:93-105) as moments
+    z1 I0 = {0, 0}, Q0 = {0, 0};
+    z3 A = z3zero(), Q1 = z3zero();
+    for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
+      const d3 l = {nodes[u][0], nodes[u][1], nodes[u][2]};
+      const double ws = nodes[u][3];
+      const d3 x = rts - l;
+      const double R2 = dot(x, x);
+      const double R = sqrt(R2);
+      const z1 e = zexp_ikR(g, R);
+      // scalar_gradient_smooth, src/GreensFunction.cpp:54-69
+      const double Ri = 1.0 / R;
+      const z1 gs = zsub(zscale(Ri, z1{e.r - 1.0, e.i}), zscale(R, k2));
+      const z1 ikR = {g.ikr * R, g.iki * R};
+      z1 num = zmul(e, z1{1.0 - ikR.r, -ikR.i});
+      num = zadd(num, zscale(R2, k2));
+      num.r -= 1.0;
+      const z1 qq = zscale(Ri * Ri * Ri, num);
+      const z1 gw = zscale(ws, gs), qw = zscale(ws, qq);
+      zacc(I0, gw);
+      A = z3add(A, zs_v(gw, l));
+      zacc(Q0, qw);
+      Q1 = z3add(Q1, zs_v(qw, l));
+    }
+    // LKCloseOuterIntegrand::weighPoint, src/Impedance.cpp:194-250
+    double ISn3h, ISn1, IS1;
+    d3 IL1, IL3;
+    eh_nonsmooth(S, rt, ISn3h, ISn1, IS1, IL1, IL3);
+    const z3 IL13 = z3scale(Ai2, z3add_r(zs_v(zscale(BEM_ONETHIRD, k2), IL3), IL1));
+    z1 ISn11 = zscale(Ai2, z1{ISn1 + k2.r * IS1, k2.i * IS1});
+    const double h = dot(rt - Ps, nS);
+    const z1 L2 = zadd(zscale(2.0, ISn11), I0);
+    if (fabs(h) < 1e-8 * S.elen0) {
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        if (j >= nhs) break;
+        const z3 Gphij = z3scale(0.5, z3sub(A, zs_v(I0, dj[j])));
+        const z3 K21 = z3add(IL13, zs_v(ISn11, rt - ld3(S.hp0[j])));
+        const z3 GK = z3add(Gphij, K21);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          if (i >= nht) break;
+          const d3 phi = 0.5 * (rt - ld3(T.hp0[i]));
+          const z1 t = zsub(zmul(ksq, rdot(phi, GK)), L2);
+          zacc(L[i * 3 + j], zscale(w, t));
+        }
+      }
+    } else {
+      const d3 ISn3hn = (Ai2 * ISn3h) * nS;
+      const d3 rho = rt - h * nS;
+      const z1 Ai2k2 = zscale(Ai2, k2);
+      const z3 K31 = zs_v(Ai2k2, IL1 - (h * ISn1) * nS);
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        if (j >= nhs) break;
+        const d3 p0j = ld3(S.hp0[j]);
+        const z3 Gphij = z3scale(0.5, z3sub(A, zs_v(I0, dj[j])));
+        const z3 DGxphij = z3scale(0.5, rcross(rt - p0j, z3sub(Q1, zs_v(Q0, dj[j]))));
+        const z3 K21 = z3add(IL13, zs_v(ISn11, rho - p0j));
+        const z3 K41 = zcross(K31, rt - p0j);
+        const z3 GK = z3add(Gphij, K21);
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          if (i >= nht) break;
+          const d3 p0i = ld3(T.hp0[i]);
+          const d3 phi = 0.5 * (rt - p0i);
+          const z1 t = zsub(zmul(ksq, rdot(phi, GK)), L2);
+          zacc(L[i * 3 + j], zscale(w, t));
+          const d3 vts = p0j - p0i;
+          const z3 KK = z3add(z3add_r(DGxphij, cross(vts, ISn3hn)), K41);
+          const z1 kk = rdot(phi, KK);
+          K[i * 3 + j].r -= w * kk.r;
+          K[i * 3 + j].i -= w * kk.i;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    L[k].r = warp_sum(L[k].r); L[k].i = warp_sum(L[k].i);
+    K[k].r = warp_sum(K[k].r); K[k].i = warp_sum(K[k].i);
+  }
+  if (!np.same) {
+    // neighbour-edge K correction, src/Impedance.cpp:301-324: three source
+    // edges x QuadratureGauss15, LKNeighborEdgeIntegrand over t[0].
+    d3 Ke[3][3];
+#pragma unroll
+    for (int e = 0; e < 3; e++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) Ke[e][i] = {0, 0, 0};
+    const d3 nT = ld3(T.n);
+    for (int idx = lane; idx < 45; idx += 32) {
+      const int e = idx / 15, q = idx - e * 15;
+      const d3 v0 = e == 0 ? ld3(S.p0) : (e == 1 ? ld3(S.p1) : ld3(S.p2));
+      const d3 v1 = e == 0 ? ld3(S.v01) : (e == 1 ? ld3(S.v12) : ld3(S.v20));
+      const d3 v = v0 + c_line15[q][0] * v1;
+      const double w = c_line15[q][1];
+      double ISn1;
+      d3 IL1;
+      lk_edge_integral(T, v, ISn1, IL1);
+      const double h = dot(v - Pt, nT);
+      const d3 rho = v - h * nT;
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        if (i >= nht) break;
+        const d3 c = IL1 + ISn1 * (rho - ld3(T.hp0[i]));
+        if (e == 0) Ke[0][i] = Ke[0][i] + w * c;
+        else if (e == 1) Ke[1][i] = Ke[1][i] + w * c;
+        else Ke[2][i] = Ke[2][i] + w * c;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 3; e++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        Ke[e][i].x = warp_sum(Ke[e][i].x);
+        Ke[e][i].y = warp_sum(Ke[e][i].y);
+        Ke[e][i].z = warp_sum(Ke[e][i].z);
+      }
+    const double c = 0.125 * T.Ai * S.Ai;
+    const d3 m01 = ld3(S.m01), m12 = ld3(S.m12), m20 = ld3(S.m20);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        if (i >= nht || j >= nhs) continue;
+        const d3 v = ld3(T.hp0[i]) - ld3(S.hp0[j]);
+        K[i * 3 + j].r += c * (dot(cross(v, m01), Ke[0][i]) / S.nv01i + dot(cross(v, m12), Ke[1][i]) / S.nv12i +
+                               dot(cross(v, m20), Ke[2][i]) / S.nv20i);
+      }
+  }
+  if (lane < nht * nhs) {
+    const int i = lane / nhs, j = lane - (lane / nhs) * nhs;
+    z1 Lv = {0, 0}, Kv = {0, 0};
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+      if (k == i * 3 + j) { Lv = L[k]; Kv = K[k]; }
+    const double c = scatter_coef(T, i, S, j);
+    store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, Lv), zscale(c, Kv));
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_kernel(
     const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr, const NearPair *__restrict__ list, int64_t npairs,
     GreenDev g, HalfPairBlock *__restrict__ H, int ntr) {
   __shared__ double s_nodes[NEAR_WARPS][BEMGPU_TRI_RULE91_N][4];  // l = r_s - P_s (xyz), weight
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  double(*nodes)[4] = s_nodes[wid];
-  const z1 ksq = {g.ksqr, g.ksqi};
-  const z1 k2 = {g.k2r, g.k2i};
-  for (int64_t p = (int64_t)blockIdx.x * NEAR_WARPS + wid; p < npairs; p += (int64_t)gridDim.x * NEAR_WARPS) {
-    const NearPair np = list[p];
-    const TriRec &T = Tr[np.t];
-    const TriRec &S = Sr[np.s];
-    const d3 Pt = ld3(T.p0), Ps = ld3(S.p0);
-    const d3 v01t = ld3(T.v01), v02t = ld3(T.v02);
-    {
-      const d3 v01s = ld3(S.v01), v02s = ld3(S.v02);
-      for (int u = lane; u < BEMGPU_TRI_RULE91_N; u += 32) {
-        const d3 l = c_rule91[u][0] * v01s + c_rule91[u][1] * v02s;
-        nodes[u][0] = l.x; nodes[u][1] = l.y; nodes[u][2] = l.z;
-        nodes[u][3] = c_rule91[u][2];
-      }
+  for (int64_t p = (int64_t)blockIdx.x * NEAR_WARPS + wid; p < npairs; p += (int64_t)gridDim.x * NEAR_WARPS)
+    near_pair_fp64(Tr, Sr, list, p, g, H, ntr, s_nodes[wid], lane);
+}
+
+// A group of fills in FP64: the warps walk the group's near pairs (a task's
+// pairs are units [near0, near0 + nnear) of the group).
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_pairs_group_kernel(const FillTask *__restrict__ tasks,
+                                                                           int ntask, int64_t units) {
+  __shared__ double s_nodes[NEAR_WARPS][BEMGPU_TRI_RULE91_N][4];
+  __shared__ GreenDev s_g[NEAR_WARPS];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  int cur = -1;
+  for (int64_t u = (int64_t)blockIdx.x * NEAR_WARPS + wid; u < units; u += (int64_t)gridDim.x * NEAR_WARPS) {
+    const int i = task_of_near(tasks, ntask, u);
+    const FillTask &tk = tasks[i];
+    if (i != cur) {
+      if (lane == 0) s_g[wid] = tk.g;
+      __syncwarp();
+      cur = i;
     }
-    __syncwarp();
-    const int nht = T.nh, nhs = S.nh;
-    d3 dj[3];
-    for (int j = 0; j < 3; j++) dj[j] = (j < nhs) ? ld3(S.hp0[j]) - Ps : d3{0, 0, 0};
-    z1 L[9], K[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) { L[k] = {0, 0}; K[k] = {0, 0}; }
-    const d3 nS = ld3(S.n);
-    const double Ai2 = 0.5 * S.Ai;
-    for (int q = lane; q < BEMGPU_TRI_RULE105_N; q += 32) {
-      const double w = c_rule105[q][2];
-      const d3 rt = (Pt + c_rule105[q][0] * v01t) + c_rule105[q][1] * v02t;
-      const d3 rts = rt - Ps;
-      // LKSmoothInnerIntegrand over s[0] (src/Impedance.cpp:93-105) as moments
-      z1 I0 = {0, 0}, Q0 = {0, 0};
-      z3 A = z3zero(), Q1 = z3zero();
-      for (int u = 0; u < BEMGPU_TRI_RULE91_N; u++) {
-        const d3 l = {nodes[u][0], nodes[u][1], nodes[u][2]};
-        const double ws = nodes[u][3];
-        const d3 x = rts - l;
-        const double R2 = dot(x, x);
-        const double R = sqrt(R2);
-        const z1 e = zexp_ikR(g, R);
-        // scalar_gradient_smooth, src/GreensFunction.cpp:54-69
-        const double Ri = 1.0 / R;
-        const z1 gs = zsub(zscale(Ri, z1{e.r - 1.0, e.i}), zscale(R, k2));
-        const z1 ikR = {g.ikr * R, g.iki * R};
-        z1 num = zmul(e, z1{1.0 - ikR.r, -ikR.i});
-        num = zadd(num, zscale(R2, k2));
-        num.r -= 1.0;
-        const z1 qq = zscale(Ri * Ri * Ri, num);
-        const z1 gw = zscale(ws, gs), qw = zscale(ws, qq);
-        zacc(I0, gw);
-        A = z3add(A, zs_v(gw, l));
-        zacc(Q0, qw);
-        Q1 = z3add(Q1, zs_v(qw, l));
-      }
-      // LKCloseOuterIntegrand::weighPoint, src/Impedance.cpp:194-250
-      double ISn3h, ISn1, IS1;
-      d3 IL1, IL3;
-      eh_nonsmooth(S, rt, ISn3h, ISn1, IS1, IL1, IL3);
-      const z3 IL13 = z3scale(Ai2, z3add_r(zs_v(zscale(BEM_ONETHIRD, k2), IL3), IL1));
-      z1 ISn11 = zscale(Ai2, z1{ISn1 + k2.r * IS1, k2.i * IS1});
-      const double h = dot(rt - Ps, nS);
-      const z1 L2 = zadd(zscale(2.0, ISn11), I0);
-      if (fabs(h) < 1e-8 * S.elen0) {
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-          if (j >= nhs) break;
-          const z3 Gphij = z3scale(0.5, z3sub(A, zs_v(I0, dj[j])));
-          const z3 K21 = z3add(IL13, zs_v(ISn11, rt - ld3(S.hp0[j])));
-          const z3 GK = z3add(Gphij, K21);
-#pragma unroll
-          for (int i = 0; i < 3; i++) {
-            if (i >= nht) break;
-            const d3 phi = 0.5 * (rt - ld3(T.hp0[i]));
-            const z1 t = zsub(zmul(ksq, rdot(phi, GK)), L2);
-            zacc(L[i * 3 + j], zscale(w, t));
-          }
-        }
-      } else {
-        const d3 ISn3hn = (Ai2 * ISn3h) * nS;
-        const d3 rho = rt - h * nS;
-        const z1 Ai2k2 = zscale(Ai2, k2);
-        const z3 K31 = zs_v(Ai2k2, IL1 - (h * ISn1) * nS);
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-          if (j >= nhs) break;
-          const d3 p0j = ld3(S.hp0[j]);
-          const z3 Gphij = z3scale(0.5, z3sub(A, zs_v(I0, dj[j])));
-          const z3 DGxphij = z3scale(0.5, rcross(rt - p0j, z3sub(Q1, zs_v(Q0, dj[j]))));
-          const z3 K21 = z3add(IL13, zs_v(ISn11, rho - p0j));
-          const z3 K41 = zcross(K31, rt - p0j);
-          const z3 GK = z3add(Gphij, K21);
-#pragma unroll
-          for (int i = 0; i < 3; i++) {
-            if (i >= nht) break;
-            const d3 p0i = ld3(T.hp0[i]);
-            const d3 phi = 0.5 * (rt - p0i);
-            const z1 t = zsub(zmul(ksq, rdot(phi, GK)), L2);
-            zacc(L[i * 3 + j], zscale(w, t));
-            const d3 vts = p0j - p0i;
-            const z3 KK = z3add(z3add_r(DGxphij, cross(vts, ISn3hn)), K41);
-            const z1 kk = rdot(phi, KK);
-            K[i * 3 + j].r -= w * kk.r;
-            K[i * 3 + j].i -= w * kk.i;
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 9; k++) {
-      L[k].r = warp_sum(L[k].r); L[k].i = warp_sum(L[k].i);
-      K[k].r = warp_sum(K[k].r); K[k].i = warp_sum(K[k].i);
-    }
-    if (!np.same) {
-      // neighbour-edge K correction, src/Impedance.cpp:301-324: three source
-      // edges x QuadratureGauss15, LKNeighborEdgeIntegrand over t[0].
-      d3 Ke[3][3];
-#pragma unroll
-      for (int e = 0; e < 3; e++)
-#pragma unroll
-        for (int i = 0; i < 3; i++) Ke[e][i] = {0, 0, 0};
-      const d3 nT = ld3(T.n);
-      for (int idx = lane; idx < 45; idx += 32) {
-        const int e = idx / 15, q = idx - e * 15;
-        const d3 v0 = e == 0 ? ld3(S.p0) : (e == 1 ? ld3(S.p1) : ld3(S.p2));
-        const d3 v1 = e == 0 ? ld3(S.v01) : (e == 1 ? ld3(S.v12) : ld3(S.v20));
-        const d3 v = v0 + c_line15[q][0] * v1;
-        const double w = c_line15[q][1];
-        double ISn1;
-        d3 IL1;
-        lk_edge_integral(T, v, ISn1, IL1);
-        const double h = dot(v - Pt, nT);
-        const d3 rho = v - h * nT;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-          if (i >= nht) break;
-          const d3 c = IL1 + ISn1 * (rho - ld3(T.hp0[i]));
-          if (e == 0) Ke[0][i] = Ke[0][i] + w * c;
-          else if (e == 1) Ke[1][i] = Ke[1][i] + w * c;
-          else Ke[2][i] = Ke[2][i] + w * c;
-        }
-      }
-#pragma unroll
-      for (int e = 0; e < 3; e++)
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-          Ke[e][i].x = warp_sum(Ke[e][i].x);
-          Ke[e][i].y = warp_sum(Ke[e][i].y);
-          Ke[e][i].z = warp_sum(Ke[e][i].z);
-        }
-      const double c = 0.125 * T.Ai * S.Ai;
-      const d3 m01 = ld3(S.m01), m12 = ld3(S.m12), m20 = ld3(S.m20);
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-          if (i >= nht || j >= nhs) continue;
-          const d3 v = ld3(T.hp0[i]) - ld3(S.hp0[j]);
-          K[i * 3 + j].r += c * (dot(cross(v, m01), Ke[0][i]) / S.nv01i + dot(cross(v, m12), Ke[1][i]) / S.nv12i +
-                                 dot(cross(v, m20), Ke[2][i]) / S.nv20i);
-        }
-    }
-    if (lane < nht * nhs) {
-      const int i = lane / nhs, j = lane - (lane / nhs) * nhs;
-      z1 Lv = {0, 0}, Kv = {0, 0};
-#pragma unroll
-      for (int k = 0; k < 9; k++)
-        if (k == i * 3 + j) { Lv = L[k]; Kv = K[k]; }
-      const double c = scatter_coef(T, i, S, j);
-      store_block(H, ntr, T.hrwg[i], T.hneg[i], S.hrwg[j], S.hneg[j], zscale(c, Lv), zscale(c, Kv));
-    }
-    __syncwarp();
+    near_pair_fp64(tk.T, tk.S, tk.near, u - tk.near0, s_g[wid], tk.H, tk.ntr, s_nodes[wid], lane);
   }
 }
 
@@ -1543,80 +1521,106 @@ int load_tables(bemgpu_ctx_s *ctx) {
 
 }  // namespace
 
-int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s, const bemgpu_green_t *g,
-                   const bemgpu_options_t *opt, int precision, HalfPairBlock *H, cudaStream_t stream,
-                   int64_t *n_near, int64_t *n_far) {
+int bem_fill_group(bemgpu_ctx_s *ctx, FillJob *jobs, int njobs, const bemgpu_options_t *opt, int precision,
+                   cudaStream_t stream) {
+  if (njobs < 1) return BEMGPU_OK;
   int rc = load_tables(ctx);
   if (rc) return rc;
-  const NearList *nl = bem_near_list(ctx, t, s);
-  if (!nl) return bem_fail(ctx, BEMGPU_ERR_OOM, "near list allocation failed");
-  GreenDev gd = to_dev(g);
-  FarOpts fo = {opt->farThresh6, opt->farThresh10, opt->farThresh15, opt->farThresh21};
   const int mode = precision == BEMGPU_PREC_MIXED ? FILL_FP32_FAR : precision == BEMGPU_PREC_MIXED_LA ? FILL_DF : FILL_FP64;
+  const FarOpts fo = {opt->farThresh6, opt->farThresh10, opt->farThresh15, opt->farThresh21};
   const int fr = ctx->tune.far_rows;
-  dim3 blk(32, fr);
-  dim3 grd((s->ntri + 31) / 32, (t->ntri + fr - 1) / fr);
-  double far_flops = 0, far_bytes = 0, near_flops = 0, near_bytes = 0;
-  if (ctx->prof) {
-    const int64_t *fc = bem_far_rule_counts(ctx, t, s, opt);
-    const int P[5] = {6, 10, 15, 21, 36};
-    int64_t nfar = 0;
-    for (int k = 0; k < 5; k++) { far_flops += fc[k] * bem_far_pair_flops(P[k]); nfar += fc[k]; }
-    // half-pair products written: 9 per pair on average (nh_t * nh_s)
-    far_bytes = (double)nfar * 9.0 * BEM_HALFPAIR_BYTES_FP64;
-    near_flops = (double)nl->n * bem_near_pair_flops(true);
-    near_bytes = (double)nl->n * 9.0 * BEM_HALFPAIR_BYTES_FP64;
+  std::vector<FillTask> tasks(njobs);
+  std::vector<const NearList *> lists(njobs);
+  size_t ndf = 0;
+  for (int i = 0; i < njobs; i++) {
+    lists[i] = bem_near_list(ctx, jobs[i].t, jobs[i].s);
+    if (!lists[i]) return bem_fail(ctx, BEMGPU_ERR_OOM, "near list allocation failed");
+    ndf += (size_t)jobs[i].t->ntri + jobs[i].s->ntri;
   }
-  {
-    ProfScope ps(ctx, BEMGPU_K_FILL_FAR, stream, far_flops, far_bytes);
-    TriDF *tdf = nullptr, *sdf = nullptr;
-    if (mode == FILL_DF) {
-      tdf = (TriDF *)bem_workspace(ctx, "fill_tdf", sizeof(TriDF) * (size_t)t->ntri);
-      sdf = (TriDF *)bem_workspace(ctx, "fill_sdf", sizeof(TriDF) * (size_t)s->ntri);
-      if (!tdf || !sdf) return bem_fail(ctx, BEMGPU_ERR_OOM, "fill: double-float records");
-      tri_df_kernel<<<(t->ntri + 127) / 128, 128, 0, stream>>>(t->d_rec, t->ntri, tdf);
-      tri_df_kernel<<<(s->ntri + 127) / 128, 128, 0, stream>>>(s->d_rec, s->ntri, sdf);
+  TriDF *df = nullptr;
+  if (mode == FILL_DF) {
+    df = (TriDF *)bem_workspace(ctx, "fill_tdf", sizeof(TriDF) * ndf);
+    if (!df) return bem_fail(ctx, BEMGPU_ERR_OOM, "fill: double-float records");
+  }
+  FillTask *dtasks = (FillTask *)bem_workspace(ctx, "fill_tasks", sizeof(FillTask) * (size_t)njobs);
+  if (!dtasks) return bem_fail(ctx, BEMGPU_ERR_OOM, "fill: task table");
+  double far_flops = 0, far_bytes = 0, near_flops = 0, near_bytes = 0;
+  int64_t far_tiles = 0, near_units = 0;
+  size_t dfo = 0;
+  for (int i = 0; i < njobs; i++) {
+    const bemgpu_tree_s *t = jobs[i].t, *s = jobs[i].s;
+    FillTask &tk = tasks[i];
+    tk.T = t->d_rec;
+    tk.S = s->d_rec;
+    tk.TD = tk.SD = nullptr;
+    if (df) {
+      tk.TD = df + dfo;
+      tk.SD = df + dfo + t->ntri;
+      tri_df_kernel<<<(t->ntri + 127) / 128, 128, 0, stream>>>(t->d_rec, t->ntri, df + dfo);
+      tri_df_kernel<<<(s->ntri + 127) / 128, 128, 0, stream>>>(s->d_rec, s->ntri, df + dfo + t->ntri);
       ctx->launches += 2;
+      dfo += (size_t)t->ntri + s->ntri;
     }
-    far_pairs_kernel<<<grd, blk, 0, stream>>>(t->d_rec, t->ntri, s->d_rec, s->ntri, gd, fo, H, t->nrwg, mode, tdf,
-                                              sdf);
+    tk.near = lists[i]->d;
+    tk.nnear = lists[i]->n;
+    tk.H = jobs[i].H;
+    tk.ntT = t->ntri;
+    tk.ntS = s->ntri;
+    tk.ntr = t->nrwg;
+    tk.far_tx = (s->ntri + 31) / 32;
+    tk.far0 = far_tiles;
+    far_tiles += (int64_t)tk.far_tx * ((t->ntri + fr - 1) / fr);
+    tk.near0 = near_units;
+    near_units += mode == FILL_DF ? (tk.nnear + 1) / 2 : tk.nnear;  // the df kernel works pair couples
+    tk.g = to_dev(&jobs[i].g);
+    jobs[i].near = tk.nnear;
+    jobs[i].far = (int64_t)t->ntri * s->ntri - tk.nnear;
+    if (ctx->prof) {
+      const int64_t *fc = bem_far_rule_counts(ctx, t, s, opt);
+      const int P[5] = {6, 10, 15, 21, 36};
+      int64_t nfar = 0;
+      for (int k = 0; k < 5; k++) { far_flops += fc[k] * bem_far_pair_flops(P[k]); nfar += fc[k]; }
+      // half-pair products written: 9 per pair on average (nh_t * nh_s)
+      far_bytes += (double)nfar * 9.0 * BEM_HALFPAIR_BYTES_FP64;
+      near_flops += (double)tk.nnear * bem_near_pair_flops(true);
+      near_bytes += (double)tk.nnear * 9.0 * BEM_HALFPAIR_BYTES_FP64;
+    }
+  }
+  // the table is copied from this call's host vector before the call returns
+  BEM_CUDA_TRY(ctx, cudaMemcpyAsync(dtasks, tasks.data(), sizeof(FillTask) * (size_t)njobs, cudaMemcpyHostToDevice,
+                                    stream));
+  if (far_tiles > 0) {
+    if (far_tiles > 0x7fffffffll) return bem_fail(ctx, BEMGPU_ERR_ARG, "fill: %lld far tiles", (long long)far_tiles);
+    ProfScope ps(ctx, BEMGPU_K_FILL_FAR, stream, far_flops, far_bytes);
+    far_pairs_group_kernel<<<(unsigned)far_tiles, dim3(32, fr), 0, stream>>>(dtasks, njobs, fo, mode);
     ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
-  if (nl->n > 0) {
-    const int per_block = mode == FILL_DF ? 2 * NEAR_WARPS : NEAR_WARPS;  // the df kernel takes two pairs per warp
-    int64_t blocks = (nl->n + per_block - 1) / per_block;
-    int nb = (int)std::min<int64_t>(blocks, (int64_t)ctx->num_sms * 16);
+  if (near_units > 0) {
+    const int nb = (int)std::min<int64_t>((near_units + NEAR_WARPS - 1) / NEAR_WARPS, (int64_t)ctx->num_sms * 16);
     ProfScope ps(ctx, BEMGPU_K_FILL_NEAR, stream, near_flops, near_bytes);
-    if (mode == FILL_DF) {
-      // chunks of pairs: inner moments into the scratch, then the outer part
-      const int64_t chunk = std::min<int64_t>(nl->n, NEAR_MOM_CHUNK);
-      float *mom = (float *)bem_workspace(ctx, "fill_near_mom",
-                                          sizeof(float) * NEAR_MOM_FLOATS * (size_t)chunk * BEMGPU_TRI_RULE105_N);
-      if (!mom) return bem_fail(ctx, BEMGPU_ERR_OOM, "fill: near-pair moment scratch");
-      for (int64_t c0 = 0; c0 < nl->n; c0 += chunk) {
-        const int64_t nc = std::min<int64_t>(chunk, nl->n - c0);
-        const int nbc = (int)std::min<int64_t>((nc + per_block - 1) / per_block, (int64_t)ctx->num_sms * 16);
-        const NearPair *lc = nl->d + c0;
-        if (ctx->tune.near_minb == 4)
-          near_moments_df_kernel<4><<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, lc, nc, gd, mom);
-        else if (ctx->tune.near_minb == 2)
-          near_moments_df_kernel<2><<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, lc, nc, gd, mom);
-        else
-          near_moments_df_kernel<3><<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, lc, nc, gd, mom);
-        near_outer_df_kernel<<<nbc, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d + c0, nc, gd, mom, H,
-                                                                   t->nrwg);
-        ctx->launches += 2;
-      }
-    } else {
-      near_pairs_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(t->d_rec, s->d_rec, nl->d, nl->n, gd, H, t->nrwg);
-      ctx->launches++;
-    }
+    if (mode == FILL_DF && ctx->tune.near_minb == 3)
+      near_pairs_df_group_kernel<3><<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+    else if (mode == FILL_DF && ctx->tune.near_minb == 4)
+      near_pairs_df_group_kernel<4><<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+    else if (mode == FILL_DF)
+      near_pairs_df_group_kernel<2><<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+    else
+      near_pairs_group_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+    ctx->launches++;
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
-  if (n_near) *n_near = nl->n;
-  if (n_far) *n_far = (int64_t)t->ntri * s->ntri - nl->n;
   return BEMGPU_OK;
+}
+
+int bem_fill_pairs(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s, const bemgpu_green_t *g,
+                   const bemgpu_options_t *opt, int precision, HalfPairBlock *H, cudaStream_t stream,
+                   int64_t *n_near, int64_t *n_far) {
+  FillJob job = {t, s, *g, H, 0, 0};
+  const int rc = bem_fill_group(ctx, &job, 1, opt, precision, stream);
+  if (n_near) *n_near = job.near;
+  if (n_far) *n_far = job.far;
+  return rc;
 }
 
 int bem_gather_z(bemgpu_ctx_s *ctx, const HalfPairBlock *H, int ntr, int nsr, const bemgpu_green_t *g, double *Z,

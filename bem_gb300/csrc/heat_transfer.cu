@@ -212,10 +212,19 @@ extern "C" int64_t bemgpu_ctx_solve_footprint(bemgpu_ctx_t ctx, int nrwg_s, int 
   return (int64_t)(fill_phase_bytes(nrwg_s, nrwg_t) + solve_phase_bytes(nrwg_s, nrwg_t, precision, ctx->solver));
 }
 
-extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
-                                    const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
-                                    double *P_out, bemgpu_solve_info_t *info) {
-  if (!ctx || !top || !s || !t || !req || !P_out) return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: null argument");
+namespace {
+
+// One request's sizes and Green's functions (GreensFunction::init of the
+// exterior and the two bodies, src/HeatTransfer.cpp:10-24).
+struct ReqSetup {
+  int Ns, Nt, N, n, ns2, nt2;
+  double omega;
+  bemgpu_green_t gext, g1, g2;
+};
+
+int setup_request(bemgpu_ctx_s *ctx, const bemgpu_tree_s *top, const bemgpu_tree_s *s, const bemgpu_tree_s *t,
+                  const bemgpu_solve_req_t *req, int precision, ReqSetup &r) {
+  if (!top || !s || !t || !req) return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: null argument");
   if (top->geom != s->geom || top->geom != t->geom)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: trees must share one geometry");
   if (top->geom->ctx->device != ctx->device)
@@ -225,64 +234,32 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: size(top) != size(s) + size(t)");
   if (precision != BEMGPU_PREC_FP64 && precision != BEMGPU_PREC_MIXED && precision != BEMGPU_PREC_MIXED_LA)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: unknown precision %d", precision);
-  const int fill_prec = precision;  // FP64, FP32 far pairs, or double-float (fill.cu)
-  bemgpu_options_t o;
-  if (opt) o = *opt; else bemgpu_options_default(&o);
-  std::lock_guard<std::mutex> lk(ctx->mu);
-  cudaSetDevice(ctx->device);
-  cudaStream_t st = ctx->stream;
+  r.Ns = s->nrwg;
+  r.Nt = t->nrwg;
+  r.N = r.Ns + r.Nt;
+  r.n = 2 * r.N;
+  r.ns2 = 2 * r.Ns;
+  r.nt2 = 2 * r.Nt;
+  r.omega = bemgpu_dimensionless_omega(req->a, req->eV);
+  const double om[2] = {r.omega, 0.0}, one_c[2] = {1.0, 0.0};
+  bemgpu_green_init(one_c, one_c, om, 1, &r.gext);
+  bemgpu_green_init(req->eps1, req->mu1, om, 0, &r.g1);
+  bemgpu_green_init(req->eps2, req->mu2, om, 0, &r.g2);
+  return BEMGPU_OK;
+}
 
-  const int Ns = s->nrwg, Nt = t->nrwg, N = Ns + Nt;
-  const int n = 2 * N, ns2 = 2 * Ns, nt2 = 2 * Nt;
-  const double omega = bemgpu_dimensionless_omega(req->a, req->eV);
-  const double om[2] = {omega, 0.0}, one_c[2] = {1.0, 0.0};
-  bemgpu_green_t gext, g1, g2;
-  bemgpu_green_init(one_c, one_c, om, 1, &gext);
-  bemgpu_green_init(req->eps1, req->mu1, om, 0, &g1);
-  bemgpu_green_init(req->eps2, req->mu2, om, 0, &g2);
-
-  HalfPairBlock *He = (HalfPairBlock *)bem_workspace(ctx, "Hext", sizeof(HalfPairBlock) * (size_t)N * N);
-  HalfPairBlock *H1 = (HalfPairBlock *)bem_workspace(ctx, "Hint1", sizeof(HalfPairBlock) * (size_t)Ns * Ns);
-  HalfPairBlock *H2 = (HalfPairBlock *)bem_workspace(ctx, "Hint2", sizeof(HalfPairBlock) * (size_t)Nt * Nt);
-  double *W = (double *)bem_workspace(ctx, "W", sizeof(double) * 2 * (size_t)n * n);
-  double *G1 = (double *)bem_workspace(ctx, "G1", sizeof(double) * 2 * (size_t)ns2 * ns2);
-  double *G2 = (double *)bem_workspace(ctx, "G2", sizeof(double) * 2 * (size_t)nt2 * nt2);
-  if (!He || !H1 || !H2 || !W || !G1 || !G2)
-    return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
-
+// The solve after W, G1, G2 are gathered: the mixed path (pre: its complex64
+// LU done by a batch) or the plain FP64 path, then P.  ev[1..5] are used.
+int finish_request(bemgpu_ctx_s *ctx, const ReqSetup &r, const bemgpu_solve_req_t *req, double *W, double *G1,
+                   double *G2, int precision, cudaStream_t st, const MixedLU *pre, double *P_out,
+                   bemgpu_solve_info_t *info) {
   cudaEvent_t *ev = ctx->ev;
-  cudaEventRecord(ev[0], st);
-  int64_t near1 = 0, far1 = 0, near2 = 0, far2 = 0, near3 = 0, far3 = 0;
-  int rc = bem_fill_pairs(ctx, top, top, &gext, &o, fill_prec, He, st, &near1, &far1);
-  if (!rc) rc = bem_fill_pairs(ctx, s, s, &g1, &o, fill_prec, H1, st, &near2, &far2);
-  if (!rc) rc = bem_fill_pairs(ctx, t, t, &g2, &o, fill_prec, H2, st, &near3, &far3);
-  if (!rc)
-    rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &gext, &g1, &g2, W, n, G1, ns2, G2, nt2, st,
-                      fill_prec == BEMGPU_PREC_MIXED_LA);
-  if (rc) return rc;
-  cudaEventRecord(ev[7], st);
-  {
-    // The half-pair blocks are dead once W, G1, G2 are gathered.  When the
-    // solve phase would not fit beside them, give them back first (large
-    // solves); otherwise keep them for the next request of this size.
-    size_t fr = 0, tot = 0;
-    cudaMemGetInfo(&fr, &tot);
-    const size_t held = bem_workspace_bytes(ctx), need = solve_phase_bytes(Ns, Nt, precision, ctx->solver);
-    const size_t fill = fill_phase_bytes(Ns, Nt);
-    // solve-phase bytes not yet held (what the context holds beyond the fill
-    // buffers is solve-phase workspace of an earlier request)
-    const size_t missing = need - std::min(need, held > fill ? held - fill : (size_t)0);
-    if ((double)fr < 1.05 * (double)missing + (double)(1u << 30)) {
-      bem_workspace_release(ctx, "Hext");
-      bem_workspace_release(ctx, "Hint1");
-      bem_workspace_release(ctx, "Hint2");
-    }
-  }
+  const int n = r.n, ns2 = r.ns2, nt2 = r.nt2;
   if (precision != BEMGPU_PREC_FP64) {
     bemgpu_solve_info_t mi;
     memset(&mi, 0, sizeof mi);
     double S[2] = {0, 0};
-    rc = bem_mixed_solve(ctx, W, n, ns2, G1, G2, st, S, &mi);
+    int rc = bem_mixed_solve(ctx, W, n, ns2, G1, G2, st, S, &mi, pre);
     if (rc == BEM_SOLVE_ON_FP64_PATH) {
       // the FP64-class refinement stalled above the fallback tolerance: W is
       // as filled, solve it on the plain FP64 path (FP64 LU, no refinement);
@@ -300,32 +277,198 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
       mi.ms_trace = elapsed(ev[3], ev[4]);
     }
     if (rc && rc != BEMGPU_ERR_NO_CONVERGE) return rc;
-    *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
+    *P_out = S[0] * (bemgpu_theta(r.omega, req->T1) - bemgpu_theta(r.omega, req->T2));
     if (info) {
+      const double ms_fill = info->ms_fill;
+      const int64_t pn = info->pairs_near, pf = info->pairs_far_fp64;
       *info = mi;
-      info->ms_fill = elapsed(ev[0], ev[7]);
+      info->ms_fill = ms_fill;
+      info->pairs_near = pn;
+      info->pairs_far_fp64 = pf;
       info->S_re = S[0];
       info->S_im = S[1];
-      info->pairs_near = near1 + near2 + near3;
-      info->pairs_far_fp64 = far1 + far2 + far3;
     }
     return rc;
   }
   double S[2];
   cudaEventRecord(ev[1], st);
-  rc = fp64_path_solve(ctx, W, n, ns2, G1, G2, st, S, ev);
+  int rc = fp64_path_solve(ctx, W, n, ns2, G1, G2, st, S, ev);
   if (rc) return rc;
-  *P_out = S[0] * (bemgpu_theta(omega, req->T1) - bemgpu_theta(omega, req->T2));
+  *P_out = S[0] * (bemgpu_theta(r.omega, req->T1) - bemgpu_theta(r.omega, req->T2));
   if (info) {
-    memset(info, 0, sizeof *info);
-    info->ms_fill = elapsed(ev[0], ev[7]);
     info->ms_lu = elapsed(ev[1], ev[2]);
     info->ms_solve = elapsed(ev[2], ev[3]);
     info->ms_trace = elapsed(ev[3], ev[4]);
     info->S_re = S[0];
     info->S_im = S[1];
-    info->pairs_near = near1 + near2 + near3;
-    info->pairs_far_fp64 = far1 + far2 + far3;
   }
   return BEMGPU_OK;
+}
+
+// Gives back the named half-pair blocks when the solve phase (`need` bytes)
+// would not fit beside what the context holds (large solves).
+void release_fill_if_short(bemgpu_ctx_s *ctx, size_t need, size_t fill, std::initializer_list<const char *> names) {
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  const size_t held = bem_workspace_bytes(ctx);
+  // solve-phase bytes not yet held (what the context holds beyond the fill
+  // buffers is solve-phase workspace of an earlier request)
+  const size_t missing = need - std::min(need, held > fill ? held - fill : (size_t)0);
+  if ((double)fr < 1.05 * (double)missing + (double)(1u << 30))
+    for (const char *nm : names) bem_workspace_release(ctx, nm);
+}
+
+}  // namespace
+
+extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, bemgpu_tree_t t,
+                                    const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
+                                    double *P_out, bemgpu_solve_info_t *info) {
+  if (!ctx || !P_out) return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer: null argument");
+  ReqSetup r;
+  int rc = setup_request(ctx, top, s, t, req, precision, r);
+  if (rc) return rc;
+  bemgpu_options_t o;
+  if (opt) o = *opt; else bemgpu_options_default(&o);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const int N = r.N, Ns = r.Ns, Nt = r.Nt, n = r.n, ns2 = r.ns2, nt2 = r.nt2;
+  HalfPairBlock *He = (HalfPairBlock *)bem_workspace(ctx, "Hext", sizeof(HalfPairBlock) * (size_t)N * N);
+  HalfPairBlock *H1 = (HalfPairBlock *)bem_workspace(ctx, "Hint1", sizeof(HalfPairBlock) * (size_t)Ns * Ns);
+  HalfPairBlock *H2 = (HalfPairBlock *)bem_workspace(ctx, "Hint2", sizeof(HalfPairBlock) * (size_t)Nt * Nt);
+  double *W = (double *)bem_workspace(ctx, "W", sizeof(double) * 2 * (size_t)n * n);
+  double *G1 = (double *)bem_workspace(ctx, "G1", sizeof(double) * 2 * (size_t)ns2 * ns2);
+  double *G2 = (double *)bem_workspace(ctx, "G2", sizeof(double) * 2 * (size_t)nt2 * nt2);
+  if (!He || !H1 || !H2 || !W || !G1 || !G2)
+    return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer: workspace allocation failed (n=%d)", n);
+  cudaEvent_t *ev = ctx->ev;
+  cudaEventRecord(ev[0], st);
+  // the three Zts of CalcHeatTransfer (src/HeatTransfer.cpp:26-29) in one
+  // far-pair and one near-pair launch
+  FillJob jobs[3] = {{top, top, r.gext, He, 0, 0}, {s, s, r.g1, H1, 0, 0}, {t, t, r.g2, H2, 0, 0}};
+  rc = bem_fill_group(ctx, jobs, 3, &o, precision, st);
+  if (!rc)
+    rc = bem_gather_w(ctx, He, H1, H2, Ns, Nt, &r.gext, &r.g1, &r.g2, W, n, G1, ns2, G2, nt2, st,
+                      precision == BEMGPU_PREC_MIXED_LA);
+  if (rc) return rc;
+  cudaEventRecord(ev[7], st);
+  // The half-pair blocks are dead once W, G1, G2 are gathered.  When the
+  // solve phase would not fit beside them, give them back first (large
+  // solves); otherwise keep them for the next request of this size.
+  release_fill_if_short(ctx, solve_phase_bytes(Ns, Nt, precision, ctx->solver), fill_phase_bytes(Ns, Nt),
+                        {"Hext", "Hint1", "Hint2"});
+  bemgpu_solve_info_t mine;
+  bemgpu_solve_info_t *pi = info ? info : &mine;
+  memset(pi, 0, sizeof *pi);
+  pi->ms_fill = elapsed(ev[0], ev[7]);
+  pi->pairs_near = jobs[0].near + jobs[1].near + jobs[2].near;
+  pi->pairs_far_fp64 = jobs[0].far + jobs[1].far + jobs[2].far;
+  return finish_request(ctx, r, req, W, G1, G2, precision, st, nullptr, P_out, pi);
+}
+
+extern "C" int64_t bemgpu_batch_footprint(int nreq, int nrwg_s, int nrwg_t, int precision) {
+  if (nreq < 1 || nrwg_s < 1 || nrwg_t < 1) return BEMGPU_ERR_ARG;
+  const size_t n = 2 * ((size_t)nrwg_s + nrwg_t);
+  // every request's fill blocks and matrices, one solve phase, and the
+  // complex64 factors of the batched LU beyond the one the solve holds
+  size_t b = (size_t)nreq * fill_phase_bytes(nrwg_s, nrwg_t) + solve_phase_bytes(nrwg_s, nrwg_t, precision, 0);
+  if (precision != BEMGPU_PREC_FP64) b += (size_t)nreq * (8 * n * n + 4 * n + 16);
+  return (int64_t)b;
+}
+
+extern "C" int bemgpu_heat_transfer_batch(bemgpu_ctx_t ctx, int nreq, const bemgpu_tree_t *tops,
+                                          const bemgpu_tree_t *ss, const bemgpu_tree_t *ts,
+                                          const bemgpu_solve_req_t *reqs, const bemgpu_options_t *opt, int precision,
+                                          double *P_out, bemgpu_solve_info_t *infos, int *status) {
+  if (!ctx || nreq < 1 || !tops || !ss || !ts || !reqs || !P_out || !status)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer_batch: null argument or empty batch");
+  if (nreq > BEM_MAX_BATCH)
+    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer_batch: %d requests, at most %d", nreq, BEM_MAX_BATCH);
+  std::vector<ReqSetup> r(nreq);
+  for (int i = 0; i < nreq; i++) {
+    const int rc = setup_request(ctx, tops[i], ss[i], ts[i], &reqs[i], precision, r[i]);
+    if (rc) return rc;
+  }
+  bemgpu_options_t o;
+  if (opt) o = *opt; else bemgpu_options_default(&o);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  // every request's half-pair blocks and matrices, side by side
+  std::vector<size_t> hoff(nreq + 1, 0), moff(nreq + 1, 0);
+  bool same = true;
+  for (int i = 0; i < nreq; i++) {
+    const size_t N = r[i].N, Ns = r[i].Ns, Nt = r[i].Nt;
+    hoff[i + 1] = hoff[i] + N * N + Ns * Ns + Nt * Nt;
+    moff[i + 1] = moff[i] + 2 * ((size_t)r[i].n * r[i].n + (size_t)r[i].ns2 * r[i].ns2 + (size_t)r[i].nt2 * r[i].nt2);
+    same = same && r[i].Ns == r[0].Ns && r[i].Nt == r[0].Nt;
+  }
+  HalfPairBlock *H = (HalfPairBlock *)bem_workspace(ctx, "bH", sizeof(HalfPairBlock) * hoff[nreq]);
+  double *M = (double *)bem_workspace(ctx, "bM", sizeof(double) * moff[nreq]);
+  if (!H || !M) return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer_batch: workspace allocation failed");
+  std::vector<FillJob> jobs(3 * (size_t)nreq);
+  std::vector<double *> W(nreq), G1(nreq), G2(nreq);
+  for (int i = 0; i < nreq; i++) {
+    const size_t N = r[i].N, Ns = r[i].Ns;
+    HalfPairBlock *He = H + hoff[i], *H1 = He + N * N, *H2 = H1 + Ns * Ns;
+    jobs[3 * i] = {tops[i], tops[i], r[i].gext, He, 0, 0};
+    jobs[3 * i + 1] = {ss[i], ss[i], r[i].g1, H1, 0, 0};
+    jobs[3 * i + 2] = {ts[i], ts[i], r[i].g2, H2, 0, 0};
+    W[i] = M + moff[i];
+    G1[i] = W[i] + 2 * (size_t)r[i].n * r[i].n;
+    G2[i] = G1[i] + 2 * (size_t)r[i].ns2 * r[i].ns2;
+  }
+  cudaEvent_t *ev = ctx->ev;
+  cudaEventRecord(ev[0], st);
+  // every request's three Zts in one far-pair and one near-pair launch
+  int rc = bem_fill_group(ctx, jobs.data(), 3 * nreq, &o, precision, st);
+  for (int i = 0; i < nreq && !rc; i++) {
+    const HalfPairBlock *He = jobs[3 * i].H, *H1 = jobs[3 * i + 1].H, *H2 = jobs[3 * i + 2].H;
+    rc = bem_gather_w(ctx, He, H1, H2, r[i].Ns, r[i].Nt, &r[i].gext, &r[i].g1, &r[i].g2, W[i], r[i].n, G1[i],
+                      r[i].ns2, G2[i], r[i].nt2, st, precision == BEMGPU_PREC_MIXED_LA);
+  }
+  if (rc) return rc;
+  cudaEventRecord(ev[7], st);
+  const float fill_ms = elapsed(ev[0], ev[7]);
+  {
+    size_t need = 0, fill = 0;
+    for (int i = 0; i < nreq; i++) {
+      need = std::max(need, solve_phase_bytes(r[i].Ns, r[i].Nt, precision, ctx->solver));
+      fill += fill_phase_bytes(r[i].Ns, r[i].Nt);
+    }
+    release_fill_if_short(ctx, need, fill, {"bH"});
+  }
+  // the complex64 LU of equal-size requests together: their panels in one
+  // cooperative launch per block column
+  std::vector<MixedLU> pre;
+  if (precision != BEMGPU_PREC_FP64 && ctx->solver != 2 && same && nreq > 1) {
+    const int n = r[0].n;
+    const size_t nn = (size_t)n * n;
+    float *W32 = (float *)bem_workspace(ctx, "bW32", 8 * nn * nreq);
+    int *piv = (int *)bem_workspace(ctx, "bipiv", 4 * (size_t)n * nreq);
+    int *inf = (int *)bem_workspace(ctx, "binfo", 4 * (size_t)nreq);
+    if (!W32 || !piv || !inf) return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer_batch: LU workspace");
+    for (int i = 0; i < nreq; i++) bem_c128_to_c64(ctx, W[i], n, W32 + 2 * nn * i, st);
+    rc = bem_cgetrf_batch(ctx, W32, (int64_t)(2 * nn), nreq, n, n, piv, inf, st);
+    if (rc) return rc;
+    for (int i = 0; i < nreq; i++) pre.push_back({W32 + 2 * nn * i, piv + (size_t)n * i, inf + i});
+  }
+  int first = BEMGPU_OK;
+  for (int i = 0; i < nreq; i++) {
+    bemgpu_solve_info_t mine;
+    bemgpu_solve_info_t *pi = infos ? &infos[i] : &mine;
+    memset(pi, 0, sizeof *pi);
+    pi->ms_fill = fill_ms / nreq;  // the batch's fill, shared
+    pi->pairs_near = jobs[3 * i].near + jobs[3 * i + 1].near + jobs[3 * i + 2].near;
+    pi->pairs_far_fp64 = jobs[3 * i].far + jobs[3 * i + 1].far + jobs[3 * i + 2].far;
+    status[i] = finish_request(ctx, r[i], &reqs[i], W[i], G1[i], G2[i], precision, st,
+                               pre.empty() ? nullptr : &pre[i], &P_out[i], pi);
+    if (status[i] != BEMGPU_OK && first == BEMGPU_OK) first = status[i];
+    if (status[i] == BEMGPU_ERR_TIMEOUT) {
+      // a wait ran out: the device state of the batch is not to be trusted
+      for (int j = i + 1; j < nreq; j++) status[j] = BEMGPU_ERR_TIMEOUT;
+      return first;
+    }
+  }
+  return first;
 }

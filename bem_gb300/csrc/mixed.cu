@@ -258,6 +258,30 @@ int spectral_trace(bemgpu_ctx_s *ctx, MixedBufs &b, int n, int ns2, int nt2, cud
 
 namespace {
 
+// Sizes a refinement correction dY (just quantized to DELTA_SLICES slices,
+// op = its operand) against the iterate (eb_y: exponent field of Y's largest
+// entry) and sets how the next products use it.  A small correction (|dY| <=
+// 2^-12 |Y|): the residual update -W dY takes levels 0..2 of the slice
+// products (error 2^-24 |W||dY| <= 2^-36 |W||Y|) and the trace is updated by
+// H1 dX and H2 dX^H.  A large one (a slowly contracting refinement): the
+// residual update takes every product of W's 5 slices and dY's 3 exact ones
+// (2^-40 |W||dY|), and the trace is formed again from the whole iterate,
+// since an incremental update carries 2^-24 of |dX| into S and S may be a
+// small difference of its terms.  Synchronizes the stream (reads dY's exponent).
+bool correction_is_small(bemgpu_ctx_s *ctx, ExactOperand &op, unsigned eb_y, cudaStream_t st) {
+  unsigned eb_dy = 0;
+  if (cudaMemcpyAsync(&eb_dy, op.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    cudaGetLastError();
+    op.exact = true;
+    return false;
+  }
+  (void)ctx;
+  const bool small = (int)eb_dy - (int)eb_y <= -12;
+  op.exact = !small;
+  return small;
+}
+
 // The FP64-class solve: W (already sliced into b.opW) is factored in place by
 // the tensor-core LU of FP64 accuracy (bem_zgetrf_exact), Y0 = W^-1 E_t by its
 // blocked solve, then the same refinement and trace as the complex64 path with
@@ -296,12 +320,7 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
       if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
-      // as in the complex64 refinement: every slice product while the
-      // correction is above 2^-12 of the iterate, levels 0..2 below
-      unsigned eb_dy = 0;
-      BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_dy, opDY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-      BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      opDY.exact = (int)eb_dy - (int)eb_y > -12;
+      // as in the complex64 refinement (exact products for a large correction)
       rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opDY, b.R64, n, 1, st);
     }
     if (rc) return rc;
@@ -312,9 +331,10 @@ int fp64lu_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, MixedBufs &b, cud
     if (rc) return rc;
     add_fp64_kernel<<<gm, 256, 0, st>>>(b.Y, b.dY, n, n);
     ctx->launches++;
+    const bool small = correction_is_small(ctx, opDY, eb_y, st);
     Sprev[0] = S[0];
     Sprev[1] = S[1];
-    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, true);
+    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, small);
     if (rc) return rc;
     if (bem_tc_error(ctx, true))
       return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "FP64-class solve: a tensor-core pipeline wait ran out");
@@ -338,8 +358,16 @@ void bem_release_if_short(bemgpu_ctx_s *ctx, size_t need, std::initializer_list<
   for (const char *nm : names) bem_workspace_release(ctx, nm);
 }
 
+// W32 = fl32(W) for the batch driver (heat_transfer.cu): the conversion the
+// mixed solve does before its LU.
+void bem_c128_to_c64(bemgpu_ctx_s *ctx, const double *W, int n, float *W32, cudaStream_t st) {
+  const dim3 gn((n + 255) / 256, n);
+  c128_to_c64_kernel<<<gn, 256, 0, st>>>(W, n, W32, n, n, n);
+  ctx->launches++;
+}
+
 int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *G1, const double *G2,
-                    cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info) {
+                    cudaStream_t st, double S_out[2], bemgpu_solve_info_t *info, const MixedLU *pre) {
   if (!bem_exact_available())
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "mixed solve: tensor-map encoding (driver entry point) unavailable");
   const int nt2 = n - ns2;
@@ -348,8 +376,10 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   b.ntiles = ((ns2 + 31) / 32) * ((nt2 + 31) / 32);
   // the complex64 factors are not allocated when the context solves FP64-class only
   const bool c64 = ctx->solver != 2;
+  if (pre && !c64) return bem_fail(ctx, BEMGPU_ERR_ARG, "mixed solve: complex64 factors given to an FP64-class solve");
   if (c64) {
-    b.W32 = (float *)bem_workspace(ctx, "m_W32", 8 * nn);
+    // a batch's complex64 LU (bem_cgetrf_batch) arrives factored
+    b.W32 = pre ? pre->W32 : (float *)bem_workspace(ctx, "m_W32", 8 * nn);
     b.R32 = (float *)bem_workspace(ctx, "m_R32", 8 * nm);
     b.Linv = (float *)bem_workspace(ctx, "m_Linv", 8 * nn);
     b.Uinv = (float *)bem_workspace(ctx, "m_Uinv", 8 * nn);
@@ -364,8 +394,8 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   b.B1 = (double *)bem_workspace(ctx, "m_B1", 16 * st2);
   b.C = (double *)bem_workspace(ctx, "m_C", 16 * st2);
   b.partial = (double *)bem_workspace(ctx, "m_partial", 16 * (size_t)b.ntiles + 64);
-  b.ipiv = (int *)bem_workspace(ctx, "m_ipiv", 4 * (size_t)n);
-  b.info = (int *)bem_workspace(ctx, "m_info", 16);
+  b.ipiv = pre ? pre->ipiv : (int *)bem_workspace(ctx, "m_ipiv", 4 * (size_t)n);
+  b.info = pre ? pre->info : (int *)bem_workspace(ctx, "m_info", 16);
   const bool ok = (!c64 || (b.W32 && b.R32 && b.Linv && b.Uinv && b.T32)) && b.H1 && b.H2 && b.Y && b.dY && b.R64 &&
                   b.XH && b.B1 && b.C && b.partial && b.ipiv && b.info;
   if (!ok) return bem_fail(ctx, BEMGPU_ERR_OOM, "mixed solve: workspace allocation failed (n=%d)", n);
@@ -373,7 +403,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
   const dim3 gn((n + 255) / 256, n), gm((n + 255) / 256, nt2);
   {
     ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, (c64 ? 24.0 * nn : 0.0) + 48.0 * ((double)ns2 * ns2 + (double)nt2 * nt2));
-    if (c64) {
+    if (c64 && !pre) {
       c128_to_c64_kernel<<<gn, 256, 0, st>>>(W, n, b.W32, n, n, n);
       ctx->launches++;
     }
@@ -407,7 +437,7 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     if (err > 1e-6) return bem_fail(ctx, BEMGPU_ERR_NO_CONVERGE, "FP64-class solve: refinement stalled at %.2e", err);
     return BEMGPU_OK;
   }
-  rc = bem_cgetrf(ctx, b.W32, n, n, b.ipiv, b.info, st);
+  if (!pre) rc = bem_cgetrf(ctx, b.W32, n, n, b.ipiv, b.info, st);
   if (!rc) rc = bem_ctri_inverses(ctx, b.W32, n, n, b.Linv, b.Uinv, st);
   if (rc) return rc;
   cudaEventRecord(ev[2], st);
@@ -442,14 +472,8 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
       if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
-      // -W dY: all 12 slice products of W's 5 slices and the correction's 3
-      // exact ones (2^-40 of |W||dY|) while |dY| > 2^-12 |Y| (a slowly
-      // contracting refinement); below that, the 6 products of levels 0..2,
-      // whose error 2^-24 |W||dY| stays under 2^-36 |W||Y|, at half the cost
-      unsigned eb_dy = 0;
-      BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_dy, opDY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-      BEM_CUDA_TRY(ctx, cudaStreamSynchronize(st));
-      opDY.exact = (int)eb_dy - (int)eb_y > -12;
+      // -W dY of the last correction (its products chosen by its size,
+      // correction_is_small)
       rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opDY, b.R64, n, 1, st);
     }
     if (rc) return rc;
@@ -467,10 +491,11 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     if (rc) return rc;
     add_fp64_kernel<<<gm, 256, 0, st>>>(b.Y, b.dY, n, n);
     ctx->launches++;
+    const bool small = correction_is_small(ctx, opDY, eb_y, st);
     iters++;
     Sprev[0] = S[0];
     Sprev[1] = S[1];
-    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, iters > 1);
+    rc = spectral_trace(ctx, b, n, ns2, nt2, st, S, iters > 1 && small);
     if (rc) return rc;
     if (bem_tc_error(ctx, true))
       return bem_fail(ctx, BEMGPU_ERR_TIMEOUT, "mixed solve: a tensor-core pipeline wait ran out");

@@ -1,7 +1,7 @@
 """Autotuner of the hot path's launch shapes.
 
 The library exposes its launch-shape knobs per context (bemgpu_ctx_set_tuning,
-include/bemgpu.h): the register budget of the near-pair inner-moment kernel
+include/bemgpu.h): the register budget of the double-float near-pair kernel
 (CTAs per SM), the far-pair kernel's warps per CTA, and the rasterization band
 of the tensor-core products.  None changes a result; each changes how fast
 one kernel class runs on a given workload.  tune() times every candidate
@@ -29,7 +29,7 @@ KNOBS = {
     "far_rows": (_lib.TUNE_FAR_ROWS, (1, 2, 4, 8), ("fill_far",)),
     "raster": (_lib.TUNE_RASTER, (4, 8, 16), ("lu_gemm", "trsm", "solve_gemm", "trace", "refine_gemm")),
 }
-DEFAULTS = {"near_minb": 3, "far_rows": 4, "raster": 8}
+DEFAULTS = {"near_minb": 2, "far_rows": 4, "raster": 8}
 
 _lock = threading.Lock()
 

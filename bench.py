@@ -277,7 +277,7 @@ def run_ours(args, rank, world):
     a = 1e-6
     # requests go through the farm: `lanes` contexts, each on its own stream
     # and host thread, so consecutive solves overlap on the GPU
-    farm = api.Farm(args.lanes, dev)
+    farm = api.Farm(args.lanes, dev, batch=args.batch)
     lane_ctx = farm.lane_contexts()
     solver = {"escalate": 0, "c64": 1, "fp64class": 2}[args.solver]
     for c in lane_ctx:
@@ -591,7 +591,8 @@ def workload_config(args, n_unknowns, world):
         name = args.workload
     n_max = n_unknowns if isinstance(n_unknowns, int) else int(str(n_unknowns).split("-")[-1])
     return {"workload": name, "precision": args.precision, "N": n_unknowns, "parallelism": f"replicas x{world}",
-            "lanes": getattr(args, "lanes", 1), "solver": getattr(args, "solver", "escalate"),
+            "lanes": getattr(args, "lanes", 1), "batch": getattr(args, "batch", 1),
+            "solver": getattr(args, "solver", "escalate"),
             "l2": "inputs larger than L2 (W alone is %.0f MB)" % (n_max ** 2 * 16 / 1e6)}
 
 
@@ -803,6 +804,8 @@ def main():
     ap.add_argument("--workload", default="ico3", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lanes", type=int, default=4, help="farm lanes: solves in flight at once on the GPU")
+    ap.add_argument("--batch", type=int, default=1,
+                    help="continuous batching: queued requests of equal size a lane solves together")
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests of the Poisson-arrival serving measurement (0: skip)")
     ap.add_argument("--solver", default="escalate", choices=["escalate", "c64", "fp64class"],

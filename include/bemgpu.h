@@ -129,9 +129,9 @@ int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
 /* Launch-shape knobs of this context (no reference counterpart), set by the
  * project's autotuner (bem_gb300/tuning.py: it times each candidate on the
  * caller's workload and caches the best per GPU and size class).
- *   BEMGPU_TUNE_NEAR_MINB  CTAs per SM that the near-pair inner-moment kernel's
- *                          register budget allows: 2 (224 registers), 3 (168,
- *                          default) or 4 (128, some spilled);
+ *   BEMGPU_TUNE_NEAR_MINB  CTAs per SM that the double-float near-pair kernel's
+ *                          register budget allows: 2 (default), 3 (168
+ *                          registers) or 4 (128, some spilled);
  *   BEMGPU_TUNE_FAR_ROWS   warps per CTA of the far-pair kernel: 1, 2, 4 (default), 8;
  *   BEMGPU_TUNE_RASTER     M-tiles per rasterization band of the tensor-core
  *                          products: 1..64 (default 8).
@@ -287,6 +287,23 @@ int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_tree_t s, b
                          const bemgpu_solve_req_t *req, const bemgpu_options_t *opt, int precision,
                          double *P_out, bemgpu_solve_info_t *info);
 
+/* Several CalcHeatTransfer requests solved together (no counterpart in the
+ * reference, whose task farm solves one per process): request i is
+ * (tops[i], ss[i], ts[i], reqs[i]).  The three fills of every request run in
+ * one far-pair and one near-pair launch; the complex64 LU panels of requests
+ * of equal size (a frequency sweep of one geometry) run in one cooperative
+ * launch per block column; the rest is per request.  P_out[i] and infos[i]
+ * (infos may be NULL; its ms_fill is the batch's fill time / nreq) equal
+ * bemgpu_heat_transfer's for the same request bit for bit, and status[i] is
+ * its status.  Returns the first non-zero status (BEMGPU_OK when all
+ * succeeded).  At most 64 requests; the device memory it needs is
+ * bemgpu_batch_footprint's.  Synchronous. */
+int bemgpu_heat_transfer_batch(bemgpu_ctx_t ctx, int nreq, const bemgpu_tree_t *tops, const bemgpu_tree_t *ss,
+                               const bemgpu_tree_t *ts, const bemgpu_solve_req_t *reqs, const bemgpu_options_t *opt,
+                               int precision, double *P_out, bemgpu_solve_info_t *infos, int *status);
+/* Device bytes a batch of nreq equal-size requests needs at most. */
+int64_t bemgpu_batch_footprint(int nreq, int nrwg_s, int nrwg_t, int precision);
+
 /* ---- request farm ----
  * Replaces the reference's MPI task farm (src/transfer-mpi.cpp:25-190: a Master
  * queue of (a, gap, f, T1, T2) jobs, Servants that run CalcHeatTransfer and
@@ -299,6 +316,13 @@ int bemgpu_farm_create(int device, int lanes, bemgpu_farm_t *out);
  * waits for the running ones, and frees the lanes. */
 int bemgpu_farm_destroy(bemgpu_farm_t farm);
 int bemgpu_farm_lanes(bemgpu_farm_t farm);
+/* Continuous batching: a lane that takes a request also takes up to
+ * max_requests - 1 more queued requests of the same sizes, precision and
+ * options (in queue order) and solves them together with
+ * bemgpu_heat_transfer_batch, admitted by bemgpu_batch_footprint (a batch
+ * over the budget runs its first request alone).  Results are those of the
+ * requests solved one by one.  Default 1 (no batching); at most 64. */
+int bemgpu_farm_set_batch(bemgpu_farm_t farm, int max_requests);
 /* Device bytes the lanes may hold together (admission by footprint); the
  * default is 90 % of the memory free when the farm was created. */
 int bemgpu_farm_set_budget(bemgpu_farm_t farm, int64_t bytes);
