@@ -320,8 +320,10 @@ def CalcHeatTransferBatch(jobs, options: Options | None = None, precision: int =
     P = (ctypes.c_double * n)()
     si = (_lib.SolveInfo * n)()
     st = (ctypes.c_int * n)()
-    _lib.load().bemgpu_heat_transfer_batch(ctx.handle, n, tops, ss, ts, reqs, ctypes.byref(options._c()),
-                                           int(precision), P, si, st)
+    rc = _lib.load().bemgpu_heat_transfer_batch(ctx.handle, n, tops, ss, ts, reqs, ctypes.byref(options._c()),
+                                                int(precision), P, si, st)
+    if rc == _lib.ERR_ARG and all(st[i] == _lib.OK for i in range(n)):
+        _check(rc, ctx)
     for i in range(n):
         if not (st[i] == _lib.ERR_NO_CONVERGE and not strict) and st[i] != _lib.OK:
             _check(st[i], ctx)

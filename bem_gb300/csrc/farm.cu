@@ -203,10 +203,8 @@ void lane_main(bemgpu_farm_s *f, int lane) {
         ts[k] = jobs[k].t;
         reqs[k] = jobs[k].req;
       }
-      const int rc = bemgpu_heat_transfer_batch(ctx, nb, tops.data(), ss.data(), ts.data(), reqs.data(), &jobs[0].opt,
-                                                jobs[0].precision, P.data(), info.data(), rcs.data());
-      if (rc == BEMGPU_ERR_ARG || rc == BEMGPU_ERR_OOM)  // the batch as a whole did not start
-        for (int k = 0; k < nb; k++) rcs[k] = rc;
+      bemgpu_heat_transfer_batch(ctx, nb, tops.data(), ss.data(), ts.data(), reqs.data(), &jobs[0].opt,
+                                 jobs[0].precision, P.data(), info.data(), rcs.data());
     }
     const size_t held = (size_t)std::max<int64_t>(0, bemgpu_ctx_workspace_bytes(ctx));
     {

@@ -360,10 +360,11 @@ extern "C" int bemgpu_heat_transfer(bemgpu_ctx_t ctx, bemgpu_tree_t top, bemgpu_
   bemgpu_solve_info_t mine;
   bemgpu_solve_info_t *pi = info ? info : &mine;
   memset(pi, 0, sizeof *pi);
-  pi->ms_fill = elapsed(ev[0], ev[7]);
   pi->pairs_near = jobs[0].near + jobs[1].near + jobs[2].near;
   pi->pairs_far_fp64 = jobs[0].far + jobs[1].far + jobs[2].far;
-  return finish_request(ctx, r, req, W, G1, G2, precision, st, nullptr, P_out, pi);
+  rc = finish_request(ctx, r, req, W, G1, G2, precision, st, nullptr, P_out, pi);
+  pi->ms_fill = elapsed(ev[0], ev[7]);  // the solve has synchronised the stream
+  return rc;
 }
 
 extern "C" int64_t bemgpu_batch_footprint(int nreq, int nrwg_s, int nrwg_t, int precision) {
@@ -382,12 +383,17 @@ extern "C" int bemgpu_heat_transfer_batch(bemgpu_ctx_t ctx, int nreq, const bemg
                                           double *P_out, bemgpu_solve_info_t *infos, int *status) {
   if (!ctx || nreq < 1 || !tops || !ss || !ts || !reqs || !P_out || !status)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer_batch: null argument or empty batch");
+  // until a request has its own outcome, every status is the batch's
+  auto fail_all = [&](int rc) {
+    for (int i = 0; i < nreq; i++) status[i] = rc;
+    return rc;
+  };
   if (nreq > BEM_MAX_BATCH)
-    return bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer_batch: %d requests, at most %d", nreq, BEM_MAX_BATCH);
+    return fail_all(bem_fail(ctx, BEMGPU_ERR_ARG, "heat_transfer_batch: %d requests, at most %d", nreq, BEM_MAX_BATCH));
   std::vector<ReqSetup> r(nreq);
   for (int i = 0; i < nreq; i++) {
     const int rc = setup_request(ctx, tops[i], ss[i], ts[i], &reqs[i], precision, r[i]);
-    if (rc) return rc;
+    if (rc) return fail_all(rc);
   }
   bemgpu_options_t o;
   if (opt) o = *opt; else bemgpu_options_default(&o);
@@ -405,7 +411,7 @@ extern "C" int bemgpu_heat_transfer_batch(bemgpu_ctx_t ctx, int nreq, const bemg
   }
   HalfPairBlock *H = (HalfPairBlock *)bem_workspace(ctx, "bH", sizeof(HalfPairBlock) * hoff[nreq]);
   double *M = (double *)bem_workspace(ctx, "bM", sizeof(double) * moff[nreq]);
-  if (!H || !M) return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer_batch: workspace allocation failed");
+  if (!H || !M) return fail_all(bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer_batch: workspace allocation failed"));
   std::vector<FillJob> jobs(3 * (size_t)nreq);
   std::vector<double *> W(nreq), G1(nreq), G2(nreq);
   for (int i = 0; i < nreq; i++) {
@@ -427,8 +433,9 @@ extern "C" int bemgpu_heat_transfer_batch(bemgpu_ctx_t ctx, int nreq, const bemg
     rc = bem_gather_w(ctx, He, H1, H2, r[i].Ns, r[i].Nt, &r[i].gext, &r[i].g1, &r[i].g2, W[i], r[i].n, G1[i],
                       r[i].ns2, G2[i], r[i].nt2, st, precision == BEMGPU_PREC_MIXED_LA);
   }
-  if (rc) return rc;
+  if (rc) return fail_all(rc);
   cudaEventRecord(ev[7], st);
+  BEM_CUDA_TRY(ctx, cudaEventSynchronize(ev[7]));
   const float fill_ms = elapsed(ev[0], ev[7]);
   {
     size_t need = 0, fill = 0;
@@ -447,10 +454,10 @@ extern "C" int bemgpu_heat_transfer_batch(bemgpu_ctx_t ctx, int nreq, const bemg
     float *W32 = (float *)bem_workspace(ctx, "bW32", 8 * nn * nreq);
     int *piv = (int *)bem_workspace(ctx, "bipiv", 4 * (size_t)n * nreq);
     int *inf = (int *)bem_workspace(ctx, "binfo", 4 * (size_t)nreq);
-    if (!W32 || !piv || !inf) return bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer_batch: LU workspace");
+    if (!W32 || !piv || !inf) return fail_all(bem_fail(ctx, BEMGPU_ERR_OOM, "heat_transfer_batch: LU workspace"));
     for (int i = 0; i < nreq; i++) bem_c128_to_c64(ctx, W[i], n, W32 + 2 * nn * i, st);
     rc = bem_cgetrf_batch(ctx, W32, (int64_t)(2 * nn), nreq, n, n, piv, inf, st);
-    if (rc) return rc;
+    if (rc) return fail_all(rc);
     for (int i = 0; i < nreq; i++) pre.push_back({W32 + 2 * nn * i, piv + (size_t)n * i, inf + i});
   }
   int first = BEMGPU_OK;

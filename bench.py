@@ -55,11 +55,12 @@ WORKLOADS = {
     "ico3": dict(kind="ico", level=3, gaps=[0.02, 0.05, 0.1, 0.2, 0.5, 1.0], freqs=np.linspace(0.08, 0.13, 64)),
     "ico2": dict(kind="ico", level=2, gaps=[0.02, 0.05, 0.1, 0.2, 0.5, 1.0], freqs=np.linspace(0.08, 0.13, 64)),
     "cube4": dict(kind="cube", nsub=4, gaps=[0.1], freqs=np.linspace(0.08, 0.13, 20)),
-    # a tip over a plate: per request a cone (0.5 um base radius, 1 um high,
+    # a tip over a plate: per geometry a cone (0.5 um base radius, 1 um high,
     # hemispherical apex 50-200 nm) of 300-1500 RWG edges drawn from a seed, a
-    # 4 x 4 x 0.5 um plate of 1920 edges, gap log-uniform 10-1000 nm, frequency
-    # uniform 0.08-0.13 eV: requests of uneven N (4400-6800 unknowns)
-    "tip": dict(kind="tip", requests=64, seed=7),
+    # 4 x 4 x 0.5 um plate of 1920 edges, gap log-uniform 10-1000 nm, and a
+    # sweep of 64 frequencies uniform in 0.08-0.13 eV: 64 x 64 = 4096 solves of
+    # uneven N (4400-6800 unknowns); the steps walk each geometry's sweep in turn
+    "tip": dict(kind="tip", requests=64, seed=7, sweep=64),
     # two thin slabs facing each other across the gap (x is the 0.5 um side):
     # 2 x 35 x 35 squares per face, 8190 RWG edges each, N = 32760; W alone is
     # 17 GB in complex128
@@ -89,6 +90,13 @@ def tip_requests(wl):
         plate = mesh.Body.from_mesh(pv + np.array([0.0, 0.0, -gap - 0.25]), pt)
         out.append((mesh.Body.from_mesh(tv, tt), plate, float(rng.uniform(0.08, 0.13))))
     return out
+
+
+def tip_sweep(wl, i, eV0):
+    """The frequencies of tip geometry i: its request's own eV, then
+    sweep - 1 more drawn uniform in 0.08-0.13 eV (seeded per geometry)."""
+    rng = np.random.default_rng([wl["seed"], i])
+    return [eV0] + [float(x) for x in rng.uniform(0.08, 0.13, wl.get("sweep", 1) - 1)]
 
 
 def _tip_mesh(rng):
@@ -158,7 +166,7 @@ def step_grid(wl):
     """(system index, eV, T1) per step.  The mix walks its requests' sweeps
     request-minor, so that consecutive steps are different requests."""
     if wl["kind"] == "tip":
-        return [(i, r[2], 300.0) for i, r in enumerate(tip_requests(wl))]
+        return [(i, f, 300.0) for i, r in enumerate(tip_requests(wl)) for f in tip_sweep(wl, i, r[2])]
     if wl["kind"] == "mix":
         reqs = mix_requests(wl)
         return [(i, float(f), reqs[i][3]) for f in mix_freqs(wl) for i in range(len(reqs))]
@@ -576,9 +584,10 @@ def workload_config(args, n_unknowns, world):
         name = (f"{args.workload}: two r=1um icospheres L3 (1280 tris, 1920 RWGs each), N={n_unknowns}, SiC, "
                 f"gaps {wl['gaps']} um x {len(wl['freqs'])} f in 0.08-0.13 eV")
     elif args.workload == "tip":
-        name = (f"tip: {wl['requests']} requests, cone tip (300-1500 RWGs, apex 50-200 nm) over a 4x4x0.5 um "
-                f"plate (1920 RWGs), gap log-uniform 10-1000 nm, f uniform 0.08-0.13 eV, seed {wl['seed']}; "
-                f"N varies per request")
+        name = (f"tip: {wl['requests']} geometries x {wl['sweep']} frequencies = {wl['requests'] * wl['sweep']} "
+                f"solves, cone tip (300-1500 RWGs, apex 50-200 nm) over a 4x4x0.5 um plate (1920 RWGs), gap "
+                f"log-uniform 10-1000 nm, f uniform 0.08-0.13 eV, seed {wl['seed']}; N varies per geometry; the "
+                f"timed steps are the first {args.steps} of the geometry-major order")
     elif args.workload == "slab":
         name = (f"slab: two 10x10x0.5 um slabs (5460 tris, 8190 RWGs each), N={n_unknowns}, SiC, gap 50 nm, "
                 f"{len(wl['freqs'])} f in 0.115-0.119 eV")
@@ -759,7 +768,9 @@ def run_reference(args, rank, world):
 
 # Sub-results of the default line: the other synthetic workloads, each run as
 # its own bench process (its own GPU memory) after the main measurement, and
-# summarised in the main line.  slab: the large single solve (N = 32760, one
+# summarised in the main line.  cube4: the reference's CPU case (N = 1152);
+# tip: the first 256 solves (4 geometries x 64 frequencies) of the
+# tip-over-plate sweep; slab: the large single solve (N = 32760, one
 # FP64-class solve after one warm-up solve of the same size); mix: the
 # serving mix (64 requests: closed-loop rate of one frequency per request,
 # then 64 Poisson-arrival sweeps of SUB_MIX_SWEEP frequencies).
@@ -769,7 +780,8 @@ SUBS = {
              "--serve-requests", "0", "--fp64-steps", "0", "--lite"],
     "mix": ["--workload", "mix", "--steps", "64", "--warmup", "4", "--serve-requests", "64",
             "--sweep", str(SUB_MIX_SWEEP), "--lite"],
-    "tip": ["--workload", "tip", "--steps", "64", "--warmup", "4", "--serve-requests", "0", "--lite"],
+    "cube4": ["--workload", "cube4", "--steps", "128", "--warmup", "16", "--serve-requests", "0", "--lite"],
+    "tip": ["--workload", "tip", "--steps", "256", "--warmup", "16", "--serve-requests", "0", "--lite"],
 }
 SUB_KEYS = ("value", "unit", "ms_per_step", "steps", "config", "err_est", "factorization", "serving", "stage_ms",
             "fp64_path", "accuracy", "mixed_over_fp64", "clocks", "gpu_launches", "fill_gentries_per_s", "tiles")
@@ -836,7 +848,7 @@ def main():
             print(json.dumps(run_reference(args, rank, world)))
         return
     out = run_ours(args, rank, world)
-    subs = (["slab", "mix"] if args.workload == "ico3" else []) if args.subs == "default" else \
+    subs = (["cube4", "tip", "slab", "mix"] if args.workload == "ico3" else []) if args.subs == "default" else \
         [x for x in args.subs.split(",") if x and x != "none"]
     if rank == 0 and subs and world == 1:
         out["subs"] = run_subs(subs)
