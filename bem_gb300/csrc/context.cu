@@ -120,7 +120,6 @@ void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::v
 }
 
 const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
-  (void)ctx;
   bemgpu_geom_s *g = t->geom;
   std::lock_guard<std::mutex> lk(g->cache_mu);
   auto key = std::make_pair(t, s);
@@ -135,7 +134,15 @@ const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const b
       cudaGetLastError();
       return nullptr;
     }
-    cudaMemcpy(nl.d, pairs.data(), sizeof(NearPair) * pairs.size(), cudaMemcpyHostToDevice);
+    // a copy from pageable memory may return before it lands; kernels on any
+    // lane's stream read the list, so it must be complete on return
+    if (cudaMemcpyAsync(nl.d, pairs.data(), sizeof(NearPair) * pairs.size(), cudaMemcpyHostToDevice,
+                        ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(nl.d);
+      return nullptr;
+    }
   }
   auto res = g->near_cache.emplace(key, nl);
   return &res.first->second;
@@ -453,7 +460,11 @@ int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t 
     delete t;
     return bem_fail(ctx, BEMGPU_ERR_OOM, "tree_create: device allocation failed");
   }
-  if (cudaMemcpy(t->d_rec, t->host_rec.data(), sizeof(TriRec) * t->ntri, cudaMemcpyHostToDevice) != cudaSuccess) {
+  // complete on return (a copy from pageable memory may return before it
+  // lands, and any context's stream may read the records next)
+  if (cudaMemcpyAsync(t->d_rec, t->host_rec.data(), sizeof(TriRec) * t->ntri, cudaMemcpyHostToDevice,
+                      ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
     cudaFree(t->d_rec);
     delete t;
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "tree_create: upload failed");

@@ -878,7 +878,14 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
   typedef typename V2<T>::type T2;
   rc = BEMGPU_OK;
   const int rows = n - k0;
-  const int G = std::max(1, std::min(ctx->num_sms, (rows + 15) / 16));
+  int G = std::max(1, std::min(ctx->num_sms, (rows + 15) / 16));
+  if (nb > 1) {
+    // a batch shares about the CTAs one panel would take (more rows per CTA,
+    // up to what shared memory holds), so that its cooperative launch does
+    // not need more of the GPU than a single panel's
+    const int max_chunk = (int)(COOP_MAX_SMEM / (sizeof(T2) * (size_t)w)) - 1;
+    G = std::max((rows + max_chunk - 1) / max_chunk, (G + nb - 1) / nb);
+  }
   const int chunk = (rows + G - 1) / G;
   const size_t smem = sizeof(T2) * (size_t)(chunk + 1) * w;
   if (smem > (size_t)COOP_MAX_SMEM) return false;

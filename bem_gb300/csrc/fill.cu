@@ -1515,6 +1515,9 @@ int load_tables(bemgpu_ctx_s *ctx) {
     split(bemgpu_tri_rule91, 91, v);
     BEM_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_rdf91, v.data(), sizeof(float) * v.size()));
   }
+  // the copies from host memory may return before they land: every stream
+  // of the device reads the tables from now on
+  BEM_CUDA_TRY(ctx, cudaDeviceSynchronize());
   g_tables_loaded[ctx->device] = true;
   return BEMGPU_OK;
 }

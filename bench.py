@@ -10,15 +10,20 @@ Synthetic meshes from bem_gb300.mesh (seeded), no dataset.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--precision fp64|mixed] [--workload ico3|ico2|cube4|tip|slab|mix] [--lanes L]
-                  [--solver escalate|c64|fp64class] [--serve-requests R] [--sweep F]
-                  [--e2e-steps K2] [--prof-steps K3] [--no-cpu-baseline]
+                  [--batch B] [--solver escalate|c64|fp64class] [--serve-requests R] [--sweep F]
+                  [--e2e-steps K2] [--prof-steps K3] [--fp64-steps K4] [--subs LIST]
+                  [--tune cache|retune|off] [--lite] [--no-cpu-baseline]
 
 Other workloads: cube4 (two 1 um cubes, 4x4 squares per face, N = 1152, gap
-100 nm, 20 f); tip (a cone tip over a plate, uneven N per request); slab (two
-10 x 10 x 0.5 um slabs of 8190 RWGs each, N = 32760, gap 50 nm, 8 f in
-0.115-0.119 eV); mix (the serving mix: each request a frequency sweep over a
-random pair of bodies drawn from cubes, icospheres, thin slabs and cone tips,
-SiC or alumina, gap log-uniform 10-1000 nm, T1 uniform 300-600 K).
+100 nm, 20 f); tip (64 cone tips over a plate, each with a 64-frequency
+sweep, uneven N per tip); slab (two 10 x 10 x 0.5 um slabs of 8190 RWGs each,
+N = 32760, gap 50 nm, 8 f in 0.115-0.119 eV); mix (the serving mix: each
+request a frequency sweep over a random pair of bodies drawn from cubes,
+icospheres, thin slabs and cone tips, SiC or alumina, gap log-uniform
+10-1000 nm, T1 uniform 300-600 K).  The default ico3 line also carries the
+FP64 path's rate on its first timed requests with the measured error of the
+mixed results against it, and sub-results of cube4, tip, slab and mix, each
+run as its own process.
 
 Requests go through the request farm (bem_gb300.api.Farm): L lanes (default
 4), each a context with its own stream and host thread, keep L solves in
@@ -27,8 +32,9 @@ region is bracketed by device synchronisations and CUDA events, so it is the
 GPU's wall time for K solves.
 
 --impl reference times the reference path's CPU implementation on the host
-cores (the oracle port: oracle/bem_oracle.c fill + numpy LAPACK algebra), on a
-bounded sample of each step's work.
+cores (the oracle port: oracle/bem_oracle.c fill + LAPACK zgetrf/zgetri and
+the trace products) in the reference's throughput mode, one single-threaded
+process per core, each on a bounded sample of a solve.
 """
 from __future__ import annotations
 
@@ -475,14 +481,23 @@ def _kernel_segment(args, job, prec, ctx, clk, L, api, torch, _lib, ctypes):
     events on the launching stream, per kernel class) over solves run one at
     a time, the same requests as the first timed steps."""
     n_prof = args.prof_steps or min(args.steps, 4)
+    if args.batch > 1:
+        # the farm solved batches: so do the profiled solves (whole batches)
+        n_prof = max(n_prof, args.batch) // args.batch * args.batch
     prof_jobs = [job(args.warmup + k) for k in range(n_prof)]
     api.CalcHeatTransfer(*job(0), precision=prec, strict=False)  # workspace of this context
+    if args.batch > 1:
+        api.CalcHeatTransferBatch(prof_jobs[:args.batch], precision=prec, strict=False)
     torch.cuda.synchronize()
     L.bemgpu_prof_enable(ctx.handle, 1)
     prof_infos = []
-    for j in prof_jobs:
-        prof_infos.append({})
-        api.CalcHeatTransfer(*j, precision=prec, strict=False, info=prof_infos[-1])
+    if args.batch > 1:
+        for k in range(0, n_prof, args.batch):
+            api.CalcHeatTransferBatch(prof_jobs[k:k + args.batch], precision=prec, strict=False, infos=prof_infos)
+    else:
+        for j in prof_jobs:
+            prof_infos.append({})
+            api.CalcHeatTransfer(*j, precision=prec, strict=False, info=prof_infos[-1])
     stats = {}
     for kk, name in enumerate(_lib.K_NAMES):
         n = ctypes.c_int64()
