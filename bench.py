@@ -242,10 +242,21 @@ FP64_NOMINAL_TFLOPS = 1.25
 # FP32 lanes of the GPU (152 SMs x 128): the issue rate of the double-float fill.
 FP32_LANES = 152 * 128
 # FP32-pipe thread instructions per algorithmic FP64-class flop of the
-# double-float fill kernels, from ncu's instruction counts on the ico2
-# workload: near pairs 7.06 (2.84e9 warp instructions, 8200 pairs x 1.57
-# Mflop), far pairs 6.85 (6.44e8 warp instructions, 401400 pairs x 7506 flop).
-DF_INSTR_PER_FLOP = 7.0
+# double-float fill kernels, from ncu's smsp__inst_executed on the ico2
+# workload (one launch each over the three fills of a solve): near pairs 7.76
+# (6.24e9 warp instructions, 16400 pairs x 1.57 Mflop), far pairs 7.2 (1.01e9
+# warp instructions for 598000 pairs, 5 % more per pair than the 6.85 counted
+# on the exterior fill alone with the rules' frozen flop counts).
+DF_INSTR_PER_FLOP = {"fill_near": 7.76, "fill_far": 7.2}
+# DRAM bytes of the fill (far and near launch together) per matrix entry of the
+# three Zts outputs, from ncu on the ico2 workload: 246.7 MB (far 118.2 MB +
+# near 128.5 MB) for 5.53 M entries; the half-pair blocks the fill writes are
+# 32 B per entry (177 MB), so the measured traffic is 1.39x the algorithmic.
+FILL_DRAM_BYTES_PER_ENTRY = 44.6
+# The exact product's DRAM bytes against the library's operand-traffic model
+# (its ProfScope bytes: A re-read once per band of N-tiles, B once, C written):
+# ncu 313.7 MB against 327 MB modelled for ex_gemm_kernel<5, 3> at ico2.
+EX_TRAFFIC_PER_MODEL_BYTE = 0.96
 
 
 def shard_steps(grid, rank, world):
@@ -515,7 +526,8 @@ def _kernel_segment(args, job, prec, ctx, clk, L, api, torch, _lib, ctypes):
     fill_s = sum(i["ms_fill"] for i in prof_infos) / 1e3
     pk, pk_kind = peaks()
     roof = roofline(stats, args.precision, pk, pk_kind,
-                    fp64class=all(i.get("solver") == 2 for i in prof_infos), sm_mhz=clk.summary()["sm_mhz"])
+                    fp64class=all(i.get("solver") == 2 for i in prof_infos), sm_mhz=clk.summary()["sm_mhz"],
+                    entries=sum(entries(j) for j in prof_jobs))
     return {
         "fill_gentries_per_s": sum(entries(j) for j in prof_jobs) / fill_s / 1e9,
         # the three Zts outputs written as complex128 (16 B per entry)
@@ -545,9 +557,10 @@ GROUPS = {
 }
 
 
-def roofline(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None):
+def roofline(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None, entries=None):
     """Roofline of the dominant kernel group of the timed region: algorithmic
-    flops (or bytes) per CUDA-event second against the measured peak."""
+    flops (or bytes) per CUDA-event second against the measured peak.
+    entries: matrix entries the profiled solves filled (the fill's traffic)."""
     groups = dict(GROUPS)
     if fp64class:
         groups["ex_lu"] = groups.pop("tc_gemm")
@@ -560,12 +573,18 @@ def roofline(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None):
     n = sum(stats[k]["launches"] for k in ks if k in stats)
     base = {"kernel": dom, "kinds": list(ks), "launches": n, "avg_launch_ms": ms / max(1, n), "traffic": None}
     if dom == "fill":
+        if entries:
+            base["traffic"] = FILL_DRAM_BYTES_PER_ENTRY * entries / max(1, n)
+            base["traffic_algorithmic"] = 32.0 * entries / max(1, n)
+            base["traffic_source"] = ("ncu dram__bytes_read + dram__bytes_write of the far and near launches at ico2 "
+                                      "per matrix entry, times this launch's entries")
         if precision == "fp64":
             ach = fl / (ms / 1e3) / 1e12
             return dict(base, bound="fp64", achieved=ach, peak=FP64_NOMINAL_TFLOPS, unit="TFLOP/s",
                         frac=ach / FP64_NOMINAL_TFLOPS, peak_source="nominal GB300 FP64 (not in MEASURED_PEAKS.json)")
         alg = fl / (ms / 1e3) / 1e12
-        ach = alg * DF_INSTR_PER_FLOP
+        instr = sum(stats[k]["flops"] * DF_INSTR_PER_FLOP[k] for k in ks if k in stats)
+        ach = instr / (ms / 1e3) / 1e12
         peak = FP32_LANES * (sm_mhz or 2070.0) * 1e6 / 1e12
         return dict(base, bound="fp32 issue (double-float)", achieved=ach, peak=peak,
                     unit="T thread-instructions/s", frac=ach / peak,
@@ -573,8 +592,14 @@ def roofline(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None):
                     alg_fp64class_tflops=alg, instr_per_alg_flop=DF_INSTR_PER_FLOP,
                     note="the fill is FP64-class arithmetic in double-float on the FP32 pipes: its algorithmic "
                          "FP64-class flops (frozen count, live) per CUDA-event second times the FP32-pipe "
-                         "thread instructions per algorithmic flop that ncu counted on the two fill kernels")
+                         "thread instructions per algorithmic flop that ncu counted on each fill kernel "
+                         "(smsp__inst_executed, ico2)")
     if bound == "tensor":
+        if dom == "ex_gemm":
+            base["traffic"] = EX_TRAFFIC_PER_MODEL_BYTE * by / max(1, n)
+            base["traffic_algorithmic"] = by / max(1, n)
+            base["traffic_source"] = ("the library's operand-traffic model of each launch, scaled by ncu's "
+                                      "dram__bytes / model on ex_gemm_kernel<5, 3> at ico2 (0.96)")
         ach = fl / (ms / 1e3) / 1e12
         peak = pk.get("bf16_tflops_sustained", 1700.0)
         tens = sum(stats[k].get("tensor", 0.0) for k in ks if k in stats)
@@ -610,7 +635,9 @@ def workload_config(args, n_unknowns, world):
         name = (f"mix: {wl['requests']} requests, each a pair of bodies from {{cube 288-1152, icosphere L2-L3, "
                 f"10x10x0.5 um slab 2142-4032, cone tip 300-1500 RWGs}}, SiC or alumina, gap log-uniform "
                 f"10-1000 nm, T1 300-600 K, sweep of {args.sweep or wl['sweep']} f in 0.08-0.13 eV "
-                f"(timed steps: one f of each request in turn), seed {wl['seed']}")
+                f"(timed steps: one f of each request in turn), seed {wl['seed']}; narrowed from icosphere L2-L4 "
+                f"and slabs of 2000-8000 RWGs: L4 icospheres and slabs above 4032 RWGs take seconds per solve "
+                f"(the slab workload measures that class)")
     else:
         name = args.workload
     n_max = n_unknowns if isinstance(n_unknowns, int) else int(str(n_unknowns).split("-")[-1])
