@@ -109,6 +109,9 @@ struct bemgpu_ctx_s {
     int near_minb = 2;   // CTAs per SM of the double-float near-pair kernel's register budget (2, 3, 4)
     int far_rows = 4;    // warps per CTA of the far-pair kernel (1, 2, 4, 8)
     int raster = 8;      // M-tiles per rasterization band of the tensor-core products (1..64)
+    int panel_ctas = 0;  // CTAs of a cooperative LU panel at most (0: one per SM)
+    int near_sync = 1;   // double-float near-pair CTAs barrier after each pair couple (0, 1)
+    int near_grid = 16;  // CTAs per SM in the near-pair launch's grid at most (1..64)
   } tune;
   double escalate_tol = 1e-6;  // complex64 refinement error estimate above which the solve escalates
   double fallback_tol = 1e-6;  // FP64-class error estimate above which mode 0 re-solves on the FP64 path

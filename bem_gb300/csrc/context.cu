@@ -527,6 +527,18 @@ int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value) {
       if (value < 1 || value > 64) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: raster %d not in 1..64", value);
       ctx->tune.raster = value;
       return BEMGPU_OK;
+    case BEMGPU_TUNE_PANEL_CTAS:
+      if (value < 0 || value > 1024) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: panel_ctas %d not in 0..1024", value);
+      ctx->tune.panel_ctas = value;
+      return BEMGPU_OK;
+    case BEMGPU_TUNE_NEAR_SYNC:
+      if (value < 0 || value > 1) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: near_sync %d not 0 or 1", value);
+      ctx->tune.near_sync = value;
+      return BEMGPU_OK;
+    case BEMGPU_TUNE_NEAR_GRID:
+      if (value < 1 || value > 64) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: near_grid %d not in 1..64", value);
+      ctx->tune.near_grid = value;
+      return BEMGPU_OK;
     default:
       return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
   }
@@ -538,6 +550,9 @@ int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value) {
     case BEMGPU_TUNE_NEAR_MINB: *value = ctx->tune.near_minb; return BEMGPU_OK;
     case BEMGPU_TUNE_FAR_ROWS: *value = ctx->tune.far_rows; return BEMGPU_OK;
     case BEMGPU_TUNE_RASTER: *value = ctx->tune.raster; return BEMGPU_OK;
+    case BEMGPU_TUNE_PANEL_CTAS: *value = ctx->tune.panel_ctas; return BEMGPU_OK;
+    case BEMGPU_TUNE_NEAR_SYNC: *value = ctx->tune.near_sync; return BEMGPU_OK;
+    case BEMGPU_TUNE_NEAR_GRID: *value = ctx->tune.near_grid; return BEMGPU_OK;
     default: return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
   }
 }

@@ -879,6 +879,14 @@ bool panel_coop(bemgpu_ctx_s *ctx, T *A, int64_t lda, int n, int k0, int w, int 
   rc = BEMGPU_OK;
   const int rows = n - k0;
   int G = std::max(1, std::min(ctx->num_sms, (rows + 15) / 16));
+  {
+    // fewer, fuller CTAs leave SMs to the other lanes' products while this
+    // latency-bound panel runs (BEMGPU_TUNE_PANEL_CTAS), as far as shared
+    // memory holds their rows
+    const int cap = ctx->tune.panel_ctas;
+    const int max_chunk = (int)(COOP_MAX_SMEM / (sizeof(T2) * (size_t)w)) - 1;
+    if (cap > 0) G = std::max(std::min(G, cap), (rows + max_chunk - 1) / max_chunk);
+  }
   if (nb > 1) {
     // a batch shares about the CTAs one panel would take (more rows per CTA,
     // up to what shared memory holds), so that its cooperative launch does

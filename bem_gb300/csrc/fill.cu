@@ -1132,7 +1132,13 @@ __device__ __forceinline__ void stage_outer_df(float (*outer)[6]) {
 // task's Green's function in shared memory.  MINB: CTAs per SM that the
 // register allocation must allow (2: ~250 registers; 3: 168; 4: 128 with
 // spills), chosen by the context's tuning.
-template <int MINB>
+// Warp w of CTA b takes units b * NEAR_WARPS + w + k * (grid warps), k = 0, 1, ...
+// SYNC: the CTA's warps meet at a barrier after each unit.  A pair couple runs
+// several large code regions (the inner rule, the closed-form potentials, the
+// edge correction); with two warps per scheduler, warps that have drifted into
+// different regions stall on instruction fetch, which the barrier prevents.
+// The units and their order per warp are the same either way.
+template <int MINB, bool SYNC>
 __global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_pairs_df_group_kernel(const FillTask *__restrict__ tasks,
                                                                                     int ntask, int64_t units) {
   __shared__ __align__(16) float s_nodes[NEAR_WARPS][2][BEMGPU_TRI_RULE91_N][8];
@@ -1144,17 +1150,29 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_pairs_df_group_ker
   stage_outer_df(s_outer);
   const int64_t nw = (int64_t)gridDim.x * NEAR_WARPS;
   int cur = -1;
-  for (int64_t u = (int64_t)blockIdx.x * NEAR_WARPS + wid; u < units; u += nw) {
-    const int i = task_of_near(tasks, ntask, u);
-    const FillTask &tk = tasks[i];
-    if (i != cur) {
-      if (lane == 0) s_g[wid] = tk.g;
-      __syncwarp();
-      cur = i;
+  for (int64_t base = (int64_t)blockIdx.x * NEAR_WARPS; base < units; base += nw) {
+    const int64_t u = base + wid;
+    if (u < units) {
+      const int i = task_of_near(tasks, ntask, u);
+      const FillTask &tk = tasks[i];
+      if (i != cur) {
+        if (lane == 0) s_g[wid] = tk.g;
+        __syncwarp();
+        cur = i;
+      }
+      near_couple_df(tk.T, tk.S, tk.near, tk.nnear, 2 * (u - tk.near0), s_g[wid], tk.H, tk.ntr, s_nodes[wid],
+                     s_outer, s_pc[wid], lane);
     }
-    near_couple_df(tk.T, tk.S, tk.near, tk.nnear, 2 * (u - tk.near0), s_g[wid], tk.H, tk.ntr, s_nodes[wid],
-                   s_outer, s_pc[wid], lane);
+    if (SYNC) __syncthreads();  // base is the same for the whole CTA
   }
+}
+
+template <int MINB>
+void launch_near_df(bool sync, int nb, cudaStream_t stream, const FillTask *tasks, int ntask, int64_t units) {
+  if (sync)
+    near_pairs_df_group_kernel<MINB, true><<<nb, 32 * NEAR_WARPS, 0, stream>>>(tasks, ntask, units);
+  else
+    near_pairs_df_group_kernel<MINB, false><<<nb, 32 * NEAR_WARPS, 0, stream>>>(tasks, ntask, units);
 }
 
 // Near pairs in FP64 (the plain path), one pair per warp: lanes take the
@@ -1600,14 +1618,16 @@ int bem_fill_group(bemgpu_ctx_s *ctx, FillJob *jobs, int njobs, const bemgpu_opt
   }
   BEM_CUDA_TRY(ctx, cudaGetLastError());
   if (near_units > 0) {
-    const int nb = (int)std::min<int64_t>((near_units + NEAR_WARPS - 1) / NEAR_WARPS, (int64_t)ctx->num_sms * 16);
+    const int nb = (int)std::min<int64_t>((near_units + NEAR_WARPS - 1) / NEAR_WARPS,
+                                          (int64_t)ctx->num_sms * ctx->tune.near_grid);
     ProfScope ps(ctx, BEMGPU_K_FILL_NEAR, stream, near_flops, near_bytes);
+    const bool sync = ctx->tune.near_sync != 0;
     if (mode == FILL_DF && ctx->tune.near_minb == 3)
-      near_pairs_df_group_kernel<3><<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+      launch_near_df<3>(sync, nb, stream, dtasks, njobs, near_units);
     else if (mode == FILL_DF && ctx->tune.near_minb == 4)
-      near_pairs_df_group_kernel<4><<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+      launch_near_df<4>(sync, nb, stream, dtasks, njobs, near_units);
     else if (mode == FILL_DF)
-      near_pairs_df_group_kernel<2><<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
+      launch_near_df<2>(sync, nb, stream, dtasks, njobs, near_units);
     else
       near_pairs_group_kernel<<<nb, 32 * NEAR_WARPS, 0, stream>>>(dtasks, njobs, near_units);
     ctx->launches++;

@@ -325,7 +325,14 @@ def run_ours(args, rank, world):
                                       retune=args.tune == "retune")
         for c in lane_ctx:
             tuning.apply(c, params)
+        # the tuning solves ran on the main context: give back its workspace
+        # before the lanes allocate theirs
+        _check_rc(L.bemgpu_ctx_trim(ctx.handle))
         tiles = dict(params, source=source, seconds=time.perf_counter() - t0t)
+    if args.panel_ctas:
+        for c in lane_ctx + [ctx.handle]:
+            _check_rc(L.bemgpu_ctx_set_tuning(c, _lib.TUNE_PANEL_CTAS, args.panel_ctas))
+        tiles = dict(tiles or {}, panel_ctas=args.panel_ctas)
     farm.map([job(k) for k in range(args.warmup)], precision=prec, strict=False)
     if world > 1:
         import torch.distributed as dist
@@ -819,7 +826,7 @@ def run_reference(args, rank, world):
 SUB_MIX_SWEEP = 8
 SUBS = {
     "slab": ["--workload", "slab", "--solver", "fp64class", "--steps", "1", "--warmup", "1", "--lanes", "1",
-             "--serve-requests", "0", "--fp64-steps", "0", "--lite"],
+             "--serve-requests", "0", "--fp64-steps", "0", "--tune", "off", "--lite"],
     "mix": ["--workload", "mix", "--steps", "64", "--warmup", "4", "--serve-requests", "64",
             "--sweep", str(SUB_MIX_SWEEP), "--lite"],
     "cube4": ["--workload", "cube4", "--steps", "128", "--warmup", "16", "--serve-requests", "0", "--lite"],
@@ -878,6 +885,8 @@ def main():
     ap.add_argument("--tune", default="cache", choices=["cache", "retune", "off"],
                     help="launch shapes from the autotuner's cache (tuned first when missing), re-tuned, or the "
                          "library defaults")
+    ap.add_argument("--panel-ctas", type=int, default=0,
+                    help="CTAs of a cooperative LU panel at most (0: one per SM)")
     ap.add_argument("--lite", action="store_true",
                     help="skip the end-to-end and per-kernel segments (sub-workload runs)")
     args = ap.parse_args()

@@ -134,11 +134,23 @@ int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
  *                          registers) or 4 (128, some spilled);
  *   BEMGPU_TUNE_FAR_ROWS   warps per CTA of the far-pair kernel: 1, 2, 4 (default), 8;
  *   BEMGPU_TUNE_RASTER     M-tiles per rasterization band of the tensor-core
- *                          products: 1..64 (default 8).
+ *                          products: 1..64 (default 8);
+ *   BEMGPU_TUNE_PANEL_CTAS CTAs of a cooperative LU panel at most (fewer,
+ *                          fuller CTAs leave SMs to other lanes' work while a
+ *                          latency-bound panel runs): 0 (one per SM, default)
+ *                          or a cap, raised where shared memory requires;
+ *   BEMGPU_TUNE_NEAR_SYNC  1 (default): the double-float near-pair kernel's
+ *                          CTAs barrier after each pair couple, keeping their
+ *                          warps in the same code region; 0: no barrier;
+ *   BEMGPU_TUNE_NEAR_GRID  CTAs per SM of the near-pair launch's grid at most:
+ *                          1..64 (default 16).
  * BEMGPU_ERR_ARG for an unknown knob or value.  Results do not depend on them. */
 #define BEMGPU_TUNE_NEAR_MINB 0
 #define BEMGPU_TUNE_FAR_ROWS 1
 #define BEMGPU_TUNE_RASTER 2
+#define BEMGPU_TUNE_PANEL_CTAS 3
+#define BEMGPU_TUNE_NEAR_SYNC 4
+#define BEMGPU_TUNE_NEAR_GRID 5
 int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value);
 int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value);
 /* Tracing: with BEMGPU_TRACE set (not "0") in the environment, the library

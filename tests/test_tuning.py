@@ -40,6 +40,13 @@ def test_results_do_not_depend_on_the_launch_shapes(tmp_path):
         for v in cands:
             tuning.apply(ctx.handle, dict(tuning.DEFAULTS, **{name: v}))
             assert run() == base, (name, v)
+    L = _lib.load()
+    # knobs the tuner leaves at their measured defaults: the same results too
+    for knob, vals in ((_lib.TUNE_NEAR_SYNC, (0, 1)), (_lib.TUNE_NEAR_GRID, (2, 16)),
+                       (_lib.TUNE_PANEL_CTAS, (38, 0))):
+        for v in vals:
+            assert L.bemgpu_ctx_set_tuning(ctx.handle, knob, v) == _lib.OK
+            assert run() == base, (knob, v)
     params, timings = tuning.tune(lambda: api.CalcHeatTransfer(1e-6, 0.116, 300.0, 0.0, top, s, tt,
                                                                precision=_lib.PREC_MIXED_LA), ctx.handle, reps=1)
     assert all(params[k] in tuning.KNOBS[k][1] for k in tuning.KNOBS)
@@ -49,6 +56,8 @@ def test_results_do_not_depend_on_the_launch_shapes(tmp_path):
     tuning.store(tuning.cache_key(2 * top.rwgs), params, path)
     p3, src = tuning.tuned(lambda: None, ctx.handle, 2 * top.rwgs, path=path)
     assert src == "cache" and p3 == params
-    L = _lib.load()
     assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_NEAR_MINB, 5) == _lib.ERR_ARG
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_NEAR_SYNC, 2) == _lib.ERR_ARG
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_NEAR_GRID, 0) == _lib.ERR_ARG
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_PANEL_CTAS, -1) == _lib.ERR_ARG
     assert L.bemgpu_ctx_set_tuning(ctx.handle, 99, 1) == _lib.ERR_ARG
