@@ -63,7 +63,11 @@ template <int SA, int SB>
 __host__ __device__ constexpr int ex_smem_bytes() { return ExCfg<SA, SB>::SMEM; }
 // K step of the built (SA, SB) kernels, on the host
 inline int ex_bk(int SA, int SB) {
-  return SA == 5 && SB == 3 ? ExCfg<5, 3>::BK : SA == 5 ? ExCfg<5, 5>::BK : SA == 4 ? ExCfg<4, 4>::BK : ExCfg<3, 3>::BK;
+  return SA == 5 && SB == 2   ? ExCfg<5, 2>::BK
+         : SA == 5 && SB == 3 ? ExCfg<5, 3>::BK
+         : SA == 5            ? ExCfg<5, 5>::BK
+         : SA == 4            ? ExCfg<4, 4>::BK
+                              : ExCfg<3, 3>::BK;
 }
 
 // The slice products of an (SA, SB) product: (a, b) with a < SA, b < SB and
@@ -463,7 +467,8 @@ size_t bem_exact_operand_bytes(bool is_a, int rows, int k, int slices) {
 
 int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double *M, int64_t ld, int rows, int k,
                    double sign, int slices, ExactOperand &op, cudaStream_t st, double *quantize) {
-  if (slices < 3 || slices > 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
+  // 2 slices only for a quantized B operand (the 5 x 2 product)
+  if (slices < (quantize ? 2 : 3) || slices > 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
   if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
                           : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
@@ -502,8 +507,10 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
         ex_prep_b_kernel<5><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
       else if (slices == 4)
         ex_prep_b_kernel<4><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
-      else
+      else if (slices == 3)
         ex_prep_b_kernel<3><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
+      else
+        ex_prep_b_kernel<2><<<grid, 128, 0, st>>>(M, ld, k, rows, amax, op.aux, S, rp, kp, quantize);
     }
     ctx->launches++;
   }
@@ -520,7 +527,7 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   if (!a.is_a || b.is_a || a.k != b.k || a.kp != b.kp || a.slices < b.slices)
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: operands do not match");
   const int m = a.rows, n = b.rows, SB = b.slices, SA = b.exact ? a.slices : b.slices;
-  if (!((SA == SB && SA >= 3 && SA <= 5) || (SA == 5 && SB == 3)))
+  if (!((SA == SB && SA >= 3 && SA <= 5) || (SA == 5 && (SB == 3 || SB == 2))))
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: slices (%d, %d) not built", SA, SB);
   const int SL = SB;
   ExMaps maps;
@@ -539,6 +546,8 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
                                            ex_smem_bytes<3, 3>()));
     BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            ex_smem_bytes<5, 3>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ex_smem_bytes<5, 2>()));
     ctx->ex_ready = true;
   }
   if (!ctx->tc_err_ready) {
@@ -563,7 +572,10 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   }
   const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / EX_BN));
   const int ktiles = (int)(a.kp / bk);
-  if (SA == 5 && SB == 3)
+  if (SA == 5 && SB == 2)
+    ex_gemm_kernel<5, 2><<<grid, EX_THREADS, ex_smem_bytes<5, 2>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
+                                                                          accumulate, shifts, ctx->tune.raster, err);
+  else if (SA == 5 && SB == 3)
     ex_gemm_kernel<5, 3><<<grid, EX_THREADS, ex_smem_bytes<5, 3>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
                                                                           accumulate, shifts, ctx->tune.raster, err);
   else if (SA == 5)

@@ -35,6 +35,9 @@ constexpr int MIXED_SLICES = 5;  // block fixed-point slices of the refinement a
 constexpr int DELTA_SLICES = 3;  // slices of a correction: each correction is quantized to them in
                                  // place before it is added to the iterate, so the residual's
                                  // incremental products stay exact (to 2^-40 of |W||Y|)
+constexpr int FIRST_SLICES = 2;  // slices of the complex64 path's first iterate, quantized to them in
+                                 // place: 2^-17 of its block maxima, below the complex64 LU's own
+                                 // error, so refinement corrects both in the same steps
 constexpr int TRACE_SLICES = 4;  // slices of X in the full trace products H1 X, H2 X^H (10 products):
                                  // ~2^-33 of |H||X| per entry; the trace of a product of two
                                  // absorption (semi-definite) operators does not cancel, so S keeps
@@ -464,11 +467,11 @@ int bem_mixed_solve(bemgpu_ctx_s *ctx, double *W, int n, int ns2, const double *
     // R = E_t - W Y: R64 holds -W Y; the first step forms it from Y, later
     // steps add -W dY of the last correction (3-slice product)
     if (iters == 0) {
-      // the first iterate (complex64 accuracy) is quantized to 3 slices in
-      // place; W's 5 slices times those 3 then need 12 slice products, not 15,
-      // for the same 2^-40 residual
+      // the first iterate (complex64 accuracy) is quantized to 2 slices in
+      // place; W's 5 slices times those 2 then need 9 slice products, not 15,
+      // for the same 2^-40 residual of the quantized iterate
       ExactOperand opY;
-      rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, DELTA_SLICES, opY, st, b.Y);
+      rc = bem_exact_prep(ctx, "Y", false, b.Y, n, nt2, n, 1.0, FIRST_SLICES, opY, st, b.Y);
       if (!rc) rc = bem_exact_gemm(ctx, BEMGPU_K_REFINE_GEMM, b.opW, opY, b.R64, n, 0, st);
       if (!rc) BEM_CUDA_TRY(ctx, cudaMemcpyAsync(&eb_y, opY.aux + 8, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     } else {
