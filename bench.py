@@ -532,9 +532,10 @@ def _kernel_segment(args, job, prec, ctx, clk, L, api, torch, _lib, ctypes):
 
     fill_s = sum(i["ms_fill"] for i in prof_infos) / 1e3
     pk, pk_kind = peaks()
-    roof = roofline(stats, args.precision, pk, pk_kind,
-                    fp64class=all(i.get("solver") == 2 for i in prof_infos), sm_mhz=clk.summary()["sm_mhz"],
-                    entries=sum(entries(j) for j in prof_jobs))
+    rargs = dict(fp64class=all(i.get("solver") == 2 for i in prof_infos), sm_mhz=clk.summary()["sm_mhz"],
+                 entries=sum(entries(j) for j in prof_jobs))
+    roof = roofline(stats, args.precision, pk, pk_kind, **rargs)
+    roofs = rooflines(stats, args.precision, pk, pk_kind, **rargs)
     return {
         "fill_gentries_per_s": sum(entries(j) for j in prof_jobs) / fill_s / 1e9,
         # the three Zts outputs written as complex128 (16 B per entry)
@@ -545,6 +546,8 @@ def _kernel_segment(args, job, prec, ctx, clk, L, api, torch, _lib, ctypes):
         "kernel_ms_note": f"stage and kernel-class times (and the fill rate) over {n_prof} solves run one at "
                           f"a time, without lane overlap",
         "roofline": roof,
+        # every kernel group's roofline (the dominant one above in full)
+        "rooflines": roofs,
     }
 
 
@@ -564,17 +567,45 @@ GROUPS = {
 }
 
 
+def _groups(fp64class):
+    groups = dict(GROUPS)
+    if fp64class:
+        groups["ex_lu"] = groups.pop("tc_gemm")
+    return groups
+
+
 def roofline(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None, entries=None):
     """Roofline of the dominant kernel group of the timed region: algorithmic
     flops (or bytes) per CUDA-event second against the measured peak.
     entries: matrix entries the profiled solves filled (the fill's traffic)."""
-    groups = dict(GROUPS)
-    if fp64class:
-        groups["ex_lu"] = groups.pop("tc_gemm")
+    groups = _groups(fp64class)
     tot = {g: sum(stats[k]["ms"] for k in ks if k in stats) for g, (ks, _) in groups.items()}
-    dom = max(tot, key=tot.get)
-    ks, bound = groups[dom]
-    ms = tot[dom]
+    return group_roofline(max(tot, key=tot.get), stats, precision, pk, pk_kind, fp64class, sm_mhz, entries)
+
+
+def rooflines(stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None, entries=None):
+    """The same roofline for every kernel group that ran, with its share of
+    the profiled kernel time."""
+    groups = _groups(fp64class)
+    tot = {g: sum(stats[k]["ms"] for k in ks if k in stats) for g, (ks, _) in groups.items()}
+    all_ms = sum(tot.values())
+    out = {}
+    for g in sorted(tot, key=tot.get, reverse=True):
+        if tot[g] <= 0:
+            continue
+        r = group_roofline(g, stats, precision, pk, pk_kind, fp64class, sm_mhz, entries)
+        out[g] = {k: r[k] for k in ("bound", "achieved", "peak", "unit", "frac", "avg_launch_ms", "launches",
+                                    "traffic", "executed_frac", "alg_fp64class_tflops") if k in r}
+        out[g]["ms_share"] = tot[g] / all_ms
+        if groups[g][1] == "latency":
+            out[g]["bound"] = "latency (panel bytes against HBM shown)"
+    return out
+
+
+def group_roofline(dom, stats, precision, pk, pk_kind, fp64class=False, sm_mhz=None, entries=None):
+    """Roofline of kernel group `dom` (see GROUPS)."""
+    ks, bound = _groups(fp64class)[dom]
+    ms = sum(stats[k]["ms"] for k in ks if k in stats)
     fl = sum(stats[k]["flops"] for k in ks if k in stats)
     by = sum(stats[k]["bytes"] for k in ks if k in stats)
     n = sum(stats[k]["launches"] for k in ks if k in stats)
@@ -858,8 +889,10 @@ def run_subs(names):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
-    ap.add_argument("--warmup", type=int, default=3)
+    # 32 solves through 4 lanes (8 rounds: the ramp-down of the last round is
+    # a small part of the timed region), after 8 warm-up solves
+    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "mixed-fp32fill"])
     ap.add_argument("--workload", default="ico3", choices=sorted(WORKLOADS))

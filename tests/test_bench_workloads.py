@@ -102,3 +102,9 @@ def test_roofline_block_of_each_group():
     assert r["kernel"] == "ex_gemm" and r["bound"] == "tensor" and r["peak"] == 1715.7
     assert r["executed_bf16_tflops"] == pytest.approx(4.6e13 / 0.050 / 1e12)
     assert r["slice_products_per_mac"] == pytest.approx(4.6e13 / 5.3e12)
+    # every group that ran, each with its own bound and its share of the time
+    rs = bench.rooflines(fill, "mixed", pk, "measured", sm_mhz=2070.0)
+    assert list(rs) == ["fill", "ex_gemm"]
+    assert rs["fill"]["frac"] == pytest.approx(bench.roofline(fill, "mixed", pk, "measured", sm_mhz=2070.0)["frac"])
+    assert rs["ex_gemm"]["bound"] == "tensor" and "executed_frac" in rs["ex_gemm"]
+    assert sum(v["ms_share"] for v in rs.values()) == pytest.approx(1.0)
