@@ -41,7 +41,7 @@ EXPORTED = [
     "bemgpu_ctx_set_solver", "bemgpu_ctx_wait_selftest", "bemgpu_ctx_set_escalation_tol", "bemgpu_ctx_set_fp64_fallback_tol",
     "bemgpu_zgemm_exact_quantized", "bemgpu_tree_create_body_device", "bemgpu_tree_concat", "bemgpu_tree_rwgs",
     "bemgpu_ctx_set_tuning", "bemgpu_ctx_get_tuning", "bemgpu_heat_transfer_batch", "bemgpu_batch_footprint",
-    "bemgpu_farm_set_batch",
+    "bemgpu_farm_set_batch", "bemgpu_pending_free_bytes",
 ]
 
 
@@ -131,6 +131,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "bemgpu_farm_budget": (i64, [vp]),
         "bemgpu_ctx_workspace_bytes": (i64, [vp]),
         "bemgpu_ctx_trim": (i32, [vp]),
+        "bemgpu_pending_free_bytes": (i64, []),
         "bemgpu_solve_footprint": (i64, [i32, i32, i32]),
         "bemgpu_ctx_solve_footprint": (i64, [vp, i32, i32, i32]),
         "bemgpu_ctx_set_solver": (i32, [vp, i32]),

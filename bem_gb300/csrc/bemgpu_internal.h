@@ -156,6 +156,11 @@ int bem_fail(bemgpu_ctx_s *ctx, int code, const char *fmt, ...);
 // escalations); nothing otherwise.
 void bem_trace(const char *fmt, ...);
 // Returns a device buffer of at least `bytes` for `name` (grown on demand).
+// Device memory of destroyed trees and geometries, freed in batches after a
+// device synchronisation (context.cu).
+void bem_defer_free(int device, void *p, size_t bytes);
+void bem_flush_deferred_frees();
+size_t bem_deferred_free_count();
 void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes);
 // Near pairs of (t, s) built on the host (no device memory touched).
 void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::vector<NearPair> &pairs);

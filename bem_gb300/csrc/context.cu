@@ -65,6 +65,78 @@ void bem_trace(const char *fmt, ...) {
   fprintf(stderr, "bemgpu: %s\n", buf);
 }
 
+// ---------------- deferred frees ----------------
+// Destroying a tree or geometry gives its device memory (triangle records,
+// near-pair lists) to this list instead of freeing it at once: cudaFree waits
+// for the whole device, so a serving loop that destroys each request's
+// geometry would otherwise drain every lane's work per request.  The list is
+// freed in one go - one device synchronisation, so nothing in flight still
+// reads the memory - when it holds DEFER_MAX_PTRS pointers or DEFER_MAX_BYTES,
+// when a context is trimmed or torn down, and before an allocation that
+// failed is retried.
+namespace {
+struct DeferredFrees {
+  std::mutex mu;
+  std::vector<std::pair<int, void *>> ptrs;  // (device, pointer)
+  size_t bytes = 0;
+};
+DeferredFrees &deferred_frees() {
+  static DeferredFrees d;
+  return d;
+}
+constexpr size_t DEFER_MAX_PTRS = 96;
+constexpr size_t DEFER_MAX_BYTES = (size_t)512 << 20;
+}  // namespace
+
+void bem_flush_deferred_frees() {
+  std::vector<std::pair<int, void *>> v;
+  {
+    DeferredFrees &d = deferred_frees();
+    std::lock_guard<std::mutex> lk(d.mu);
+    v.swap(d.ptrs);
+    d.bytes = 0;
+  }
+  if (v.empty()) return;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  std::sort(v.begin(), v.end());
+  int dev = -1;
+  for (auto &e : v) {
+    if (e.first != dev) {
+      dev = e.first;
+      cudaSetDevice(dev);
+      cudaDeviceSynchronize();
+    }
+    cudaFree(e.second);
+  }
+  cudaSetDevice(cur);
+}
+
+void bem_defer_free(int device, void *p, size_t bytes) {
+  if (!p) return;
+  bool flush;
+  {
+    DeferredFrees &d = deferred_frees();
+    std::lock_guard<std::mutex> lk(d.mu);
+    d.ptrs.emplace_back(device, p);
+    d.bytes += bytes;
+    flush = d.ptrs.size() >= DEFER_MAX_PTRS || d.bytes >= DEFER_MAX_BYTES;
+  }
+  if (flush) bem_flush_deferred_frees();
+}
+
+size_t bem_deferred_free_count() {
+  DeferredFrees &d = deferred_frees();
+  std::lock_guard<std::mutex> lk(d.mu);
+  return d.ptrs.size();
+}
+
+extern "C" int64_t bemgpu_pending_free_bytes(void) {
+  DeferredFrees &d = deferred_frees();
+  std::lock_guard<std::mutex> lk(d.mu);
+  return (int64_t)d.bytes;
+}
+
 void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes) {
   auto it = ctx->ws.find(name);
   if (it != ctx->ws.end() && it->second.second >= bytes) return it->second.first;
@@ -76,7 +148,12 @@ void *bem_workspace(bemgpu_ctx_s *ctx, const std::string &name, size_t bytes) {
   void *p = nullptr;
   if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
     cudaGetLastError();
-    return nullptr;
+    // memory of destroyed trees may still be waiting in the deferred list
+    bem_flush_deferred_frees();
+    if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
   }
   ctx->ws[name] = {p, bytes};
   return p;
@@ -269,6 +346,7 @@ int bemgpu_ctx_create(int device, bemgpu_ctx_t *out) {
 }
 
 static void ctx_teardown(bemgpu_ctx_s *ctx) {
+  bem_flush_deferred_frees();
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto &kv : ctx->ws) cudaFree(kv.second.first);
@@ -311,6 +389,7 @@ int64_t bemgpu_ctx_workspace_bytes(bemgpu_ctx_t ctx) {
 
 int bemgpu_ctx_trim(bemgpu_ctx_t ctx) {
   if (!ctx) return BEMGPU_ERR_ARG;
+  bem_flush_deferred_frees();
   std::lock_guard<std::mutex> lk(ctx->mu);
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
@@ -353,10 +432,10 @@ int bemgpu_geom_create(bemgpu_ctx_t ctx, const double *xyz, int nv, const int *t
 // in whatever order a caller's garbage collector finalizes them.
 // Called with ctx->mu held; returns true when the geometry was freed (the
 // caller then drops the geometry's reference on the context, unlocked).
-static bool geom_release(bemgpu_geom_s *g) {
+// Device memory it held goes to `dead` (the caller defers its free).
+static bool geom_release(bemgpu_geom_s *g, std::vector<std::pair<void *, size_t>> &dead) {
   if (--g->refs == 0) {
-    cudaSetDevice(g->ctx->device);
-    for (auto &kv : g->near_cache) cudaFree(kv.second.d);
+    for (auto &kv : g->near_cache) dead.emplace_back(kv.second.d, sizeof(NearPair) * (size_t)kv.second.n);
     delete g;
     return true;
   }
@@ -366,11 +445,14 @@ static bool geom_release(bemgpu_geom_s *g) {
 int bemgpu_geom_destroy(bemgpu_geom_t g) {
   if (!g) return BEMGPU_ERR_ARG;
   bemgpu_ctx_s *ctx = g->ctx;
+  const int device = ctx->device;
   bool freed;
+  std::vector<std::pair<void *, size_t>> dead;
   {
     std::lock_guard<std::mutex> lk(ctx->mu);
-    freed = geom_release(g);
+    freed = geom_release(g, dead);
   }
+  for (auto &d : dead) bem_defer_free(device, d.first, d.second);
   if (freed) ctx_release(ctx);
   return BEMGPU_OK;
 }
@@ -480,32 +562,35 @@ int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t 
 int bemgpu_tree_destroy(bemgpu_tree_t t) {
   if (!t) return BEMGPU_ERR_ARG;
   bemgpu_ctx_s *ctx = t->ctx;
+  const int device = ctx->device;
   bool geom_freed;
+  // any context may still have kernels in flight that read the tree: its
+  // device memory is freed later, after a device synchronisation (deferred
+  // frees), not here
+  std::vector<std::pair<void *, size_t>> dead;
   {
-  std::lock_guard<std::mutex> lk(ctx->mu);
-  // any context may have solved the tree: wait for the device, not one stream
-  cudaSetDevice(ctx->device);
-  cudaDeviceSynchronize();
-  bemgpu_geom_s *g = t->geom;
-  {
-    std::lock_guard<std::mutex> lc(g->cache_mu);
-    for (auto it = g->far_rule_cache.begin(); it != g->far_rule_cache.end();) {
-      if (it->first.first == t || it->first.second == t) it = g->far_rule_cache.erase(it);
-      else ++it;
-    }
-    for (auto it = g->near_cache.begin(); it != g->near_cache.end();) {
-      if (it->first.first == t || it->first.second == t) {
-        cudaFree(it->second.d);
-        it = g->near_cache.erase(it);
-      } else {
-        ++it;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    bemgpu_geom_s *g = t->geom;
+    {
+      std::lock_guard<std::mutex> lc(g->cache_mu);
+      for (auto it = g->far_rule_cache.begin(); it != g->far_rule_cache.end();) {
+        if (it->first.first == t || it->first.second == t) it = g->far_rule_cache.erase(it);
+        else ++it;
+      }
+      for (auto it = g->near_cache.begin(); it != g->near_cache.end();) {
+        if (it->first.first == t || it->first.second == t) {
+          dead.emplace_back(it->second.d, sizeof(NearPair) * (size_t)it->second.n);
+          it = g->near_cache.erase(it);
+        } else {
+          ++it;
+        }
       }
     }
+    dead.emplace_back(t->d_rec, sizeof(TriRec) * (size_t)t->ntri);
+    geom_freed = geom_release(t->geom, dead);
+    delete t;
   }
-  cudaFree(t->d_rec);
-  geom_freed = geom_release(t->geom);
-  delete t;
-  }
+  for (auto &d : dead) bem_defer_free(device, d.first, d.second);
   if (geom_freed) ctx_release(ctx);
   return BEMGPU_OK;
 }

@@ -520,7 +520,22 @@ int bem_cgemm_tc(bemgpu_ctx_s *ctx, int kind, int m, int n, int k, float sign, c
   }
   {
     const double cbytes = (out == TC_OUT_F32 ? 4.0 : 8.0) * 2.0 * m * n * (accumulate ? 2.0 : 1.0);
-    ProfScope ps(ctx, kind, st, 8.0 * m * n * (double)k, 12.0 * ((double)Mp * Kp + (double)Np * Kp) + cbytes);
+    // a triangular A: only the K steps the kernel runs for each M tile (the
+    // bounds of tc_gemm_kernel) count as work
+    double run = 1.0;
+    if (tri) {
+      const int64_t mtiles = Mp / TC_BM, ktiles = Kp / TC_BK;
+      int64_t steps = 0;
+      for (int64_t mt = 0; mt < mtiles; mt++) {
+        const int64_t m0 = mt * TC_BM;
+        const int64_t kb = tri == 2 ? m0 / TC_BK : 0;
+        const int64_t ke = tri == 1 ? std::min(ktiles, (m0 + TC_BM + TC_BK - 1) / TC_BK) : ktiles;
+        steps += std::max<int64_t>(0, ke - kb);
+      }
+      run = (double)steps / ((double)mtiles * (double)ktiles);
+    }
+    ProfScope ps(ctx, kind, st, 8.0 * m * n * (double)k * run,
+                 12.0 * ((double)Mp * Kp * run + (double)Np * Kp) + cbytes);
     ps.tensor = 6.0 * ps.flops;  // slice products (a, b) with a + b <= 2 of 3 slices
     const dim3 grid((unsigned)(Mp / TC_BM), (unsigned)(Np / bn));
     const int kt = (int)(Kp / TC_BK);

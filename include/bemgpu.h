@@ -195,7 +195,18 @@ int bemgpu_geom_destroy(bemgpu_geom_t g);
  * vertex 1, edge vertex 2}; row i is matrix unknown pair (2i: J, 2i+1: M).
  * Precomputes the half-RWG frames (HalfRWG::HalfRWG, src/RWG.cpp:7-39). */
 int bemgpu_tree_create(bemgpu_geom_t g, const int *rwg, int nrwg, bemgpu_tree_t *out);
+/* Destroying a tree or geometry does not wait for the device: its device
+ * memory (triangle records, near-pair lists) joins a process-wide list that
+ * is freed in one batch, after one device synchronisation, once it holds 96
+ * blocks or 512 MB, on bemgpu_ctx_trim, when a context is torn down, and
+ * before a failed allocation is retried.  (cudaFree waits for the whole
+ * device: freeing each request's geometry at once would drain every farm
+ * lane's work per request.)  A tree must not be destroyed while a call that
+ * uses it is running. */
 int bemgpu_tree_destroy(bemgpu_tree_t t);
+/* Bytes of destroyed trees' and geometries' device memory awaiting the next
+ * batch free. */
+int64_t bemgpu_pending_free_bytes(void);
 int bemgpu_tree_size(bemgpu_tree_t t);
 /* RWG table of one closed body, in the reference's edge-creation order
  * (ShapeMesh::ShapeMesh, src/ShapeMesh.cpp:857-928): triangles in order, each
