@@ -624,6 +624,10 @@ int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value) {
       if (value < 1 || value > 64) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: near_grid %d not in 1..64", value);
       ctx->tune.near_grid = value;
       return BEMGPU_OK;
+    case BEMGPU_TUNE_EX_WIDE:
+      if (value < 0 || value > 1) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: ex_wide %d not 0 or 1", value);
+      ctx->tune.ex_wide = value;
+      return BEMGPU_OK;
     default:
       return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
   }
@@ -638,6 +642,7 @@ int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value) {
     case BEMGPU_TUNE_PANEL_CTAS: *value = ctx->tune.panel_ctas; return BEMGPU_OK;
     case BEMGPU_TUNE_NEAR_SYNC: *value = ctx->tune.near_sync; return BEMGPU_OK;
     case BEMGPU_TUNE_NEAR_GRID: *value = ctx->tune.near_grid; return BEMGPU_OK;
+    case BEMGPU_TUNE_EX_WIDE: *value = ctx->tune.ex_wide; return BEMGPU_OK;
     default: return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
   }
 }

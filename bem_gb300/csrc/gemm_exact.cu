@@ -290,6 +290,225 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
   }
 }
 
+// ---------------- wide tiles: 128 x 128 of D' ----------------
+//
+// The same exact product with N = 128 MMAs (the tensor rate of M = 128, N =
+// 128 against two thirds of it for N = 64).  TMEM holds 4 x 128 columns: the
+// exact levels 0, 1, 2 once each (not double-buffered: 768 columns would not
+// fit) and one FP32 buffer summing levels 3 and 4 over the whole K.  Per
+// 128-deep exponent block (4 TMA stages of 32-deep K steps, 64-byte rows)
+// the MMA thread issues each stage's level-3/4 products first; at a block's
+// first stage it then waits, level by level, until the epilogue has drained
+// that level of the previous block (one mbarrier per level), so the drain
+// runs under the level-3/4 products and the MMAs into levels already drained.
+// Sixteen epilogue warps (a TMEM lane quarter and 32 columns each) drain level
+// 0, then 1, then 2 into their two-float (hi, lo) sums in the same order per
+// entry as ex_gemm_kernel (TwoSum X0, TwoSum X1, lo += X2).  Used for products
+// with level-3/4 work to hide the drain under (5 x 2, 5 x 3, 4 x 4); every
+// wait is bounded.
+constexpr int EXW_BN = 128;
+constexpr int EXW_BK = 32;
+constexpr int EXW_DRAIN = 128 / EXW_BK;  // TMA stages per exponent block
+constexpr int EXW_EPI_WARPS = 16;
+constexpr int EXW_THREADS = 64 + 32 * EXW_EPI_WARPS;
+constexpr int EXW_TMEM_COLS = 512;  // levels 0, 1, 2 and levels >= 3, 128 columns each
+constexpr int EXW_ZCOL = 3 * EXW_BN;
+
+template <int SA, int SB>
+struct ExWCfg {
+  static constexpr int TILE = EX_BM * EXW_BK * 2;  // one slice tile, A or B (128 rows)
+  static constexpr int STAGE = (SA + SB) * TILE;
+  static constexpr int STAGES = (EX_SMEM_MAX - 1280) / STAGE < 4 ? (EX_SMEM_MAX - 1280) / STAGE : 4;
+  static constexpr int SMEM = STAGES * STAGE + 1024 + 256;
+  static_assert(STAGES >= 3 && SMEM <= EX_SMEM_MAX, "exact gemm (wide tiles): shared memory");
+};
+template <int SA, int SB>
+__host__ __device__ constexpr int exw_smem_bytes() { return ExWCfg<SA, SB>::SMEM; }
+
+template <int SA, int SB>
+__global__ void __launch_bounds__(EXW_THREADS, 1)
+    ex_gemm_wide_kernel(const __grid_constant__ ExMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf,
+                        int mvalid, int nvalid, int accumulate, const int *__restrict__ shifts, int raster, int *err) {
+  typedef ExWCfg<SA, SB> CF;
+  constexpr int STAGE = CF::STAGE, NST = CF::STAGES, TILE = CF::TILE;
+  static_assert(SA >= 4, "wide tiles need level-3/4 products to hide the drain under");
+  extern __shared__ unsigned char ex_smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(ex_smem_raw) + 1023) &
+                                                          ~(uintptr_t)1023);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NST * STAGE);
+  uint64_t *empty = full + NST;
+  uint64_t *accf = empty + NST;  // a block's levels 0..2 written (MMA -> epilogue)
+  uint64_t *accx = accf + 1;     // level L of the last block drained (epilogue -> MMA), L = 0, 1, 2
+  uint64_t *fin = accx + 3;      // all MMAs of this CTA complete
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(fin + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int mt, nt;
+  grouped_tile(raster, mt, nt);
+  const int m0 = mt * EX_BM, n0 = nt * EXW_BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accf, 1);
+    for (int l = 0; l < 3; l++) mbar_init(&accx[l], EXW_EPI_WARPS);
+    mbar_init(fin, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(EXW_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int kt = 0; kt < ktiles; kt++) {
+        const int s = kt % NST, round = kt / NST;
+        if (kt >= NST && !mbar_wait(&empty[s], (round - 1) & 1, err)) break;
+        mbar_expect_tx(&full[s], STAGE);
+        unsigned char *st = smem + s * STAGE;
+#pragma unroll
+        for (int a = 0; a < SA; a++) tma_load_2d(st + a * TILE, &maps.a[a], kt * EXW_BK, m0, &full[s]);
+#pragma unroll
+        for (int b = 0; b < SB; b++) tma_load_2d(st + (SA + b) * TILE, &maps.b[b], kt * EXW_BK, n0, &full[s]);
+        issued = kt + 1;
+      }
+      // copies still in flight after an early stop land before the CTA exits
+      for (int kt = issued > NST ? issued - NST : 0; kt < issued; kt++)
+        if (!mbar_wait(&full[kt % NST], (kt / NST) & 1, err)) break;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(EX_BM, EXW_BN);
+      bool ok = true, zfirst = true;
+      for (int kt = 0; kt < ktiles && ok; kt++) {
+        const int s = kt % NST, round = kt / NST, dt = kt / EXW_DRAIN, q = kt % EXW_DRAIN;
+        if (!mbar_wait(&full[s], round & 1, err)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint64_t dbase = smem_desc_sw64(smem_u32(smem + s * STAGE));
+        // levels >= 3: one FP32 sum over the whole K
+#pragma unroll
+        for (int ks = 0; ks < EXW_BK / 16; ks++)
+#pragma unroll
+          for (int a = 0; a < SA; a++)
+#pragma unroll
+            for (int b = 0; b < SB; b++) {
+              if (a + b < 3 || a + b >= SA) continue;
+              const uint64_t da = dbase + (uint64_t)((a * TILE + ks * 32) >> 4);
+              const uint64_t db = dbase + (uint64_t)(((SA + b) * TILE + ks * 32) >> 4);
+              tc_mma(tmem + (uint32_t)EXW_ZCOL, da, db, idesc, zfirst ? 0u : 1u);
+              zfirst = false;
+            }
+        // levels 0..2: exact per block; at its first stage a level waits until
+        // the epilogue has drained it
+#pragma unroll
+        for (int l = 0; l < 3; l++) {
+          if (q == 0 && dt >= 1) {
+            if (!mbar_wait(&accx[l], (dt - 1) & 1, err)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+          }
+          const int amin = l - (SB - 1) > 0 ? l - (SB - 1) : 0;
+#pragma unroll
+          for (int ks = 0; ks < EXW_BK / 16; ks++)
+#pragma unroll
+            for (int a = 0; a < SA; a++) {
+              const int b = l - a;
+              if (a > l || b >= SB) continue;
+              const uint64_t da = dbase + (uint64_t)((a * TILE + ks * 32) >> 4);
+              const uint64_t db = dbase + (uint64_t)(((SA + b) * TILE + ks * 32) >> 4);
+              const bool first = q == 0 && ks == 0 && a == amin;
+              tc_mma(tmem + (uint32_t)(l * EXW_BN), da, db, idesc, first ? 0u : 1u);
+            }
+        }
+        if (!ok) break;
+        tc_commit(&empty[s]);
+        if (q == EXW_DRAIN - 1) tc_commit(accf);
+      }
+      tc_commit(fin);
+      mbar_wait(fin, 0, err);
+    }
+  } else {
+    const int quarter = warp & 3, group = (warp - 2) >> 2;  // TMEM lanes 32 quarter.., columns 32 group..
+    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(group * 32);
+    float hi[32], lo[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) hi[j] = lo[j] = 0.f;
+    bool ok = true;
+#pragma unroll 1
+    for (int dt = 0; dt < ktiles / EXW_DRAIN; dt++) {
+      int got = 1;
+      if (lane == 0) got = mbar_wait(accf, dt & 1, err) ? 1 : 0;
+      got = __shfl_sync(0xffffffffu, got, 0);
+      if (!got) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int l = 0; l < 3; l++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) {  // 8 columns per load batch
+          uint32_t v[8];
+          tc_ld8_nowait(lane_base + (uint32_t)(l * EXW_BN + 8 * c), v);
+          tc_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 8; j++) {
+            if (l < 2)
+              two_sum_acc(hi[8 * c + j], lo[8 * c + j], __uint_as_float(v[j]));
+            else
+              lo[8 * c + j] += __uint_as_float(v[j]);
+          }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&accx[l]);
+      }
+    }
+    if (ok) {
+      int got = 1;
+      if (lane == 0) got = mbar_wait(fin, 0, err) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, got, 0) != 0;
+    }
+    const int rho = m0 + quarter * 32 + lane;
+    const double scale = ldexp(1.0, -(shifts[0] + shifts[1]));
+    if (ok) asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      float z[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) z[j] = 0.f;
+      if (ok) tc_ld8(lane_base + (uint32_t)(EXW_ZCOL + 8 * c), z);
+      if (ok && rho < mvalid) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int col = n0 + group * 32 + 8 * c + j;
+          if (col < nvalid) {
+            double *p = C + rho + ldcf * (int64_t)col;
+            const double v = scale * (((double)hi[8 * c + j] + (double)lo[8 * c + j]) + (double)z[j]);
+            *p = accumulate ? *p + v : v;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(EXW_TMEM_COLS));
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -460,7 +679,7 @@ bool bem_exact_available() { return encode_fn() != nullptr; }
 
 size_t bem_exact_operand_bytes(bool is_a, int rows, int k, int slices) {
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
-                          : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
+                          : (((int64_t)rows + EXW_BN - 1) / EXW_BN) * EXW_BN;
   const int64_t kp = ((2 * (int64_t)k + 127) / 128) * 128;
   return sizeof(__nv_bfloat16) * (size_t)slices * rp * kp + 64;
 }
@@ -470,8 +689,9 @@ int bem_exact_prep(bemgpu_ctx_s *ctx, const char *name, bool is_a, const double 
   // 2 slices only for a quantized B operand (the 5 x 2 product)
   if (slices < (quantize ? 2 : 3) || slices > 5) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d slices", slices);
   if (rows <= 0 || k <= 0) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: empty operand");
+  // B rows padded to the wide tile (a multiple of the narrow one)
   const int64_t rp = is_a ? ((2 * (int64_t)rows + EX_BM - 1) / EX_BM) * EX_BM
-                          : (((int64_t)rows + EX_BN - 1) / EX_BN) * EX_BN;
+                          : (((int64_t)rows + EXW_BN - 1) / EXW_BN) * EXW_BN;
   const int64_t kp = ((2 * (int64_t)k + 127) / 128) * 128;  // whole exponent blocks (drain steps)
   if ((is_a ? rp / 2 : rp) > 65535) return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: %d rows too many", rows);
   const std::string base = std::string("ex_") + name;
@@ -530,10 +750,13 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   if (!((SA == SB && SA >= 3 && SA <= 5) || (SA == 5 && (SB == 3 || SB == 2))))
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: slices (%d, %d) not built", SA, SB);
   const int SL = SB;
+  // 128 x 128 tiles where level-3/4 products hide the single-buffered drain
+  const bool wide = ctx->tune.ex_wide && ((SA == 5 && (SB == 2 || SB == 3)) || (SA == 4 && SB == 4));
+  const int bn = wide ? EXW_BN : EX_BN;
   ExMaps maps;
-  const int bk = ex_bk(SA, SB);
+  const int bk = wide ? EXW_BK : ex_bk(SA, SB);
   if (!ex_maps(maps.a, (const __nv_bfloat16 *)a.S, SA, a.rows_p, a.kp, EX_BM, bk) ||
-      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SB, b.rows_p, b.kp, EX_BN, bk))
+      !ex_maps(maps.b, (const __nv_bfloat16 *)b.S, SB, b.rows_p, b.kp, bn, bk))
     return bem_fail(ctx, BEMGPU_ERR_CUDA, "exact gemm: tensor map encoding failed");
   int *err = (int *)bem_workspace(ctx, "tc_err", sizeof(int));
   if (!err) return bem_fail(ctx, BEMGPU_ERR_OOM, "exact gemm: workspace");
@@ -548,6 +771,12 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
                                            ex_smem_bytes<5, 3>()));
     BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            ex_smem_bytes<5, 2>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           exw_smem_bytes<5, 2>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<5, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           exw_smem_bytes<5, 3>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           exw_smem_bytes<4, 4>()));
     ctx->ex_ready = true;
   }
   if (!ctx->tc_err_ready) {
@@ -560,7 +789,7 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(shifts, a.aux, sizeof(int), cudaMemcpyDeviceToDevice, st));
   BEM_CUDA_TRY(ctx, cudaMemcpyAsync(shifts + 1, b.aux, sizeof(int), cudaMemcpyDeviceToDevice, st));
   ProfScope ps(ctx, kind, st, 8.0 * m * (double)n * a.k,
-               2.0 * SA * ((double)a.rows_p * a.kp * ((b.rows_p + EX_BN - 1) / EX_BN) / 8.0) +
+               2.0 * SA * ((double)a.rows_p * a.kp * ((b.rows_p + bn - 1) / bn) / 8.0) +
                    2.0 * SB * (double)b.rows_p * b.kp + 16.0 * m * (double)n * (accumulate ? 2 : 1));
   (void)SL;
   {
@@ -570,9 +799,18 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
       for (int j = 0; j < SB; j++) products += (i + j < SA);
     ps.tensor = products * ps.flops;
   }
-  const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / EX_BN));
+  const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / bn));
   const int ktiles = (int)(a.kp / bk);
-  if (SA == 5 && SB == 2)
+  if (wide && SA == 5 && SB == 2)
+    ex_gemm_wide_kernel<5, 2><<<grid, EXW_THREADS, exw_smem_bytes<5, 2>(), st>>>(
+        maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
+  else if (wide && SA == 5 && SB == 3)
+    ex_gemm_wide_kernel<5, 3><<<grid, EXW_THREADS, exw_smem_bytes<5, 3>(), st>>>(
+        maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
+  else if (wide)
+    ex_gemm_wide_kernel<4, 4><<<grid, EXW_THREADS, exw_smem_bytes<4, 4>(), st>>>(
+        maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
+  else if (SA == 5 && SB == 2)
     ex_gemm_kernel<5, 2><<<grid, EX_THREADS, ex_smem_bytes<5, 2>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,
                                                                           accumulate, shifts, ctx->tune.raster, err);
   else if (SA == 5 && SB == 3)

@@ -143,14 +143,22 @@ int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
  *                          CTAs barrier after each pair couple, keeping their
  *                          warps in the same code region; 0: no barrier;
  *   BEMGPU_TUNE_NEAR_GRID  CTAs per SM of the near-pair launch's grid at most:
- *                          1..64 (default 16).
- * BEMGPU_ERR_ARG for an unknown knob or value.  Results do not depend on them. */
+ *                          1..64 (default 16);
+ *   BEMGPU_TUNE_EX_WIDE    1 (default): the exact products with level-3/4
+ *                          slice products (5 x 2, 5 x 3, 4 x 4) on 128 x 128
+ *                          tiles; 0: all on 128 x 64 tiles.  The two differ
+ *                          in the last bits of an FP32 sum (levels 3 and 4
+ *                          in one buffer or two), well inside the products'
+ *                          2^-40 accuracy.
+ * BEMGPU_ERR_ARG for an unknown knob or value.  Results do not depend on
+ * them, except as BEMGPU_TUNE_EX_WIDE says. */
 #define BEMGPU_TUNE_NEAR_MINB 0
 #define BEMGPU_TUNE_FAR_ROWS 1
 #define BEMGPU_TUNE_RASTER 2
 #define BEMGPU_TUNE_PANEL_CTAS 3
 #define BEMGPU_TUNE_NEAR_SYNC 4
 #define BEMGPU_TUNE_NEAR_GRID 5
+#define BEMGPU_TUNE_EX_WIDE 6
 int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value);
 int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value);
 /* Tracing: with BEMGPU_TRACE set (not "0") in the environment, the library

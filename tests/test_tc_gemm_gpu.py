@@ -275,3 +275,42 @@ def test_tensor_flop_counts_per_product():
                                                            ctypes.c_void_p(dB.data_ptr()), k,
                                                            ctypes.c_void_p(dC.data_ptr()), m, 0))
     assert fl == 8.0 * m * n * k and tf == 12 * fl
+
+
+@pytest.mark.parametrize("quantized", [False, True])
+def test_exact_gemm_wide_and_narrow_tiles_agree(quantized):
+    """The 128 x 128-tile exact product (BEMGPU_TUNE_EX_WIDE, used for 4 x 4,
+    5 x 3 and 5 x 2 slices) against the 128 x 64-tile one on ragged shapes
+    with several M and N tiles and many exponent blocks: levels 0..2 are
+    exact in both, so they differ only by the FP32 rounding of the level-3/4
+    sums (one buffer or two), far below the products' 2^-40."""
+    import torch
+    L = _lib.load()
+    ctx = api.default_context()
+    rng = np.random.default_rng(11 + quantized)
+    m, n, k = 300, 200, 1000
+    A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    B = (rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))) * np.exp(rng.uniform(-4, 4, (k, n)))
+    C0 = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    scale = k * np.outer(np.abs(A).max(axis=1), np.abs(B).max(axis=0))
+
+    def run():
+        dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+        dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+        dC = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda()
+        torch.cuda.synchronize()
+        args = (ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), m, ctypes.c_void_p(dB.data_ptr()), k,
+                ctypes.c_void_p(dC.data_ptr()), m, 1)
+        rc = L.bemgpu_zgemm_exact_quantized(*args) if quantized else L.bemgpu_zgemm_exact(*args, 4)
+        assert rc == 0, L.bemgpu_ctx_last_error(ctx.handle)
+        return dC.cpu().numpy().T
+
+    try:
+        assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 0) == _lib.OK
+        narrow = run()
+        assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 1) == _lib.OK
+        wide = run()
+    finally:
+        L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 1)
+    assert np.max(np.abs(wide - narrow) / scale) < 2.0 ** -44
+    assert not np.array_equal(wide, np.asarray(C0, dtype=np.complex128))
