@@ -625,7 +625,7 @@ int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value) {
       ctx->tune.near_grid = value;
       return BEMGPU_OK;
     case BEMGPU_TUNE_EX_WIDE:
-      if (value < 0 || value > 1) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: ex_wide %d not 0 or 1", value);
+      if (value < 0 || value > 2) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: ex_wide %d not 0, 1 or 2", value);
       ctx->tune.ex_wide = value;
       return BEMGPU_OK;
     default:

@@ -750,8 +750,14 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   if (!((SA == SB && SA >= 3 && SA <= 5) || (SA == 5 && (SB == 3 || SB == 2))))
     return bem_fail(ctx, BEMGPU_ERR_ARG, "exact gemm: slices (%d, %d) not built", SA, SB);
   const int SL = SB;
-  // 128 x 128 tiles where level-3/4 products hide the single-buffered drain
-  const bool wide = ctx->tune.ex_wide && ((SA == 5 && (SB == 2 || SB == 3)) || (SA == 4 && SB == 4));
+  // 128 x 128 tiles where level-3/4 products hide the single-buffered drain,
+  // for grids of at least 4 waves (a smaller grid leaves more of its last
+  // wave's SMs idle with half as many tiles; ex_gemm_wide_kernel<5, 2> at
+  // 240 tiles took 342 us against 312 for 450 narrow ones); BEMGPU_TUNE_EX_WIDE
+  // 2 takes them whatever the grid
+  const int64_t wtiles = (a.rows_p / EX_BM) * ((b.rows_p + EXW_BN - 1) / EXW_BN);
+  const bool wide = ((SA == 5 && (SB == 2 || SB == 3)) || (SA == 4 && SB == 4)) &&
+                    (ctx->tune.ex_wide == 2 || (ctx->tune.ex_wide == 1 && wtiles >= 4 * (int64_t)ctx->num_sms));
   const int bn = wide ? EXW_BN : EX_BN;
   ExMaps maps;
   const int bk = wide ? EXW_BK : ex_bk(SA, SB);

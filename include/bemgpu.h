@@ -146,10 +146,11 @@ int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
  *                          1..64 (default 16);
  *   BEMGPU_TUNE_EX_WIDE    1 (default): the exact products with level-3/4
  *                          slice products (5 x 2, 5 x 3, 4 x 4) on 128 x 128
- *                          tiles; 0: all on 128 x 64 tiles.  The two differ
- *                          in the last bits of an FP32 sum (levels 3 and 4
- *                          in one buffer or two), well inside the products'
- *                          2^-40 accuracy.
+ *                          tiles when that grid has at least 4 waves; 2:
+ *                          on 128 x 128 tiles at any size; 0: all on
+ *                          128 x 64 tiles.  The two differ in the last bits
+ *                          of an FP32 sum (levels 3 and 4 in one buffer or
+ *                          two), well inside the products' 2^-40 accuracy.
  * BEMGPU_ERR_ARG for an unknown knob or value.  Results do not depend on
  * them, except as BEMGPU_TUNE_EX_WIDE says. */
 #define BEMGPU_TUNE_NEAR_MINB 0

@@ -60,5 +60,5 @@ def test_results_do_not_depend_on_the_launch_shapes(tmp_path):
     assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_NEAR_SYNC, 2) == _lib.ERR_ARG
     assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_NEAR_GRID, 0) == _lib.ERR_ARG
     assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_PANEL_CTAS, -1) == _lib.ERR_ARG
-    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 2) == _lib.ERR_ARG
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 3) == _lib.ERR_ARG
     assert L.bemgpu_ctx_set_tuning(ctx.handle, 99, 1) == _lib.ERR_ARG
