@@ -294,18 +294,21 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 //
 // The same exact product with N = 128 MMAs (the tensor rate of M = 128, N =
 // 128 against two thirds of it for N = 64).  TMEM holds 4 x 128 columns: the
-// exact levels 0, 1, 2 once each (not double-buffered: 768 columns would not
-// fit) and one FP32 buffer summing levels 3 and 4 over the whole K.  Per
+// exact levels below ZLEV once each (not double-buffered: 768 columns would
+// not fit) and one FP32 buffer summing the levels from ZLEV up over the whole
+// K.  ZLEV = 3 keeps levels 0..2 exact as ex_gemm_kernel does (the quantized
+// 5 x 2 and 5 x 3 products, whose truncation is 2^-40); ZLEV = 2 for the
+// plain 4 x 4 and 3 x 3 products, whose truncation (2^-32, 2^-24 of the
+// block maxima products) is far above the 2^-40 an FP32 level 2 adds.  Per
 // 128-deep exponent block (4 TMA stages of 32-deep K steps, 64-byte rows)
 // the MMA thread issues each stage's level-3/4 products first; at a block's
 // first stage it then waits, level by level, until the epilogue has drained
 // that level of the previous block (one mbarrier per level), so the drain
 // runs under the level-3/4 products and the MMAs into levels already drained.
-// Sixteen epilogue warps (a TMEM lane quarter and 32 columns each) drain level
-// 0, then 1, then 2 into their two-float (hi, lo) sums in the same order per
-// entry as ex_gemm_kernel (TwoSum X0, TwoSum X1, lo += X2).  Used for products
-// with level-3/4 work to hide the drain under (5 x 2, 5 x 3, 4 x 4); every
-// wait is bounded.
+// Sixteen epilogue warps (a TMEM lane quarter and 32 columns each) drain the
+// exact levels one after the other into their two-float (hi, lo) sums in the
+// same order per entry as ex_gemm_kernel (TwoSum X0, TwoSum X1, lo += X2).
+// Every wait is bounded.
 constexpr int EXW_BN = 128;
 constexpr int EXW_BK = 32;
 constexpr int EXW_DRAIN = 128 / EXW_BK;  // TMA stages per exponent block
@@ -325,13 +328,13 @@ struct ExWCfg {
 template <int SA, int SB>
 __host__ __device__ constexpr int exw_smem_bytes() { return ExWCfg<SA, SB>::SMEM; }
 
-template <int SA, int SB>
+template <int SA, int SB, int ZLEV>
 __global__ void __launch_bounds__(EXW_THREADS, 1)
     ex_gemm_wide_kernel(const __grid_constant__ ExMaps maps, int ktiles, double *__restrict__ C, int64_t ldcf,
                         int mvalid, int nvalid, int accumulate, const int *__restrict__ shifts, int raster, int *err) {
   typedef ExWCfg<SA, SB> CF;
   constexpr int STAGE = CF::STAGE, NST = CF::STAGES, TILE = CF::TILE;
-  static_assert(SA >= 4, "wide tiles need level-3/4 products to hide the drain under");
+  static_assert(ZLEV >= 2 && ZLEV <= 3 && SA > ZLEV, "wide tiles need FP32-summed levels to hide the drain under");
   extern __shared__ unsigned char ex_smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(ex_smem_raw) + 1023) &
                                                           ~(uintptr_t)1023);
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(EXW_THREADS, 1)
           for (int a = 0; a < SA; a++)
 #pragma unroll
             for (int b = 0; b < SB; b++) {
-              if (a + b < 3 || a + b >= SA) continue;
+              if (a + b < ZLEV || a + b >= SA) continue;
               const uint64_t da = dbase + (uint64_t)((a * TILE + ks * 32) >> 4);
               const uint64_t db = dbase + (uint64_t)(((SA + b) * TILE + ks * 32) >> 4);
               tc_mma(tmem + (uint32_t)EXW_ZCOL, da, db, idesc, zfirst ? 0u : 1u);
@@ -409,7 +412,7 @@ __global__ void __launch_bounds__(EXW_THREADS, 1)
         // levels 0..2: exact per block; at its first stage a level waits until
         // the epilogue has drained it
 #pragma unroll
-        for (int l = 0; l < 3; l++) {
+        for (int l = 0; l < ZLEV; l++) {
           if (q == 0 && dt >= 1) {
             if (!mbar_wait(&accx[l], (dt - 1) & 1, err)) {
               ok = false;
@@ -455,7 +458,7 @@ __global__ void __launch_bounds__(EXW_THREADS, 1)
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-      for (int l = 0; l < 3; l++) {
+      for (int l = 0; l < ZLEV; l++) {
 #pragma unroll
         for (int c = 0; c < 4; c++) {  // 8 columns per load batch
           uint32_t v[8];
@@ -756,7 +759,7 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   // 240 tiles took 342 us against 312 for 450 narrow ones); BEMGPU_TUNE_EX_WIDE
   // 2 takes them whatever the grid
   const int64_t wtiles = (a.rows_p / EX_BM) * ((b.rows_p + EXW_BN - 1) / EXW_BN);
-  const bool wide = ((SA == 5 && (SB == 2 || SB == 3)) || (SA == 4 && SB == 4)) &&
+  const bool wide = ((SA == 5 && (SB == 2 || SB == 3)) || (SA == SB && (SA == 4 || SA == 3))) &&
                     (ctx->tune.ex_wide == 2 || (ctx->tune.ex_wide == 1 && wtiles >= 4 * (int64_t)ctx->num_sms));
   const int bn = wide ? EXW_BN : EX_BN;
   ExMaps maps;
@@ -777,12 +780,14 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
                                            ex_smem_bytes<5, 3>()));
     BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_kernel<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            ex_smem_bytes<5, 2>()));
-    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<5, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           exw_smem_bytes<5, 2>()));
-    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<5, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           exw_smem_bytes<5, 3>()));
-    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<4, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           exw_smem_bytes<4, 4>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<5, 2, 3>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, exw_smem_bytes<5, 2>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<5, 3, 3>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, exw_smem_bytes<5, 3>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<4, 4, 2>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, exw_smem_bytes<4, 4>()));
+    BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(ex_gemm_wide_kernel<3, 3, 2>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, exw_smem_bytes<3, 3>()));
     ctx->ex_ready = true;
   }
   if (!ctx->tc_err_ready) {
@@ -808,13 +813,16 @@ int bem_exact_gemm(bemgpu_ctx_s *ctx, int kind, const ExactOperand &a, const Exa
   const dim3 grid((unsigned)(a.rows_p / EX_BM), (unsigned)(b.rows_p / bn));
   const int ktiles = (int)(a.kp / bk);
   if (wide && SA == 5 && SB == 2)
-    ex_gemm_wide_kernel<5, 2><<<grid, EXW_THREADS, exw_smem_bytes<5, 2>(), st>>>(
+    ex_gemm_wide_kernel<5, 2, 3><<<grid, EXW_THREADS, exw_smem_bytes<5, 2>(), st>>>(
         maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
   else if (wide && SA == 5 && SB == 3)
-    ex_gemm_wide_kernel<5, 3><<<grid, EXW_THREADS, exw_smem_bytes<5, 3>(), st>>>(
+    ex_gemm_wide_kernel<5, 3, 3><<<grid, EXW_THREADS, exw_smem_bytes<5, 3>(), st>>>(
+        maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
+  else if (wide && SA == 4)
+    ex_gemm_wide_kernel<4, 4, 2><<<grid, EXW_THREADS, exw_smem_bytes<4, 4>(), st>>>(
         maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
   else if (wide)
-    ex_gemm_wide_kernel<4, 4><<<grid, EXW_THREADS, exw_smem_bytes<4, 4>(), st>>>(
+    ex_gemm_wide_kernel<3, 3, 2><<<grid, EXW_THREADS, exw_smem_bytes<3, 3>(), st>>>(
         maps, ktiles, C, 2 * ldc, 2 * m, n, accumulate, shifts, ctx->tune.raster, err);
   else if (SA == 5 && SB == 2)
     ex_gemm_kernel<5, 2><<<grid, EX_THREADS, ex_smem_bytes<5, 2>(), st>>>(maps, ktiles, C, 2 * ldc, 2 * m, n,

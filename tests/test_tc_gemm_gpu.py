@@ -277,13 +277,17 @@ def test_tensor_flop_counts_per_product():
     assert fl == 8.0 * m * n * k and tf == 12 * fl
 
 
-@pytest.mark.parametrize("quantized", [False, True])
-def test_exact_gemm_wide_and_narrow_tiles_agree(quantized):
-    """The 128 x 128-tile exact product (BEMGPU_TUNE_EX_WIDE, used for 4 x 4,
-    5 x 3 and 5 x 2 slices on large grids) against the 128 x 64-tile one on ragged shapes
-    with several M and N tiles and many exponent blocks: levels 0..2 are
-    exact in both, so they differ only by the FP32 rounding of the level-3/4
-    sums (one buffer or two), far below the products' 2^-40."""
+@pytest.mark.parametrize("slices", [3, 4, "quantized"])
+def test_exact_gemm_wide_and_narrow_tiles_agree(slices):
+    """The 128 x 128-tile exact product (BEMGPU_TUNE_EX_WIDE: 3 x 3, 4 x 4,
+    5 x 3 and 5 x 2 slices on large grids) against the 128 x 64-tile one on
+    ragged shapes with several M and N tiles and many exponent blocks.  The
+    quantized 5 x 3 product keeps levels 0..2 exact in both, so they differ
+    only by the FP32 rounding of the level-3/4 sums (one buffer or two), far
+    below its 2^-40; the wide 3 x 3 and 4 x 4 products sum level 2 in FP32
+    too (2^-40 of the block maxima products, below their own truncation at
+    2^-24 and 2^-32)."""
+    quantized = slices == "quantized"
     import torch
     L = _lib.load()
     ctx = api.default_context()
@@ -301,7 +305,7 @@ def test_exact_gemm_wide_and_narrow_tiles_agree(quantized):
         torch.cuda.synchronize()
         args = (ctx.handle, m, n, k, ctypes.c_void_p(dA.data_ptr()), m, ctypes.c_void_p(dB.data_ptr()), k,
                 ctypes.c_void_p(dC.data_ptr()), m, 1)
-        rc = L.bemgpu_zgemm_exact_quantized(*args) if quantized else L.bemgpu_zgemm_exact(*args, 4)
+        rc = L.bemgpu_zgemm_exact_quantized(*args) if quantized else L.bemgpu_zgemm_exact(*args, slices)
         assert rc == 0, L.bemgpu_ctx_last_error(ctx.handle)
         return dC.cpu().numpy().T
 
@@ -313,5 +317,5 @@ def test_exact_gemm_wide_and_narrow_tiles_agree(quantized):
         wide = run()
     finally:
         L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 1)
-    assert np.max(np.abs(wide - narrow) / scale) < 2.0 ** -44
+    assert np.max(np.abs(wide - narrow) / scale) < (2.0 ** -44 if quantized else 2.0 ** -36)
     assert not np.array_equal(wide, np.asarray(C0, dtype=np.complex128))
