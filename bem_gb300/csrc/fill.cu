@@ -1069,15 +1069,24 @@ __device__ __noinline__ void near_finish_df(const TriRec &T, const TriRec &S, in
 // sums of the pair its node belongs to, and the warp finishes the pairs one
 // after the other.
 // The pair couple (p0, p0 + 1) of `list` (one pair when p0 + 1 == npairs),
-// worked by one warp; nodes, pc: the warp's shared staging, outer: the outer
-// rule in double-float.
-__device__ __forceinline__ void near_couple_df(const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr,
-                                               const NearPair *__restrict__ list, int64_t npairs, int64_t p0,
-                                               const GreenDev &g, HalfPairBlock *__restrict__ H, int ntr,
-                                               float (*nodes)[BEMGPU_TRI_RULE91_N][8], const float (*outer)[6],
-                                               NearPairDF *pcs, int lane) {
-  const int np2 = p0 + 1 < npairs ? 2 : 1;
+// worked by one warp in two parts: near_couple_df_sums runs the 2 x 105 outer
+// nodes (inner rule, closed forms, contraction) into acc, near_couple_df_finish
+// the warp sums, the neighbour-edge correction and the scatter.  nodes, pc:
+// the warp's shared staging, outer: the outer rule in double-float.
+struct NearCouple {
   NearPair npr[2];
+  int np2;
+  NearAccDF acc[2];
+};
+
+__device__ __forceinline__ void near_couple_df_sums(const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr,
+                                                    const NearPair *__restrict__ list, int64_t npairs, int64_t p0,
+                                                    const GreenDev &g, float (*nodes)[BEMGPU_TRI_RULE91_N][8],
+                                                    const float (*outer)[6], NearPairDF *pcs, int lane,
+                                                    NearCouple &cp) {
+  const int np2 = p0 + 1 < npairs ? 2 : 1;
+  cp.np2 = np2;
+  NearPair *npr = cp.npr;
   npr[0] = list[p0];
   npr[1] = list[np2 == 2 ? p0 + 1 : p0];
   // inner nodes l = r_s - P_s and weights of both pairs, then their records
@@ -1095,7 +1104,7 @@ __device__ __forceinline__ void near_couple_df(const TriRec *__restrict__ Tr, co
   }
   if (lane < np2) near_pair_df_setup(Tr[npr[lane].t], Sr[npr[lane].s], g, pcs[lane]);
   __syncwarp();
-  NearAccDF acc[2];
+  NearAccDF *acc = cp.acc;
   const df z = {0.f, 0.f};
 #pragma unroll
   for (int k = 0; k < 9; k++) {
@@ -1113,7 +1122,13 @@ __device__ __forceinline__ void near_couple_df(const TriRec *__restrict__ Tr, co
     near_inner_df<1>(nodes[k], &rs, g, &mom);
     near_outer_df(mom, pc, Tr[npr[k].t].nh, Sr[npr[k].s].nh, rt1, wq, acc[k]);
   }
-  for (int k = 0; k < np2; k++) near_finish_df(Tr[npr[k].t], Sr[npr[k].s], npr[k].same, pcs[k], acc[k], H, ntr);
+}
+
+__device__ __forceinline__ void near_couple_df_finish(const TriRec *__restrict__ Tr, const TriRec *__restrict__ Sr,
+                                                      HalfPairBlock *__restrict__ H, int ntr, const NearPairDF *pcs,
+                                                      const NearCouple &cp) {
+  for (int k = 0; k < cp.np2; k++)
+    near_finish_df(Tr[cp.npr[k].t], Sr[cp.npr[k].s], cp.npr[k].same, pcs[k], cp.acc[k], H, ntr);
   __syncwarp();
 }
 
@@ -1133,10 +1148,11 @@ __device__ __forceinline__ void stage_outer_df(float (*outer)[6]) {
 // register allocation must allow (2: ~250 registers; 3: 168; 4: 128 with
 // spills), chosen by the context's tuning.
 // Warp w of CTA b takes units b * NEAR_WARPS + w + k * (grid warps), k = 0, 1, ...
-// SYNC: the CTA's warps meet at a barrier after each unit.  A pair couple runs
-// several large code regions (the inner rule, the closed-form potentials, the
-// edge correction); with two warps per scheduler, warps that have drifted into
-// different regions stall on instruction fetch, which the barrier prevents.
+// SYNC: the CTA's warps meet at a barrier after the outer nodes of each unit
+// and after its finish.  A pair couple runs several large code regions (the
+// inner rule, the closed-form potentials, the edge correction); with two warps
+// per scheduler, warps that have drifted into different regions stall on
+// instruction fetch, which the barriers prevent.
 // The units and their order per warp are the same either way.
 template <int MINB, bool SYNC>
 __global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_pairs_df_group_kernel(const FillTask *__restrict__ tasks,
@@ -1152,18 +1168,24 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS, MINB) near_pairs_df_group_ker
   int cur = -1;
   for (int64_t base = (int64_t)blockIdx.x * NEAR_WARPS; base < units; base += nw) {
     const int64_t u = base + wid;
-    if (u < units) {
+    const bool active = u < units;
+    NearCouple cp;
+    const FillTask *tk = nullptr;
+    if (active) {
       const int i = task_of_near(tasks, ntask, u);
-      const FillTask &tk = tasks[i];
+      tk = &tasks[i];
       if (i != cur) {
-        if (lane == 0) s_g[wid] = tk.g;
+        if (lane == 0) s_g[wid] = tk->g;
         __syncwarp();
         cur = i;
       }
-      near_couple_df(tk.T, tk.S, tk.near, tk.nnear, 2 * (u - tk.near0), s_g[wid], tk.H, tk.ntr, s_nodes[wid],
-                     s_outer, s_pc[wid], lane);
+      near_couple_df_sums(tk->T, tk->S, tk->near, tk->nnear, 2 * (u - tk->near0), s_g[wid], s_nodes[wid], s_outer,
+                          s_pc[wid], lane, cp);
     }
-    if (SYNC) __syncthreads();  // base is the same for the whole CTA
+    // base is the same for the whole CTA: every warp meets both barriers
+    if (SYNC) __syncthreads();
+    if (active) near_couple_df_finish(tk->T, tk->S, tk->H, tk->ntr, s_pc[wid], cp);
+    if (SYNC) __syncthreads();
   }
 }
 
