@@ -18,7 +18,8 @@ ERR_CANCELLED = -8
 PENDING = 1
 K_NAMES = ["fill_far", "fill_near", "gather", "lu_panel", "lu_gemm", "trsm", "solve_gemm", "trace", "refine_gemm",
            "near_spmm", "slice"]
-TUNE_NEAR_MINB, TUNE_FAR_ROWS, TUNE_RASTER, TUNE_PANEL_CTAS, TUNE_NEAR_SYNC, TUNE_NEAR_GRID, TUNE_EX_WIDE = range(7)
+TUNE_NEAR_MINB, TUNE_FAR_ROWS, TUNE_RASTER, TUNE_PANEL_CTAS, TUNE_NEAR_SYNC, TUNE_NEAR_GRID, TUNE_EX_WIDE, \
+    TUNE_LU_SUPER = range(8)
 PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_LA = 2

@@ -113,6 +113,7 @@ struct bemgpu_ctx_s {
     int near_sync = 1;   // double-float near-pair CTAs barrier after each pair couple (0, 1)
     int near_grid = 16;  // CTAs per SM in the near-pair launch's grid at most (1..64)
     int ex_wide = 1;     // exact products with level-3/4 work on 128 x 128 tiles: 0 never, 1 large grids, 2 always
+    int lu_super = 1;    // complex64 LU panels in pairs, trailing updates of K = 256 (0, 1)
   } tune;
   double escalate_tol = 1e-6;  // complex64 refinement error estimate above which the solve escalates
   double fallback_tol = 1e-6;  // FP64-class error estimate above which mode 0 re-solves on the FP64 path

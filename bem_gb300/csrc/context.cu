@@ -628,6 +628,10 @@ int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value) {
       if (value < 0 || value > 2) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: ex_wide %d not 0, 1 or 2", value);
       ctx->tune.ex_wide = value;
       return BEMGPU_OK;
+    case BEMGPU_TUNE_LU_SUPER:
+      if (value < 0 || value > 1) return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: lu_super %d not 0 or 1", value);
+      ctx->tune.lu_super = value;
+      return BEMGPU_OK;
     default:
       return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
   }
@@ -643,6 +647,7 @@ int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value) {
     case BEMGPU_TUNE_NEAR_SYNC: *value = ctx->tune.near_sync; return BEMGPU_OK;
     case BEMGPU_TUNE_NEAR_GRID: *value = ctx->tune.near_grid; return BEMGPU_OK;
     case BEMGPU_TUNE_EX_WIDE: *value = ctx->tune.ex_wide; return BEMGPU_OK;
+    case BEMGPU_TUNE_LU_SUPER: *value = ctx->tune.lu_super; return BEMGPU_OK;
     default: return bem_fail(ctx, BEMGPU_ERR_ARG, "tuning: unknown knob %d", knob);
   }
 }

@@ -967,9 +967,18 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A0, int64_t lda, int n, int *d_ipiv0, int *
   const T mone[2] = {T(-1), T(0)}, one[2] = {T(1), T(0)};
   const double cb = 2.0 * sizeof(T);  // bytes per complex element
   constexpr int NBL = LuCfg<T>::NBL;
+  // complex64 super-blocks (BEMGPU_TUNE_LU_SUPER): panels in pairs A, B.
+  // After A only B's columns take A's update; after B the rows of B and then
+  // the trailing matrix beyond the pair take both at once, the latter as one
+  // K = 2 NBL product (half the passes over the trailing matrix).  The same
+  // updates as one panel at a time, associated differently.
+  const bool super = sizeof(T) == 4 && ctx->tune.lu_super != 0;
   for (int k0 = 0; k0 < n; k0 += NBL) {
     const int w = std::min(NBL, n - k0);
     const int rows = n - k0;
+    const bool first_half = super && (k0 / NBL) % 2 == 0;   // panel A (its B follows when k0 + w < n)
+    const bool second_half = super && (k0 / NBL) % 2 == 1;  // panel B
+    const int K0 = second_half ? k0 - NBL : k0;              // the pair's first column
     const int blocks = std::max(1, std::min(ctx->num_sms * 2, (rows + PANEL_THREADS - 1) / PANEL_THREADS));
     int prc = BEMGPU_OK;
     bool coop = ctx->coop_panel && panel_coop<T>(ctx, A0, lda, n, k0, w, d_ipiv0, d_info0, stream, prc, nb, strideA);
@@ -1016,15 +1025,33 @@ int getrf_impl(bemgpu_ctx_s *ctx, T *A0, int64_t lda, int n, int *d_ipiv0, int *
           laswp_perm_kernel<T><<<g, 32 * LASWP_WARPS, 0, stream>>>(A, lda, k0 + w, n, k0, k0 + w, d_ipiv);
           ctx->launches++;
         }
+        if (second_half) {
+          // panel A's update of B's rows beyond the pair:
+          // A[k0:k0+w, k0+w:n] -= L[k0:k0+w, K0:k0] U[K0:k0, k0+w:n]
+          int rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', w, nr, k0 - K0, mone, A + 2 * (k0 + lda * (int64_t)K0),
+                               lda, A + 2 * (K0 + lda * (int64_t)(k0 + w)), lda, one, A12, lda, stream);
+          if (rc) return rc;
+        }
         {
           ProfScope ps(ctx, BEMGPU_K_TRSM, stream, 4.0 * w * w * nr, 2.0 * cb * w * nr);
           trsm_block_kernel<T, false, NBL / 32>
               <<<tb, 256, trsm_smem_bytes<T, NBL / 32>(), stream>>>(A11, lda, w, A12, lda, nr);
           ctx->launches++;
         }
-        T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
         T *A22 = A + 2 * (k0 + w + lda * (int64_t)(k0 + w));
-        int rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, w, mone, A21, lda, A12, lda, one, A22, lda, stream);
+        int rc;
+        if (first_half) {
+          // panel B's columns only; the rest waits for B
+          T *A21 = A + 2 * (k0 + w + lda * (int64_t)k0);
+          rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, std::min(NBL, nr), w, mone, A21, lda, A12, lda, one, A22,
+                           lda, stream);
+        } else {
+          // the trailing matrix from the pair's panels at once (K = k0 + w - K0)
+          T *L21 = A + 2 * (k0 + w + lda * (int64_t)K0);
+          T *U12 = A + 2 * (K0 + lda * (int64_t)(k0 + w));
+          rc = gemm_any<T>(ctx, BEMGPU_K_LU_GEMM, 'N', nr, nr, k0 + w - K0, mone, L21, lda, U12, lda, one, A22, lda,
+                           stream);
+        }
         if (rc) return rc;
       }
       BEM_CUDA_TRY(ctx, cudaGetLastError());

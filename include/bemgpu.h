@@ -150,9 +150,13 @@ int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
  *                          on 128 x 128 tiles at any size; 0: all on
  *                          128 x 64 tiles.  The two differ in the last bits
  *                          of an FP32 sum (levels 3 and 4 in one buffer or
- *                          two), well inside the products' 2^-40 accuracy.
+ *                          two), well inside the products' 2^-40 accuracy;
+ *   BEMGPU_TUNE_LU_SUPER   1 (default): the complex64 LU factors its 128-wide
+ *                          panels in pairs and updates the trailing matrix
+ *                          once per pair (K = 256); 0: after every panel.
+ *                          The same updates, rounded in another order.
  * BEMGPU_ERR_ARG for an unknown knob or value.  Results do not depend on
- * them, except as BEMGPU_TUNE_EX_WIDE says. */
+ * them, except as BEMGPU_TUNE_EX_WIDE and BEMGPU_TUNE_LU_SUPER say. */
 #define BEMGPU_TUNE_NEAR_MINB 0
 #define BEMGPU_TUNE_FAR_ROWS 1
 #define BEMGPU_TUNE_RASTER 2
@@ -160,6 +164,7 @@ int bemgpu_ctx_set_fp64_fallback_tol(bemgpu_ctx_t ctx, double tol);
 #define BEMGPU_TUNE_NEAR_SYNC 4
 #define BEMGPU_TUNE_NEAR_GRID 5
 #define BEMGPU_TUNE_EX_WIDE 6
+#define BEMGPU_TUNE_LU_SUPER 7
 int bemgpu_ctx_set_tuning(bemgpu_ctx_t ctx, int knob, int value);
 int bemgpu_ctx_get_tuning(bemgpu_ctx_t ctx, int knob, int *value);
 /* Tracing: with BEMGPU_TRACE set (not "0") in the environment, the library

@@ -62,3 +62,37 @@ def test_results_do_not_depend_on_the_launch_shapes(tmp_path):
     assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_PANEL_CTAS, -1) == _lib.ERR_ARG
     assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_EX_WIDE, 3) == _lib.ERR_ARG
     assert L.bemgpu_ctx_set_tuning(ctx.handle, 99, 1) == _lib.ERR_ARG
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mesh_kind", ["ico2", "cube4"])
+def test_paired_lu_panels_factor_as_well(mesh_kind):
+    """BEMGPU_TUNE_LU_SUPER: the complex64 LU with its panels in pairs (one
+    K = 256 trailing update per pair) against one panel at a time.  The
+    refinement would hide a wrong factorization as slow convergence, so both
+    must converge on the complex64 path in the same number of steps, to the
+    same spectral power within the refinement's accuracy.  ico2 (N = 1920:
+    15 panels, an unpaired last one) and cube4 (N = 1152: 9 panels)."""
+    from bem_gb300 import api, mesh, _lib
+    L = _lib.load()
+    if mesh_kind == "ico2":
+        v, t = mesh.icosphere(1.0, 2, jitter=0.02, seed=12345)
+    else:
+        v, t = mesh.cube(1.0, 4)
+    b2 = mesh.Body.from_mesh(v, t)
+    b1 = b2.translated(mesh.gap_translation(v, v, 0.05))
+    d = api.FixedLorentz(*api.SIC_CONFIG)
+    ctx = api.Context(0)
+    top, s, tt = api.parseShapes(b1, b2, d, d, ctx)
+    assert L.bemgpu_ctx_set_solver(ctx.handle, 1) == _lib.OK  # complex64 only: no escalation
+    out = {}
+    for sup in (0, 1):
+        assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_LU_SUPER, sup) == _lib.OK
+        info = {}
+        P = api.CalcHeatTransfer(1e-6, 0.1, 300.0, 0.0, top, s, tt, precision=_lib.PREC_MIXED_LA, info=info)
+        out[sup] = (P, info["solver"], info["refine_iters"], info["err_est"])
+    assert out[0][1] == out[1][1] == 1
+    assert abs(out[0][2] - out[1][2]) <= 1, out
+    assert abs(out[1][0] / out[0][0] - 1) < 1e-8, out
+    assert out[1][3] < 1e-6, out
+    assert L.bemgpu_ctx_set_tuning(ctx.handle, _lib.TUNE_LU_SUPER, 2) == _lib.ERR_ARG
