@@ -353,6 +353,17 @@ def run_ours(args, rank, world):
     launches = sum(L.bemgpu_ctx_launches(c) for c in lane_ctx) - launches0
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
 
+    # e2e through the public API from host buffers, right after the timed
+    # region (the same requests): each step uploads its geometry and trees
+    # from host arrays inside the timed region, submits the request to the
+    # farm and reads the spectral power back.
+    from bem_gb300 import mesh as _mesh
+    e2e = None
+    if not args.lite:
+        with ClockSampler(dev) as e2e_clk:
+            e2e = _e2e_segment(args, order, bodies, diels, ctx, farm, prec, _mesh, api, torch, a)
+        e2e["clocks"] = e2e_clk.summary()
+
     # Serving: Poisson arrivals at 80 % of the measured throughput.  A request
     # is one (gap, frequency) solve, or for the mix a sweep of `sweep`
     # frequencies over one pair of bodies, all submitted at its arrival;
@@ -394,13 +405,6 @@ def run_ours(args, rank, world):
                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                    "mean_ms": float(np.mean(lat)), "solves_per_s": solves / span, "lanes": args.lanes}
 
-    # e2e through the public API from host buffers: each step uploads its
-    # geometry and trees from host arrays inside the timed region, submits the
-    # request to the farm and reads the spectral power back.
-    from bem_gb300 import mesh as _mesh
-    e2e = None
-    if not args.lite:
-        e2e = _e2e_segment(args, order, bodies, diels, ctx, farm, prec, _mesh, api, torch, a)
 
     # The plain FP64 path on the first timed requests, through the same farm
     # (its rate is the north-star's denominator) and, request by request, the
