@@ -98,6 +98,7 @@ struct bemgpu_ctx_s {
   int64_t launches = 0;  // kernels launched by this context
   bool tc_ready = false;      // gemm_tc.cu kernels: shared-memory attribute set
   bool ex_ready = false;      // gemm_exact.cu kernels: shared-memory attribute set
+  bool perm_ready = false;    // dense.cu perm_from_ipiv_kernel: shared-memory attribute set
   bool tc_err_ready = false;  // tensor-core pipeline error flag zeroed
   bool coop_panel = true;  // LU panels in one cooperative launch (else one launch per column)
   int gemm_engine = 0;   // complex64 LU/solve GEMMs: 0 tensor cores where possible, 2 FMA pipes only

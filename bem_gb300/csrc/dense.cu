@@ -198,6 +198,41 @@ __global__ void laswp_kernel(T *A, int64_t lda, int c0, int c1, int k1, int k2, 
   }
 }
 
+// The row interchanges ipiv[0..n) (applied in order, as laswp does) as one
+// permutation: perm[i] = the row whose content ends in row i.  One CTA: ipiv
+// and the row labels in shared memory, one thread replays the swaps.
+constexpr int PERM_MAX_N = 24576;  // 2 x 96 KB of shared memory
+
+__global__ void perm_from_ipiv_kernel(const int *__restrict__ ipiv, int n, int *__restrict__ perm) {
+  extern __shared__ int perm_smem[];
+  int *pr = perm_smem, *pv = perm_smem + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    pr[i] = i;
+    pv[i] = ipiv[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int k = 0; k < n; k++) {
+      const int p = pv[k];
+      if (p != k) {
+        const int t = pr[k];
+        pr[k] = pr[p];
+        pr[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = pr[i];
+}
+
+// out[i, c] = B[perm[i], c] for complex64 column-major B (n x ncols).
+__global__ void gather_rows_c64_kernel(const float *__restrict__ B, int64_t ldb, const int *__restrict__ perm, int n,
+                                       float *__restrict__ out, int64_t ldo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c = blockIdx.y;
+  if (i >= n) return;
+  reinterpret_cast<float2 *>(out)[i + ldo * c] = reinterpret_cast<const float2 *>(B)[perm[i] + ldb * c];
+}
+
 // The same interchanges for a panel of at most LASWP_MAXW rows, as one
 // permutation: warp 0 of each CTA replays the swaps on row labels in shared
 // memory (the panel's rows and the pivot rows below it), which gives for
@@ -1533,6 +1568,35 @@ int bem_capply_inverse_identity(bemgpu_ctx_s *ctx, const float *Linv, const floa
 
 int bem_capply_inverse(bemgpu_ctx_s *ctx, const float *Linv, const float *Uinv, int n, const int *d_ipiv, float *B,
                        int64_t ldb, int nrhs, float *tmp, cudaStream_t st) {
+  const bool gather = n <= PERM_MAX_N && ctx->gemm_engine != 2 && n >= 64 && nrhs >= 64;
+  if (gather) {
+    // the interchanges as one row permutation, gathered into tmp; the two
+    // products then alternate between tmp and B, and tmp goes back to B
+    int *perm = (int *)bem_workspace(ctx, "lu_perm", sizeof(int) * (size_t)n);
+    if (!perm) return bem_fail(ctx, BEMGPU_ERR_OOM, "apply inverse: permutation");
+    if (!ctx->perm_ready) {
+      BEM_CUDA_TRY(ctx, cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(2 * sizeof(int) * PERM_MAX_N)));
+      ctx->perm_ready = true;
+    }
+    {
+      ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, 8.0 * n + 24.0 * (double)n * nrhs);
+      perm_from_ipiv_kernel<<<1, 256, 2 * sizeof(int) * (size_t)n, st>>>(d_ipiv, n, perm);
+      gather_rows_c64_kernel<<<dim3((unsigned)((n + 255) / 256), (unsigned)nrhs), 256, 0, st>>>(B, ldb, perm, n,
+                                                                                                tmp, n);
+      ctx->launches += 2;
+    }
+    BEM_CUDA_TRY(ctx, cudaGetLastError());
+    int rc = bem_cgemm_tc(ctx, BEMGPU_K_SOLVE_GEMM, n, nrhs, n, 1.f, Linv, n, tmp, n, B, ldb, TC_OUT_F32, 0, st, 1);
+    if (!rc) rc = bem_cgemm_tc(ctx, BEMGPU_K_SOLVE_GEMM, n, nrhs, n, 1.f, Uinv, n, B, ldb, tmp, n, TC_OUT_F32, 0, st, 2);
+    if (rc) return rc;
+    {
+      ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, 16.0 * (double)n * nrhs);
+      BEM_CUDA_TRY(ctx, cudaMemcpy2DAsync(B, sizeof(float) * 2 * ldb, tmp, sizeof(float) * 2 * (size_t)n,
+                                          sizeof(float) * 2 * (size_t)n, nrhs, cudaMemcpyDeviceToDevice, st));
+    }
+    return BEMGPU_OK;
+  }
   {
     ProfScope ps(ctx, BEMGPU_K_LU_PANEL, st, 0.0, 32.0 * (double)n * nrhs);
     laswp_kernel<float><<<(nrhs + 127) / 128, 128, 0, st>>>(B, ldb, 0, nrhs, 0, n, d_ipiv);
