@@ -194,6 +194,11 @@ void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::v
     std::sort(seen.begin(), seen.end());
     for (int b : seen) pairs.push_back({a, b, s->tri_gid[b] == gt ? 1 : 0, 0});
   }
+  // self pairs (no neighbour-edge correction, a shorter finish) first, so
+  // that the near-pair kernels' CTAs, which barrier after each pair couple,
+  // take couples of one kind; each pair writes its own half-pair slots, so
+  // the order does not change a result
+  std::stable_partition(pairs.begin(), pairs.end(), [](const NearPair &p) { return p.same != 0; });
 }
 
 const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
