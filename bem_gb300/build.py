@@ -1,7 +1,7 @@
 """Builds libbemgpu.so (the C-ABI library) in-tree with nvcc for sm_103a.
 
 Each translation unit compiles in parallel; the shared library links the CUDA
-runtime statically so that only the driver is needed at run time.
+runtime statically so that only the CUDA driver library is needed at run time.
 """
 from __future__ import annotations
 

@@ -10,7 +10,9 @@ This script reads the numbers out of that header and writes them as plain
 (xi1, xi2, weight) arrays; it is run by hand where the reference checkout is
 present and its output is committed.
 
-Usage: python bem_gb300/csrc/gen_quadrature.py /root/reference/src/TriangleQuadrature.h
+Usage: python bem_gb300/csrc/gen_quadrature.py [path/to/TriangleQuadrature.h]
+(default: $BEM_REFERENCE_SRC/TriangleQuadrature.h, BEM_REFERENCE_SRC defaulting
+to /root/reference/src)
 """
 import re
 import sys
@@ -71,7 +73,9 @@ def emit(rules, line15):
 
 
 if __name__ == "__main__":
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/TriangleQuadrature.h"
+    import os
+    src = sys.argv[1] if len(sys.argv) > 1 else os.path.join(
+        os.environ.get("BEM_REFERENCE_SRC", "/root/reference/src"), "TriangleQuadrature.h")
     rules, line15 = parse(open(src).read())
     dst = __file__.replace("gen_quadrature.py", "quadrature_tables.h")
     open(dst, "w").write(emit(rules, line15))

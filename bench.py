@@ -407,7 +407,7 @@ def run_ours(args, rank, world):
 
 
     # The plain FP64 path on the first timed requests, through the same farm
-    # (its rate is the north-star's denominator) and, request by request, the
+    # (the rate the mixed path is compared with) and, request by request, the
     # measured error of the timed mixed-precision results against it.
     fp64_arm, accuracy = None, None
     n64 = min(args.fp64_steps, args.steps)
