@@ -194,11 +194,41 @@ void bem_build_near_pairs(const bemgpu_tree_s *t, const bemgpu_tree_s *s, std::v
     std::sort(seen.begin(), seen.end());
     for (int b : seen) pairs.push_back({a, b, s->tri_gid[b] == gt ? 1 : 0, 0});
   }
-  // self pairs (no neighbour-edge correction, a shorter finish) first, so
-  // that the near-pair kernels' CTAs, which barrier after each pair couple,
-  // take couples of one kind; each pair writes its own half-pair slots, so
-  // the order does not change a result
-  std::stable_partition(pairs.begin(), pairs.end(), [](const NearPair &p) { return p.same != 0; });
+  // Self pairs (no neighbour-edge correction, a shorter finish) first, then
+  // coplanar pairs (every outer node takes the in-plane branch of the
+  // close-pair contraction), then the rest, so that the near-pair kernels'
+  // CTAs, which barrier after each pair couple, take couples of one kind.
+  // Each pair writes its own half-pair slots: the order changes no result.
+  auto kind = [&](const NearPair &p) {
+    if (p.same) return 0;
+    const int *ta = &g->tri[3 * (size_t)t->tri_gid[p.t]], *sb = &g->tri[3 * (size_t)s->tri_gid[p.s]];
+    const double *x = g->xyz.data();
+    auto sub = [&](int a, int b, double *o) {
+      for (int k = 0; k < 3; k++) o[k] = x[3 * (size_t)a + k] - x[3 * (size_t)b + k];
+    };
+    double e1[3], e2[3], n[3];
+    sub(sb[1], sb[0], e1);
+    sub(sb[2], sb[0], e2);
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double el = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    if (!(nn > 0)) return 2;
+    // the test triangle's vertices in the source triangle's plane (the
+    // contraction's plane test, |h| < 1e-8 of an edge, holds at every node)
+    for (int k = 0; k < 3; k++) {
+      double d[3];
+      sub(ta[k], sb[0], d);
+      if (std::fabs(d[0] * n[0] + d[1] * n[1] + d[2] * n[2]) / nn >= 1e-9 * el) return 2;
+    }
+    return 1;
+  };
+  std::vector<std::pair<int, NearPair>> keyed(pairs.size());
+  for (size_t i = 0; i < pairs.size(); i++) keyed[i] = {kind(pairs[i]), pairs[i]};
+  std::stable_sort(keyed.begin(), keyed.end(),
+                   [](const std::pair<int, NearPair> &a, const std::pair<int, NearPair> &b) { return a.first < b.first; });
+  for (size_t i = 0; i < pairs.size(); i++) pairs[i] = keyed[i].second;
 }
 
 const NearList *bem_near_list(bemgpu_ctx_s *ctx, const bemgpu_tree_s *t, const bemgpu_tree_s *s) {
