@@ -333,6 +333,10 @@ def run_ours(args, rank, world):
         for c in lane_ctx + [ctx.handle]:
             _check_rc(L.bemgpu_ctx_set_tuning(c, _lib.TUNE_PANEL_CTAS, args.panel_ctas))
         tiles = dict(tiles or {}, panel_ctas=args.panel_ctas)
+    if args.ex_wide is not None:
+        for c in lane_ctx + [ctx.handle]:
+            _check_rc(L.bemgpu_ctx_set_tuning(c, _lib.TUNE_EX_WIDE, args.ex_wide))
+        tiles = dict(tiles or {}, ex_wide=args.ex_wide)
     farm.map([job(k) for k in range(args.warmup)], precision=prec, strict=False)
     if world > 1:
         import torch.distributed as dist
@@ -926,11 +930,14 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=4,
                     help="timed requests solved again on the plain FP64 path (rate and measured error; 0: skip)")
     ap.add_argument("--subs", default="default",
-                    help="comma-separated sub-workloads summarised in the line (slab, mix, tip), 'none', or "
-                         "'default' (slab,mix for the default ico3 workload, none otherwise)")
+                    help="comma-separated sub-workloads summarised in the line (cube4, tip, slab, mix), 'none', or "
+                         "'default' (all four for the default ico3 workload, none otherwise)")
     ap.add_argument("--tune", default="cache", choices=["cache", "retune", "off"],
                     help="launch shapes from the autotuner's cache (tuned first when missing), re-tuned, or the "
                          "library defaults")
+    ap.add_argument("--ex-wide", type=int, default=None, choices=[0, 1, 2],
+                    help="exact products' 128 x 128 tiles: 0 never, 1 grids of 4 waves or more (the library's "
+                         "default), 2 always")
     ap.add_argument("--panel-ctas", type=int, default=0,
                     help="CTAs of a cooperative LU panel at most (0: one per SM)")
     ap.add_argument("--lite", action="store_true",
