@@ -12,7 +12,8 @@ Synthetic meshes from bem_gb300.mesh (seeded), no dataset.
                   [--precision fp64|mixed] [--workload ico3|ico2|cube4|tip|slab|mix] [--lanes L]
                   [--batch B] [--solver escalate|c64|fp64class] [--serve-requests R] [--sweep F]
                   [--e2e-steps K2] [--prof-steps K3] [--fp64-steps K4] [--subs LIST]
-                  [--tune cache|retune|off] [--lite] [--no-cpu-baseline]
+                  [--tune cache|retune|off] [--ex-wide 0|1|2] [--panel-ctas C] [--lite]
+                  [--no-cpu-baseline]
 
 Other workloads: cube4 (two 1 um cubes, 4x4 squares per face, N = 1152, gap
 100 nm, 20 f); tip (64 cone tips over a plate, each with a 64-frequency
