@@ -301,10 +301,12 @@ __global__ void __launch_bounds__(EX_THREADS, 1)
 // plain 4 x 4 and 3 x 3 products, whose truncation (2^-32, 2^-24 of the
 // block maxima products) is far above the 2^-40 an FP32 level 2 adds.  Per
 // 128-deep exponent block (4 TMA stages of 32-deep K steps, 64-byte rows)
-// the MMA thread issues each stage's level-3/4 products first; at a block's
-// first stage it then waits, level by level, until the epilogue has drained
-// that level of the previous block (one mbarrier per level), so the drain
-// runs under the level-3/4 products and the MMAs into levels already drained.
+// the MMA thread issues each stage's FP32-summed products (levels ZLEV and up)
+// first; at a block's first stage it then waits, level by level, until the
+// epilogue has drained that exact level of the previous block (one mbarrier
+// per level), so the drain runs under the FP32-summed products and the MMAs
+// into levels already drained.  The host takes these tiles for grids of 4
+// waves or more (a smaller grid loses more in its last wave than it gains).
 // Sixteen epilogue warps (a TMEM lane quarter and 32 columns each) drain the
 // exact levels one after the other into their two-float (hi, lo) sums in the
 // same order per entry as ex_gemm_kernel (TwoSum X0, TwoSum X1, lo += X2).
@@ -314,7 +316,7 @@ constexpr int EXW_BK = 32;
 constexpr int EXW_DRAIN = 128 / EXW_BK;  // TMA stages per exponent block
 constexpr int EXW_EPI_WARPS = 16;
 constexpr int EXW_THREADS = 64 + 32 * EXW_EPI_WARPS;
-constexpr int EXW_TMEM_COLS = 512;  // levels 0, 1, 2 and levels >= 3, 128 columns each
+constexpr int EXW_TMEM_COLS = 512;  // three exact-level buffers and the FP32 sum, 128 columns each
 constexpr int EXW_ZCOL = 3 * EXW_BN;
 
 template <int SA, int SB>
